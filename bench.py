@@ -1,0 +1,343 @@
+"""Benchmark: boosting trees/s on the 10M x 128 regression workload on GB300.
+
+Workload (the reference project's large regression configuration): 10,000,000 rows x 128
+float32 features (64 N(0,1), 32 lognormal(0,1), 32 uniform integers in [0,1000)),
+y = sum of 16 seeded random pairwise feature products + N(0, 0.5), sample weights
+U(0.5, 1.5); quantile binning to 255 bins; depth 8, learning rate 0.05, squared error,
+min_samples_leaf 20, min_child_weight 1, reg_lambda 1. A step is one boosting round
+(one tree). Data are seeded synthetic inputs of that shape and distribution.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm prints one JSON line with the whole-job trees/s measured with CUDA events on the
+backend stream (inputs resident in HBM), an end-to-end figure through the C ABI from
+pinned host buffers, the histogram kernel's roofline and a CPU baseline (the oracle's
+restatement of the reference trainer on host cores, on a bounded row sample scaled to the
+full workload). ``--impl reference`` times that CPU implementation alone.
+Under torchrun each rank trains an independent replica on its own GPU.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ROWS, FEATURES, BINS, DEPTH, LR = 10_000_000, 128, 255, 8, 0.05
+SEED = 20260719 + 2
+PARAMS = dict(max_depth=DEPTH, learning_rate=LR, min_samples_leaf=20, min_child_weight=1.0,
+              reg_lambda=1.0, max_bins=BINS)
+METRIC = "trees/s @10Mx128x255bins d8 (fixed-point batched)"
+CONFIG = {
+    "workload": "regression 10,000,000 rows x 128 features (64 normal, 32 lognormal, 32 int[0,1000)), "
+                "255 bins, depth 8, lr 0.05, weighted squared error",
+    "rows": ROWS, "features": FEATURES, "bins": BINS, "max_depth": DEPTH, "learning_rate": LR,
+    "hist": "int64 fixed-point, all frontier nodes per launch, one CUDA graph per round",
+    "l2": "inputs (1.28 GB binned matrix) exceed the 129 MB L2; no flush between steps",
+}
+
+
+def make_data(rows: int, seed: int = SEED):
+    """Feature-major float32 matrix [features, rows], labels, weights."""
+    rng = np.random.default_rng(seed)
+    xf = np.empty((FEATURES, rows), np.float32)
+    for f in range(64):
+        xf[f] = rng.standard_normal(rows, dtype=np.float32)
+    for f in range(64, 96):
+        xf[f] = np.exp(rng.standard_normal(rows, dtype=np.float32))
+    for f in range(96, 128):
+        xf[f] = rng.integers(0, 1000, rows).astype(np.float32)
+    pairs = rng.choice(FEATURES, size=(16, 2))
+    scale = np.ones(FEATURES, np.float32)
+    scale[64:96] = 1.0 / 1.65  # lognormal mean
+    scale[96:] = 1.0 / 500.0
+    y = rng.normal(0.0, 0.5, rows)
+    for a, b in pairs:
+        y += (xf[a] * scale[a]).astype(np.float64) * (xf[b] * scale[b])
+    w = rng.uniform(0.5, 1.5, rows)
+    return xf, y, w
+
+
+def sample_clocks(stop: threading.Event, out: list):
+    cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+           "--format=csv,noheader,nounits"]
+    dev = os.environ.get("LOCAL_RANK", "0")
+    while not stop.is_set():
+        try:
+            line = subprocess.run(cmd + ["-i", dev], capture_output=True, text=True, timeout=5).stdout.strip()
+            if line:
+                out.append([v.strip() for v in line.split(",")])
+        except Exception:
+            pass
+        stop.wait(0.2)
+
+
+def clocks_summary(samples):
+    if not samples:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+    sm = [float(s[1]) for s in samples if s[1].replace(".", "").isdigit()]
+    mx = [float(s[2]) for s in samples if s[2].replace(".", "").isdigit()]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({names[i] for s in samples for i in range(4) if len(s) > 4 + i and s[4 + i] == "Active"})
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons, "samples": len(samples)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(xf, y, w, sample_rows: int, trees: int):
+    """The oracle's FP64 restatement of the reference trainer on a leading row sample."""
+    import oracle
+
+    oracle.build(reference=False)
+    orc = oracle.Oracle("port")
+    x = xf[:, :sample_rows].T  # strided view, columns contiguous
+    t0 = time.perf_counter()
+    ds = orc.quantize_dense(x, BINS)
+    tq = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    orc.train_regressor(ds, y[:sample_rows], w[:sample_rows], hist_mode=oracle.HIST_FP64,
+                        n_estimators=trees, **PARAMS)
+    dt = time.perf_counter() - t0
+    per_tree_full = dt / trees * (ROWS / sample_rows)
+    return {
+        "value": 1.0 / per_tree_full, "unit": "trees/s", "cores": 1, "kind": "port",
+        "sample": f"{trees} tree(s) on the first {sample_rows:,} rows ({dt:.1f} s training, "
+                  f"{tq:.1f} s binning), time per tree scaled by rows to {ROWS:,}",
+    }
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def reduce_max(value: float, world: int) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    xf, y, w = make_data(args.ref_rows)
+    import oracle
+
+    oracle.build(reference=False)
+    orc = oracle.Oracle("port")
+    ds = orc.quantize_dense(xf.T, BINS)
+    warm = max(1, min(args.warmup, 3))
+    orc.train_regressor(ds, y, w, hist_mode=oracle.HIST_FP64, n_estimators=warm, **PARAMS)
+    t0 = time.perf_counter()
+    orc.train_regressor(ds, y, w, hist_mode=oracle.HIST_FP64, n_estimators=args.steps, **PARAMS)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt * (args.ref_rows / ROWS)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "trees/s", "n_gpus": world,
+        "steps": args.steps, "warmup": warm, "ms_per_step": dt / args.steps * 1e3 * (ROWS / args.ref_rows),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": CONFIG,
+        "cpu_baseline": {"value": value, "unit": "trees/s", "cores": 1, "kind": "port",
+                         "sample": f"each step one tree on the first {args.ref_rows:,} rows, "
+                                   f"time scaled by rows to {ROWS:,} (single-threaded, as the reference)"},
+        "e2e": {"value": value, "unit": "trees/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import mpsboost_gb300 as mb
+    from mpsboost_gb300 import _lib
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    xf, y, w = make_data(ROWS)
+    t0 = time.perf_counter()
+    binned = mb.quantize_dense(xf.T, BINS)
+    t_bin = time.perf_counter() - t0
+    backend = mb.CudaBackend(local)
+    n_rounds = args.warmup + args.steps
+    trainer = mb.Trainer(backend, binned, y, w, n_estimators=2 * n_rounds + 4, **PARAMS)
+    trainer.run(args.warmup)
+    trainer.synchronize()
+    trainer.reset_stats()
+
+    # Timed region: K rounds, CUDA events on the backend stream.
+    samples: list = []
+    stop = threading.Event()
+    sampler = threading.Thread(target=sample_clocks, args=(stop, samples), daemon=True)
+    sampler.start()
+    barrier(world)
+    backend.synchronize()
+    backend.timer_begin()
+    trainer.run(args.steps)
+    ms = backend.timer_end()
+    backend.synchronize()
+    barrier(world)
+    stop.set()
+    sampler.join()
+    trainer.synchronize()
+    st = trainer.stats()
+    ms_max = reduce_max(ms, world)
+    value = world * args.steps / (ms_max / 1e3)
+
+    # Roofline pass: the same rounds with CUDA events around every histogram launch.
+    timed = mb.Trainer(backend, binned, y, w, n_estimators=n_rounds, options=_lib.OPT_TIMING, **PARAMS)
+    timed.run(args.warmup)
+    timed.synchronize()
+    timed.reset_stats()
+    timed.run(args.steps)
+    timed.synchronize()
+    ts = timed.stats()
+    timed.close()
+    per_launch_ms = ts["hist_ms"] / max(ts["hist_timed_launches"], 1)
+    alg_bytes = ts["hist_cells"] + 12 * ts["hist_rows"]  # bins + row id + g/h per built row
+    per_launch_bytes = alg_bytes / max(ts["hist_timed_launches"], 1)
+    achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+
+    # Plain path: FP32 atomics, one histogram launch per node, host round trip per level.
+    plain_steps = max(2, args.steps // 4)
+    plain = mb.Trainer(backend, binned, y, w, n_estimators=plain_steps + 2,
+                       options=_lib.OPT_FLOAT_HIST | _lib.OPT_PER_NODE, **PARAMS)
+    plain.run(1)
+    plain.synchronize()
+    backend.timer_begin()
+    plain.run(plain_steps)
+    plain_ms = backend.timer_end()
+    plain.synchronize()
+    plain.close()
+
+    # End to end through the C ABI: pinned host buffers in, model out, K trees.
+    e2e = None
+    if rank == 0 or world > 1:
+        e2e = run_e2e(mb, backend, binned, y, w, args.steps)
+    trainer.close()
+
+    if rank != 0:
+        return
+    cpu = cpu_baseline(xf, y, w, args.cpu_rows, 1) if world == 1 and not args.no_cpu else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "trees/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": dict(CONFIG, parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                       binning_seconds=round(t_bin, 2)),
+        "gpu_launches": int(st["kernel_launches"]),
+        "e2e": e2e,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "hist_build_kernel<fixed>",
+                     "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
+                     "cells_per_s": ts["hist_cells"] / (ts["hist_ms"] / 1e3)},
+        "plain_fp32_per_node": {"value": plain_steps / (plain_ms / 1e3), "unit": "trees/s",
+                                "speedup_of_fixed_batched": value / world / (plain_steps / (plain_ms / 1e3))},
+        "cpu_baseline": cpu,
+        "clocks": clocks_summary(samples),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_e2e(mb, backend, binned, y, w, trees):
+    """One fit through mpsb_cuda_train_regressor from pinned host buffers."""
+    import ctypes as C
+
+    from mpsboost_gb300 import _lib
+
+    lib = _lib.load()
+    bins = np.ascontiguousarray(binned.bins)
+    counts = np.ascontiguousarray(binned.bin_counts, np.uint32)
+    yy = np.ascontiguousarray(y)
+    ww = np.ascontiguousarray(w)
+    pinned = [bins, yy, ww]
+    for a in pinned:
+        _lib.check(lib.mpsb_cuda_host_register(_lib.ptr(a), a.nbytes))
+    try:
+        p, keep = mb.make_params(n_estimators=trees, **PARAMS)
+        t0 = time.perf_counter()
+        ds = C.c_void_p()
+        _lib.check(lib.mpsb_cuda_dataset_create(backend.handle, _lib.ptr(bins), 1, None, binned.rows,
+                                                binned.features, _lib.ptr(counts), C.byref(ds)))
+        model = C.c_void_p()
+        _lib.check(lib.mpsb_cuda_train_regressor(backend.handle, ds, _lib.ptr(yy), _lib.ptr(ww), yy.size,
+                                                 C.byref(p), 0, C.byref(model)))
+        nodes = 0
+        for t in range(lib.mpsb_cuda_model_tree_count(model)):
+            n = lib.mpsb_cuda_model_tree_node_count(model, t)
+            out = np.empty(n, _lib.NODE_DTYPE)
+            _lib.check(lib.mpsb_cuda_model_tree_nodes(model, t, _lib.ptr(out)))
+            nodes += n
+        dt = time.perf_counter() - t0
+        lib.mpsb_cuda_model_destroy(model)
+        lib.mpsb_cuda_dataset_destroy(ds)
+        del keep
+    finally:
+        for a in pinned:
+            lib.mpsb_cuda_host_unregister(_lib.ptr(a))
+    h2d = bins.nbytes + yy.nbytes + ww.nbytes + counts.nbytes
+    d2h = nodes * _lib.NODE_DTYPE.itemsize + yy.nbytes  # trees + final training predictions
+    return {"value": trees / dt, "unit": "trees/s", "h2d_bytes_per_step": h2d // trees,
+            "d2h_bytes_per_step": d2h // trees, "seconds": dt,
+            "note": "one fit of K trees: dataset upload, training, model readback"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-rows", type=int, default=500_000)
+    ap.add_argument("--ref-rows", type=int, default=500_000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,287 @@
+/*
+ * mpsb_cuda.h -- C ABI of the GB300 (sm_103a) CUDA backend for the MPSBoost GBDT
+ * training hot path: gradient/hessian -> histogram build (+ sibling subtraction) ->
+ * split-gain scan -> row partition.
+ *
+ * Plain pointers and sizes only. Every entry returns 0 on success or an error code
+ * (MPSB_ERR_*) and leaves a thread-local message for mpsb_cuda_last_error(). The error
+ * classes mirror the reference's exceptions: TrainingError (objective.hpp:17-20),
+ * DataError (binned_dataset.hpp:18-21) and BackendError (backend.hpp:22-25).
+ *
+ * Reference interfaces each entry replaces (paths inside the reference project):
+ *   mpsb_cuda_backend_create/destroy   MpsBackend::MpsBackend / ~MpsBackend
+ *                                      (include/mpsboost/backend.hpp:140-150)
+ *   mpsb_cuda_backend_info             QueryBackendInfo (backend.hpp:197-200)
+ *   mpsb_quantize_dense                QuantizeDense (binned_dataset.hpp:137-138)
+ *   mpsb_transform_dense               TransformDense (binned_dataset.hpp:140-144)
+ *   mpsb_cuda_dataset_create           the per-node NewBuffer(dataset.bin_data())
+ *                                      upload of src/mps/mps_histogram.mm:149, made
+ *                                      once per dataset and kept resident
+ *   mpsb_cuda_squared_error            GradientComputer::ComputeSquaredError
+ *                                      (backend.hpp:52-58)
+ *   mpsb_cuda_build_histograms         HistogramBuilder::BuildHistograms
+ *                                      (backend.hpp:64-75)
+ *   mpsb_cuda_build_layer_histograms   LayerHistogramBuilder::BuildLayerHistograms
+ *                                      (backend.hpp:124-135)
+ *   mpsb_cuda_scan_splits              MpsBackend::ScanSplitsForTest
+ *                                      (backend.hpp:173-180), with the full
+ *                                      FindBestSplit semantics (tree_split.cpp:142-234)
+ *   mpsb_cuda_partition_rows           MpsBackend::PartitionRowsForTest
+ *                                      (backend.hpp:181-185), with missing rows
+ *                                      routed by default_left (tree_split.cpp:273-285)
+ *   mpsb_cuda_train_regressor          TrainRegressionModel (trainer.hpp:133-139) as
+ *                                      called by _train_regressor_mps
+ *                                      (src/python/binding_model.cpp:34-45)
+ *   mpsb_cuda_train_ovr                the one-vs-rest fit of
+ *                                      src/mpsboost/estimators/multiclass.py:113-160
+ *   mpsb_cuda_model_create             RegressionModel::Restore (trainer.hpp:271-279)
+ *   mpsb_cuda_model_predict            RegressionModel::Predict (trainer.hpp:266-269)
+ *   mpsb_cuda_trainer_*                the same training loop as a session with
+ *                                      device-resident inputs (benchmarks, timing)
+ */
+#ifndef MPSB_CUDA_H
+#define MPSB_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPSB_CUDA_ABI_VERSION 1
+
+enum {
+  MPSB_OK = 0,
+  MPSB_ERR_TRAINING = 1, /* contract / math violation (TrainingError) */
+  MPSB_ERR_DATA = 2,     /* input data violation (DataError) */
+  MPSB_ERR_BACKEND = 3,  /* CUDA runtime / device failure (BackendError) */
+  MPSB_ERR_UNSUPPORTED = 4
+};
+
+/* Objectives: TrainingParameters::Objective (trainer.hpp:21-27). */
+enum { MPSB_SQUARED_ERROR = 0, MPSB_BINARY_LOGISTIC = 1, MPSB_QUANTILE = 2,
+       MPSB_POISSON = 3, MPSB_TWEEDIE = 4 };
+
+/* Histogram arithmetic. FIXED: FP32 g/h quantized per round to int64 with a power-of-two
+   scale from max|g| and max h; exact, order-independent, deterministic sums. FLOAT: plain
+   FP32 shared-memory atomics flushed into FP64 node histograms. */
+enum { MPSB_HIST_FIXED = 0, MPSB_HIST_FLOAT = 1 };
+
+/* Trainer option bits. */
+enum {
+  MPSB_OPT_FLOAT_HIST = 1u << 0, /* use MPSB_HIST_FLOAT */
+  MPSB_OPT_NO_GRAPH = 1u << 1,   /* launch each round's kernels directly (no CUDA graph) */
+  MPSB_OPT_PER_NODE = 1u << 2,   /* one histogram launch per node and a host round trip
+                                    per level: the shape of mps_histogram.mm:62-80 */
+  MPSB_OPT_TIMING = 1u << 3      /* CUDA events around every histogram launch */
+};
+
+/* TrainingParameters + TreeTrainingParameters (trainer.hpp:20-36, tree.hpp:47-72). */
+typedef struct {
+  uint32_t n_estimators;
+  uint32_t max_bins;
+  uint32_t objective;
+  uint32_t max_depth;
+  uint32_t max_leaves;
+  uint32_t max_active_leaves;
+  uint32_t split_strategy;  /* 0 best_gain, 1 random_threshold */
+  uint32_t growth_strategy; /* 0 level_wise (1 leaf_wise is not provided here) */
+  uint32_t random_seed;
+  uint32_t n_monotonic;
+  uint32_t n_interaction_groups;
+  uint32_t reserved;
+  uint64_t min_samples_leaf;
+  double learning_rate;
+  double objective_alpha;
+  double tweedie_variance_power;
+  double min_child_weight;
+  double reg_lambda;
+  double reg_alpha;
+  double max_delta_step;
+  double gamma;
+  double min_gain_to_split;
+  const int8_t* monotonic_constraints;  /* n_monotonic entries or NULL */
+  const uint32_t* interaction_offsets;  /* n_interaction_groups + 1 entries */
+  const uint32_t* interaction_features; /* concatenated groups */
+} mpsb_train_params;
+
+/* TreeNode (tree.hpp:31-42); 40 bytes. */
+typedef struct {
+  uint32_t feature_index;
+  uint32_t threshold_bin;
+  uint32_t left_child;
+  uint32_t right_child;
+  double leaf_value;
+  double gain;
+  uint8_t default_left;
+  uint8_t flags; /* bit 0: leaf */
+  uint8_t reserved[6];
+} mpsb_tree_node;
+
+/* HistogramBin (backend.hpp:40-44). */
+typedef struct {
+  uint64_t count;
+  double gradient_sum;
+  double hessian_sum;
+} mpsb_histogram_bin;
+
+/* SplitScanCandidate (backend.hpp:108-119) plus the chosen missing direction. */
+typedef struct {
+  uint32_t valid;
+  uint32_t feature;
+  uint32_t threshold_bin;
+  uint32_t default_left;
+  uint64_t left_count;
+  uint64_t right_count;
+  double left_gradient_sum;
+  double left_hessian_sum;
+  double right_gradient_sum;
+  double right_hessian_sum;
+  double gain;
+} mpsb_split_candidate;
+
+/* BackendInfo (backend.hpp:30-35) plus the device facts the kernels are sized by. */
+typedef struct {
+  uint32_t available;
+  uint32_t sm_count;
+  uint32_t cc_major;
+  uint32_t cc_minor;
+  uint64_t total_memory;
+  char device_name[96];
+} mpsb_cuda_info;
+
+/* Per-kernel accounting of a trainer session (what one launch list shows). */
+typedef struct {
+  uint64_t rounds;
+  uint64_t kernel_launches;    /* kernels of this library enqueued (graph nodes counted
+                                  once per replay) */
+  uint64_t hist_launches;      /* histogram-build launches */
+  uint64_t hist_cells;         /* row x feature cells accumulated by histogram builds */
+  uint64_t hist_rows;          /* rows gathered by histogram builds */
+  double hist_ms;              /* summed CUDA-event time of histogram builds
+                                  (MPSB_OPT_TIMING only) */
+  uint64_t hist_timed_launches;
+} mpsb_cuda_stats;
+
+typedef struct mpsb_cuda_backend mpsb_cuda_backend;
+typedef struct mpsb_cuda_dataset mpsb_cuda_dataset;
+typedef struct mpsb_cuda_model mpsb_cuda_model;
+typedef struct mpsb_cuda_trainer mpsb_cuda_trainer;
+
+const char* mpsb_cuda_last_error(void);
+int mpsb_cuda_abi_version(void);
+
+/* ---- backend ------------------------------------------------------------------- */
+int mpsb_cuda_backend_create(int device, mpsb_cuda_backend** out);
+void mpsb_cuda_backend_destroy(mpsb_cuda_backend* backend);
+int mpsb_cuda_backend_info(const mpsb_cuda_backend* backend, mpsb_cuda_info* out);
+/* Histogram arithmetic of the node-level entries below (MPSB_HIST_*); default FIXED. */
+int mpsb_cuda_backend_set_hist_mode(mpsb_cuda_backend* backend, int mode);
+/* CUDA-event timer on the backend's stream. */
+int mpsb_cuda_timer_begin(mpsb_cuda_backend* backend);
+int mpsb_cuda_timer_end(mpsb_cuda_backend* backend, float* milliseconds);
+int mpsb_cuda_synchronize(mpsb_cuda_backend* backend);
+/* Page-lock (pin) / release a caller-owned host buffer so copies from it run at full
+   host-link bandwidth. */
+int mpsb_cuda_host_register(void* ptr, uint64_t bytes);
+int mpsb_cuda_host_unregister(void* ptr);
+
+/* ---- binning (host) ------------------------------------------------------------- */
+/* Quantile binning with the reference's semantics. scalar_type: 1 float32, 2 float64.
+   Outputs are caller-allocated: bins [features*rows] feature-major (uint8 when
+   max_bins <= 256, else uint16), missing [features*rows] (0/1), boundaries
+   [features*(max_bins-1)] (used prefix = sum of boundary_count), boundary_offset,
+   boundary_count, bin_count, missing_count [features]. n_threads 0 = all host cores. */
+int mpsb_quantize_dense(const void* data, int scalar_type, uint64_t rows, uint32_t features,
+                        uint64_t row_stride_bytes, uint64_t column_stride_bytes,
+                        uint32_t max_bins, uint32_t n_threads, void* bins, uint8_t* missing,
+                        float* boundaries, uint64_t* boundary_offset,
+                        uint32_t* boundary_count, uint32_t* bin_count,
+                        uint64_t* missing_count);
+/* Apply an existing schema (boundaries/offsets/counts of mpsb_quantize_dense). */
+int mpsb_transform_dense(const void* data, int scalar_type, uint64_t rows, uint32_t features,
+                         uint64_t row_stride_bytes, uint64_t column_stride_bytes,
+                         uint32_t max_bins, const float* boundaries,
+                         const uint64_t* boundary_offset, const uint32_t* boundary_count,
+                         uint32_t n_threads, void* bins, uint8_t* missing);
+
+/* ---- device-resident dataset ------------------------------------------------------ */
+/* bins: feature-major [features*rows], bin_width_bytes 1 or 2; missing may be NULL.
+   Each feature needs bin_count <= 256, and <= 255 when it has missing rows. */
+int mpsb_cuda_dataset_create(mpsb_cuda_backend* backend, const void* bins,
+                             uint32_t bin_width_bytes, const uint8_t* missing,
+                             uint64_t rows, uint32_t features, const uint32_t* bin_count,
+                             mpsb_cuda_dataset** out);
+void mpsb_cuda_dataset_destroy(mpsb_cuda_dataset* dataset);
+
+/* ---- node-level entries (the backend.hpp contract) ----------------------------------- */
+int mpsb_cuda_squared_error(mpsb_cuda_backend* backend, const double* labels,
+                            const double* predictions, uint64_t n, double* out_pairs);
+/* pairs: [n_pairs][2] FP64 (GradientPair); out: features x bin_count bins; missing rows
+   are counted in bin 0 as in the reference. */
+int mpsb_cuda_build_histograms(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                               const uint64_t* rows, uint64_t n_rows, const double* pairs,
+                               uint64_t n_pairs, mpsb_histogram_bin* out);
+/* node_offsets: n_nodes+1 offsets into rows; out: n_nodes blocks of features x bin_count. */
+int mpsb_cuda_build_layer_histograms(mpsb_cuda_backend* backend,
+                                     const mpsb_cuda_dataset* dataset, const uint64_t* rows,
+                                     const uint64_t* node_offsets, uint32_t n_nodes,
+                                     const double* pairs, uint64_t n_pairs,
+                                     mpsb_histogram_bin* out);
+int mpsb_cuda_scan_splits(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                          const uint64_t* rows, uint64_t n_rows, const double* pairs,
+                          uint64_t n_pairs, const mpsb_train_params* params,
+                          mpsb_split_candidate* out_per_feature);
+int mpsb_cuda_partition_rows(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                             const uint64_t* rows, uint64_t n_rows, uint32_t feature,
+                             uint32_t threshold_bin, int default_left, uint64_t* left_out,
+                             uint64_t* right_out, uint64_t* n_left);
+
+/* ---- training ------------------------------------------------------------------ */
+/* weights may be NULL (unit weights). options: MPSB_OPT_* bits. */
+int mpsb_cuda_train_regressor(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                              const double* labels, const double* weights, uint64_t n,
+                              const mpsb_train_params* params, uint32_t options,
+                              mpsb_cuda_model** out);
+/* K binary-logistic models on labels (class ids 0..K-1), all K trees of a round built in
+   the same launches. out receives K models. */
+int mpsb_cuda_train_ovr(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                        const double* labels, const double* weights, uint64_t n,
+                        uint32_t n_classes, const mpsb_train_params* params,
+                        uint32_t options, mpsb_cuda_model** out);
+/* A model from host trees (e.g. one loaded from a file): base_score + learning_rate *
+   sum of trees, node_counts[n_trees], nodes concatenated tree by tree. */
+int mpsb_cuda_model_create(double base_score, double learning_rate, uint32_t n_trees,
+                           const uint32_t* node_counts, const mpsb_tree_node* nodes,
+                           mpsb_cuda_model** out);
+uint32_t mpsb_cuda_model_tree_count(const mpsb_cuda_model* model);
+double mpsb_cuda_model_base_score(const mpsb_cuda_model* model);
+double mpsb_cuda_model_learning_rate(const mpsb_cuda_model* model);
+uint32_t mpsb_cuda_model_tree_node_count(const mpsb_cuda_model* model, uint32_t tree);
+int mpsb_cuda_model_tree_nodes(const mpsb_cuda_model* model, uint32_t tree,
+                               mpsb_tree_node* out);
+/* Final FP64 training predictions (base + lr * sum of leaves) kept by the trainer. */
+int mpsb_cuda_model_train_predictions(const mpsb_cuda_model* model, double* out);
+int mpsb_cuda_model_predict(mpsb_cuda_backend* backend, const mpsb_cuda_model* model,
+                            const mpsb_cuda_dataset* dataset, double* out);
+void mpsb_cuda_model_destroy(mpsb_cuda_model* model);
+
+/* ---- training session (device-resident inputs; benchmarks) ---------------------------- */
+int mpsb_cuda_trainer_create(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                             const double* labels, const double* weights, uint64_t n,
+                             const mpsb_train_params* params, uint32_t options,
+                             mpsb_cuda_trainer** out);
+/* Enqueue `rounds` boosting rounds on the backend stream (asynchronous). */
+int mpsb_cuda_trainer_run(mpsb_cuda_trainer* trainer, uint32_t rounds);
+/* Wait for the stream and report any device-side error. */
+int mpsb_cuda_trainer_synchronize(mpsb_cuda_trainer* trainer);
+int mpsb_cuda_trainer_stats(const mpsb_cuda_trainer* trainer, mpsb_cuda_stats* out);
+int mpsb_cuda_trainer_reset_stats(mpsb_cuda_trainer* trainer);
+int mpsb_cuda_trainer_export(mpsb_cuda_trainer* trainer, mpsb_cuda_model** out);
+void mpsb_cuda_trainer_destroy(mpsb_cuda_trainer* trainer);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,37 @@
+"""GB300 (sm_103a) CUDA backend for the MPSBoost GBDT training hot path.
+
+gradient/hessian -> histogram build (+ sibling subtraction) -> split-gain scan -> row
+partition, behind the reference's backend contract (include/mpsboost/backend.hpp) and
+exposed through the C ABI in ``include/mpsb_cuda.h``. See ``backend`` for the Python
+mirror of the reference's native interface and ``estimators`` for the sklearn-style
+estimators with ``device="cuda"``.
+"""
+
+from ._lib import BackendError, DataError, TrainingError, UnsupportedError
+from .backend import (
+    DEFAULT_PARAMS,
+    BinnedDataset,
+    CudaBackend,
+    RegressionModel,
+    Trainer,
+    make_params,
+    quantize_dense,
+    train_ovr,
+    train_regressor,
+)
+
+__all__ = [
+    "BackendError",
+    "BinnedDataset",
+    "CudaBackend",
+    "DataError",
+    "DEFAULT_PARAMS",
+    "RegressionModel",
+    "Trainer",
+    "TrainingError",
+    "UnsupportedError",
+    "make_params",
+    "quantize_dense",
+    "train_ovr",
+    "train_regressor",
+]

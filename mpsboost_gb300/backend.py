@@ -1,0 +1,535 @@
+"""Python host mirror of the reference's native interface for the training hot path.
+
+Names and argument meaning follow the reference's pybind11 module (``_native``) and its
+C++ types:
+
+* :func:`quantize_dense` / :meth:`BinnedDataset.transform` -- ``_quantize_dense``
+  (src/python/binding_dataset.cpp), QuantizeDense / TransformDense
+  (include/mpsboost/binned_dataset.hpp:137-144).
+* :class:`CudaBackend` -- ``_MpsBackend`` (src/python/binding_backend.cpp:18-84):
+  ``gradients``, ``histograms``, ``layer_histograms``, ``split_candidates``,
+  ``partition_rows``, plus the device-resident :meth:`CudaBackend.dataset`.
+* :func:`train_regressor` -- ``_train_regressor_mps`` (src/python/binding_model.cpp:34-45)
+  over TrainRegressionModel (include/mpsboost/trainer.hpp:133-139).
+* :func:`train_ovr` -- the one-vs-rest multiclass fit of
+  src/mpsboost/estimators/multiclass.py:113-160, all K trees of a round in one launch.
+
+Every device computation runs in ``libmpsb_cuda.so``; nothing here computes on the CPU
+except binning (which the reference also does on the CPU) and the argument checks.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import HIST_DTYPE, NODE_DTYPE, SPLIT_DTYPE, TrainParams, check, ptr
+
+OBJECTIVES = {"squared_error": 0, "binary_logistic": 1, "quantile": 2, "poisson": 3, "tweedie": 4}
+
+# C++ defaults of TrainingParameters / TreeTrainingParameters (trainer.hpp:29-35,
+# tree.hpp:57-71).
+DEFAULT_PARAMS = dict(
+    n_estimators=100,
+    learning_rate=0.1,
+    max_bins=256,
+    objective="squared_error",
+    max_depth=6,
+    max_leaves=0,
+    max_active_leaves=0,
+    min_samples_leaf=1,
+    min_child_weight=0.0,
+    reg_lambda=1.0,
+    reg_alpha=0.0,
+    max_delta_step=0.0,
+    gamma=0.0,
+    min_gain_to_split=0.0,
+    split_strategy="best_gain",
+    growth_strategy="level_wise",
+    random_seed=0,
+    objective_alpha=0.5,
+    tweedie_variance_power=1.5,
+    monotonic_constraints=None,
+    interaction_constraints=None,
+)
+
+
+def make_params(**overrides) -> tuple[TrainParams, list]:
+    """``(TrainParams, keepalive)`` from keyword overrides of :data:`DEFAULT_PARAMS`."""
+
+    unknown = set(overrides) - set(DEFAULT_PARAMS)
+    if unknown:
+        raise ValueError(f"unknown parameter(s): {sorted(unknown)}")
+    v = dict(DEFAULT_PARAMS, **overrides)
+    p = TrainParams()
+    for name in (
+        "n_estimators", "max_bins", "max_depth", "max_leaves", "max_active_leaves",
+        "random_seed", "min_samples_leaf", "learning_rate", "objective_alpha",
+        "tweedie_variance_power", "min_child_weight", "reg_lambda", "reg_alpha",
+        "max_delta_step", "gamma", "min_gain_to_split",
+    ):
+        setattr(p, name, v[name])
+    obj = v["objective"]
+    if isinstance(obj, str):
+        if obj not in OBJECTIVES:
+            raise ValueError("unknown training objective")
+        obj = OBJECTIVES[obj]
+    p.objective = obj
+    try:
+        p.split_strategy = {"best_gain": 0, "random_threshold": 1}[v["split_strategy"]]
+        p.growth_strategy = {"level_wise": 0, "leaf_wise": 1}[v["growth_strategy"]]
+    except KeyError as exc:
+        raise ValueError(f"unknown split or growth strategy: {exc}") from None
+    keep: list = []
+    if v["monotonic_constraints"] is not None:
+        mono = np.ascontiguousarray(v["monotonic_constraints"], dtype=np.int8)
+        keep.append(mono)
+        p.n_monotonic = mono.size
+        p.monotonic_constraints = mono.ctypes.data_as(C.POINTER(C.c_int8))
+    if v["interaction_constraints"]:
+        groups = [list(g) for g in v["interaction_constraints"]]
+        offsets = np.cumsum([0] + [len(g) for g in groups]).astype(np.uint32)
+        feats = np.asarray([f for g in groups for f in g] or [0], dtype=np.uint32)
+        keep += [offsets, feats]
+        p.n_interaction_groups = len(groups)
+        p.interaction_offsets = offsets.ctypes.data_as(C.POINTER(C.c_uint32))
+        p.interaction_features = feats.ctypes.data_as(C.POINTER(C.c_uint32))
+    return p, keep
+
+
+# --------------------------------------------------------------------------------------
+# Binning (host, reference semantics)
+# --------------------------------------------------------------------------------------
+@dataclass
+class BinnedDataset:
+    """Feature-major bins + missing mask + frozen schema (binned_dataset.hpp:81-126)."""
+
+    rows: int
+    features: int
+    max_bins: int
+    bins: np.ndarray  # [features, rows] uint8 (max_bins <= 256) or uint16
+    missing: np.ndarray  # [features, rows] bool
+    boundaries_flat: np.ndarray
+    boundary_offsets: np.ndarray
+    boundary_counts: np.ndarray
+    bin_counts: np.ndarray
+    missing_counts: np.ndarray
+    _device: dict = field(default_factory=dict, repr=False)
+
+    @property
+    def boundaries(self) -> list[list[float]]:
+        return [
+            self.boundaries_flat[o : o + c].tolist()
+            for o, c in zip(self.boundary_offsets, self.boundary_counts)
+        ]
+
+    @property
+    def bin_width(self) -> int:
+        return 8 if self.max_bins <= 256 else 16
+
+    def transform(self, matrix, n_threads: int = 0) -> "BinnedDataset":
+        """Bin new data with this schema (TransformDense, binned_dataset.cpp:190-238)."""
+
+        x, st = _as_matrix(matrix)
+        if x.shape[1] != self.features:
+            raise _lib.DataError("Prediction input feature count does not match the binned schema")
+        rows, feats = x.shape
+        wide = self.max_bins > 256
+        bins = np.empty((feats, rows), np.uint16 if wide else np.uint8)
+        missing = np.empty((feats, rows), np.uint8)
+        lib = _lib.load()
+        bnd = np.ascontiguousarray(self.boundaries_flat, np.float32)
+        check(
+            lib.mpsb_transform_dense(
+                ptr(x), st, rows, feats, x.strides[0], x.strides[1], self.max_bins, ptr(bnd),
+                ptr(self.boundary_offsets), ptr(self.boundary_counts), n_threads, ptr(bins), ptr(missing),
+            )
+        )
+        return BinnedDataset(
+            rows, feats, self.max_bins, bins, missing.astype(bool), self.boundaries_flat,
+            self.boundary_offsets, self.boundary_counts, self.bin_counts,
+            missing.sum(axis=1).astype(np.uint64),
+        )
+
+
+def _as_matrix(matrix) -> tuple[np.ndarray, int]:
+    x = np.asarray(matrix)
+    if x.dtype not in (np.float32, np.float64):
+        x = x.astype(np.float32)
+    if x.ndim != 2:
+        raise _lib.DataError("Input matrix must be two-dimensional")
+    if x.shape[0] == 0 or x.shape[1] == 0:
+        raise _lib.DataError("Input matrix must contain at least one row and one feature")
+    if min(x.strides) < x.itemsize:  # broadcast or reversed views: read a dense copy
+        x = np.ascontiguousarray(x)
+    return x, 1 if x.dtype == np.float32 else 2
+
+
+def quantize_dense(matrix, max_bins: int = 256, n_threads: int = 0) -> BinnedDataset:
+    """Quantile-bin a float32/float64 matrix (QuantizeDense, binned_dataset.cpp:126-188)."""
+
+    x, st = _as_matrix(matrix)
+    rows, feats = x.shape
+    if not 2 <= max_bins <= 65536:
+        raise _lib.DataError("max_bins must be in [2, 65536]")
+    wide = max_bins > 256
+    bins = np.empty((feats, rows), np.uint16 if wide else np.uint8)
+    missing = np.empty((feats, rows), np.uint8)
+    bnd = np.empty(max(feats * (max_bins - 1), 1), np.float32)
+    off = np.empty(feats, np.uint64)
+    cnt = np.empty(feats, np.uint32)
+    binc = np.empty(feats, np.uint32)
+    miss = np.empty(feats, np.uint64)
+    lib = _lib.load()
+    check(
+        lib.mpsb_quantize_dense(
+            ptr(x), st, rows, feats, x.strides[0], x.strides[1], max_bins, n_threads, ptr(bins),
+            ptr(missing), ptr(bnd), ptr(off), ptr(cnt), ptr(binc), ptr(miss),
+        )
+    )
+    total = int(cnt.sum())
+    return BinnedDataset(rows, feats, max_bins, bins, missing.astype(bool), bnd[:total].copy(), off, cnt, binc, miss)
+
+
+# --------------------------------------------------------------------------------------
+# Backend
+# --------------------------------------------------------------------------------------
+class DeviceDataset:
+    """A binned dataset resident in HBM (column-blocked u8, missing at slot 255)."""
+
+    def __init__(self, backend: "CudaBackend", binned: BinnedDataset):
+        lib = _lib.load()
+        self.backend = backend
+        self.binned = binned
+        self.rows = binned.rows
+        self.features = binned.features
+        bins = np.ascontiguousarray(binned.bins)
+        missing = np.ascontiguousarray(binned.missing, dtype=np.uint8) if binned.missing.any() else None
+        counts = np.ascontiguousarray(binned.bin_counts, dtype=np.uint32)
+        handle = C.c_void_p()
+        check(
+            lib.mpsb_cuda_dataset_create(
+                backend.handle, ptr(bins), bins.dtype.itemsize, ptr(missing), binned.rows,
+                binned.features, ptr(counts), C.byref(handle),
+            )
+        )
+        self.handle = handle
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            _lib.load().mpsb_cuda_dataset_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CudaBackend:
+    """One GB300 and one CUDA stream (MpsBackend, backend.hpp:140-195)."""
+
+    def __init__(self, device: int = 0, hist_mode: str = "fixed"):
+        lib = _lib.load()
+        handle = C.c_void_p()
+        check(lib.mpsb_cuda_backend_create(device, C.byref(handle)))
+        self.handle = handle
+        self.set_hist_mode(hist_mode)
+
+    def set_hist_mode(self, mode: str) -> None:
+        code = {"fixed": _lib.HIST_FIXED, "float": _lib.HIST_FLOAT}[mode]
+        check(_lib.load().mpsb_cuda_backend_set_hist_mode(self.handle, code))
+        self.hist_mode = mode
+
+    @property
+    def info(self) -> dict:
+        inf = _lib.Info()
+        check(_lib.load().mpsb_cuda_backend_info(self.handle, C.byref(inf)))
+        return {
+            "available": bool(inf.available),
+            "device_name": inf.device_name.decode(),
+            "sm_count": inf.sm_count,
+            "compute_capability": (inf.cc_major, inf.cc_minor),
+            "total_memory": inf.total_memory,
+        }
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            _lib.load().mpsb_cuda_backend_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- datasets ------------------------------------------------------------------------
+    def dataset(self, binned: BinnedDataset) -> DeviceDataset:
+        key = id(self)
+        dev = binned._device.get(key)
+        if dev is None:
+            dev = DeviceDataset(self, binned)
+            binned._device[key] = dev
+        return dev
+
+    # -- node-level entries (binding_backend.cpp:19-71) ----------------------------------
+    def gradients(self, labels, predictions) -> np.ndarray:
+        """Squared-error pairs ``[n, 2]`` (GradientComputer::ComputeSquaredError)."""
+
+        y = np.ascontiguousarray(labels, dtype=np.float64)
+        p = np.ascontiguousarray(predictions, dtype=np.float64)
+        if y.size == 0:
+            raise _lib.TrainingError("Labels must not be empty")
+        if y.size != p.size:
+            raise _lib.TrainingError("Label and prediction lengths do not match")
+        out = np.empty((y.size, 2), np.float64)
+        check(_lib.load().mpsb_cuda_squared_error(self.handle, ptr(y), ptr(p), y.size, ptr(out)))
+        return out
+
+    def histograms_from_pairs(self, dataset: BinnedDataset, pairs, rows) -> list[np.ndarray]:
+        """Per-feature HistogramBin arrays of one node (HistogramBuilder::BuildHistograms)."""
+
+        return self.layer_histograms(dataset, pairs, [rows])[0]
+
+    def layer_histograms(self, dataset: BinnedDataset, pairs, node_rows) -> list[list[np.ndarray]]:
+        """All nodes of a layer in one launch (LayerHistogramBuilder::BuildLayerHistograms)."""
+
+        dev = self.dataset(dataset)
+        g = np.ascontiguousarray(pairs, dtype=np.float64).reshape(-1, 2)
+        parts = [np.ascontiguousarray(r, dtype=np.uint64).ravel() for r in node_rows]
+        if not parts:
+            return []
+        rows = np.concatenate(parts) if parts else np.empty(0, np.uint64)
+        offsets = np.cumsum([0] + [p.size for p in parts]).astype(np.uint64)
+        per_node = int(dataset.bin_counts.sum())
+        out = np.empty(per_node * len(parts), HIST_DTYPE)
+        check(
+            _lib.load().mpsb_cuda_build_layer_histograms(
+                self.handle, dev.handle, ptr(rows), ptr(offsets), len(parts), ptr(g), g.shape[0], ptr(out)
+            )
+        )
+        splits = np.cumsum(dataset.bin_counts)[:-1]
+        return [np.split(out[i * per_node : (i + 1) * per_node], splits) for i in range(len(parts))]
+
+    def histograms(self, dataset: BinnedDataset, labels, predictions, rows) -> dict:
+        """The reference hook's shape: squared-error pairs, then one node's histograms."""
+
+        pairs = self.gradients(labels, predictions)
+        return {"histograms": self.histograms_from_pairs(dataset, pairs, rows)}
+
+    def split_candidates_from_pairs(self, dataset: BinnedDataset, pairs, rows, **params) -> np.ndarray:
+        dev = self.dataset(dataset)
+        g = np.ascontiguousarray(pairs, dtype=np.float64).reshape(-1, 2)
+        r = np.ascontiguousarray(rows, dtype=np.uint64)
+        p, keep = make_params(**params)
+        out = np.empty(dataset.features, SPLIT_DTYPE)
+        check(
+            _lib.load().mpsb_cuda_scan_splits(
+                self.handle, dev.handle, ptr(r), r.size, ptr(g), g.shape[0], C.byref(p), ptr(out)
+            )
+        )
+        del keep
+        return out
+
+    def split_candidates(self, dataset, labels, predictions, rows, *, min_samples_leaf=1,
+                         min_child_weight=0.0, reg_lambda=1.0, gamma=0.0) -> np.ndarray:
+        """Best split per feature of one node (ScanSplitsForTest, backend.hpp:173-180)."""
+
+        pairs = self.gradients(labels, predictions)
+        return self.split_candidates_from_pairs(
+            dataset, pairs, rows, min_samples_leaf=min_samples_leaf,
+            min_child_weight=min_child_weight, reg_lambda=reg_lambda, gamma=gamma,
+        )
+
+    def partition_rows(self, dataset: BinnedDataset, rows, feature: int, threshold: int,
+                       default_left: bool = True) -> tuple[list[int], list[int]]:
+        """Stable left/right split of node rows (PartitionRowsForTest, backend.hpp:181-185)."""
+
+        dev = self.dataset(dataset)
+        r = np.ascontiguousarray(rows, dtype=np.uint64)
+        left = np.empty(max(r.size, 1), np.uint64)
+        right = np.empty(max(r.size, 1), np.uint64)
+        nl = C.c_uint64()
+        check(
+            _lib.load().mpsb_cuda_partition_rows(
+                self.handle, dev.handle, ptr(r), r.size, feature, threshold, int(bool(default_left)),
+                ptr(left), ptr(right), C.byref(nl),
+            )
+        )
+        return left[: nl.value].tolist(), right[: r.size - nl.value].tolist()
+
+    # -- timing ----------------------------------------------------------------------------
+    def timer_begin(self) -> None:
+        check(_lib.load().mpsb_cuda_timer_begin(self.handle))
+
+    def timer_end(self) -> float:
+        ms = C.c_float()
+        check(_lib.load().mpsb_cuda_timer_end(self.handle, C.byref(ms)))
+        return float(ms.value)
+
+    def synchronize(self) -> None:
+        check(_lib.load().mpsb_cuda_synchronize(self.handle))
+
+
+# --------------------------------------------------------------------------------------
+# Models and training
+# --------------------------------------------------------------------------------------
+@dataclass
+class RegressionModel:
+    """base_score + learning_rate * sum of flat trees (RegressionModel, trainer.hpp:37-76)."""
+
+    base_score: float
+    learning_rate: float
+    trees: list
+    train_predictions: np.ndarray | None = None
+
+    @classmethod
+    def _from_handle(cls, handle) -> "RegressionModel":
+        lib = _lib.load()
+        trees = []
+        for t in range(lib.mpsb_cuda_model_tree_count(handle)):
+            nodes = np.empty(lib.mpsb_cuda_model_tree_node_count(handle, t), NODE_DTYPE)
+            check(lib.mpsb_cuda_model_tree_nodes(handle, t, ptr(nodes)))
+            trees.append(nodes)
+        model = cls(lib.mpsb_cuda_model_base_score(handle), lib.mpsb_cuda_model_learning_rate(handle), trees)
+        return model
+
+    def predict(self, backend: CudaBackend, dataset: BinnedDataset) -> np.ndarray:
+        """Device batch prediction over a binned dataset with the training schema."""
+
+        lib = _lib.load()
+        dev = backend.dataset(dataset)
+        handle = self._handle(lib)
+        out = np.empty(dataset.rows, np.float64)
+        try:
+            check(lib.mpsb_cuda_model_predict(backend.handle, handle, dev.handle, ptr(out)))
+        finally:
+            lib.mpsb_cuda_model_destroy(handle)
+        return out
+
+    def _handle(self, lib):
+        counts = np.asarray([len(t) for t in self.trees], np.uint32)
+        nodes = np.concatenate(self.trees) if self.trees else np.empty(0, NODE_DTYPE)
+        nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+        h = C.c_void_p()
+        check(lib.mpsb_cuda_model_create(self.base_score, self.learning_rate, len(self.trees),
+                                         ptr(counts), ptr(nodes), C.byref(h)))
+        return h
+
+
+def _train(backend, dataset, labels, weights, options, n_classes, **params):
+    dev = backend.dataset(dataset)
+    y = np.ascontiguousarray(labels, dtype=np.float64)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    params.setdefault("max_bins", dataset.max_bins)
+    p, keep = make_params(**params)
+    lib = _lib.load()
+    if n_classes:
+        handles = (C.c_void_p * n_classes)()
+        check(lib.mpsb_cuda_train_ovr(backend.handle, dev.handle, ptr(y), ptr(w), y.size, n_classes,
+                                      C.byref(p), options, handles))
+        raw = list(handles)
+    else:
+        h = C.c_void_p()
+        check(lib.mpsb_cuda_train_regressor(backend.handle, dev.handle, ptr(y), ptr(w), y.size,
+                                            C.byref(p), options, C.byref(h)))
+        raw = [h.value]
+    del keep
+    models = []
+    for h in raw:
+        m = RegressionModel._from_handle(h)
+        m.train_predictions = np.empty(dataset.rows, np.float64)
+        check(lib.mpsb_cuda_model_train_predictions(h, ptr(m.train_predictions)))
+        lib.mpsb_cuda_model_destroy(h)
+        models.append(m)
+    return models
+
+
+def train_regressor(backend: CudaBackend, dataset: BinnedDataset, labels, weights=None, *,
+                    hist_mode: str = "fixed", batched: bool = True, graph: bool = True,
+                    **params) -> RegressionModel:
+    """Boosted regression trees on the GPU (TrainRegressionModel, trainer.cpp:226-266)."""
+
+    options = _options(hist_mode, batched, graph)
+    return _train(backend, dataset, labels, weights, options, 0, **params)[0]
+
+
+def train_ovr(backend: CudaBackend, dataset: BinnedDataset, labels, n_classes: int, weights=None, *,
+              hist_mode: str = "fixed", graph: bool = True, **params) -> list[RegressionModel]:
+    """K binary-logistic models, one per class, built side by side in the same launches."""
+
+    params.setdefault("objective", "binary_logistic")
+    options = _options(hist_mode, True, graph)
+    return _train(backend, dataset, labels, weights, options, int(n_classes), **params)
+
+
+def _options(hist_mode: str, batched: bool, graph: bool) -> int:
+    opts = 0
+    if hist_mode == "float":
+        opts |= _lib.OPT_FLOAT_HIST
+    elif hist_mode != "fixed":
+        raise ValueError("hist_mode must be 'fixed' or 'float'")
+    if not batched:
+        opts |= _lib.OPT_PER_NODE
+    if not graph:
+        opts |= _lib.OPT_NO_GRAPH
+    return opts
+
+
+class Trainer:
+    """A training session with device-resident inputs (benchmarks and timing)."""
+
+    def __init__(self, backend: CudaBackend, dataset: BinnedDataset, labels, weights=None, *,
+                 options: int = 0, **params):
+        self.backend = backend
+        self._dev = backend.dataset(dataset)
+        y = np.ascontiguousarray(labels, dtype=np.float64)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        params.setdefault("max_bins", dataset.max_bins)
+        p, keep = make_params(**params)
+        h = C.c_void_p()
+        check(_lib.load().mpsb_cuda_trainer_create(backend.handle, self._dev.handle, ptr(y), ptr(w), y.size,
+                                                   C.byref(p), options, C.byref(h)))
+        del keep
+        self.handle = h
+
+    def run(self, rounds: int) -> None:
+        check(_lib.load().mpsb_cuda_trainer_run(self.handle, rounds))
+
+    def synchronize(self) -> None:
+        check(_lib.load().mpsb_cuda_trainer_synchronize(self.handle))
+
+    def stats(self) -> dict:
+        s = _lib.Stats()
+        check(_lib.load().mpsb_cuda_trainer_stats(self.handle, C.byref(s)))
+        return {name: getattr(s, name) for name, _ in s._fields_}
+
+    def reset_stats(self) -> None:
+        check(_lib.load().mpsb_cuda_trainer_reset_stats(self.handle))
+
+    def export(self) -> RegressionModel:
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.mpsb_cuda_trainer_export(self.handle, C.byref(h)))
+        m = RegressionModel._from_handle(h)
+        m.train_predictions = np.empty(self._dev.rows, np.float64)
+        check(lib.mpsb_cuda_model_train_predictions(h, ptr(m.train_predictions)))
+        lib.mpsb_cuda_model_destroy(h)
+        return m
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            _lib.load().mpsb_cuda_trainer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

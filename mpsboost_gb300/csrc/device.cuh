@@ -1,0 +1,255 @@
+// Device-side data structures and exact arithmetic shared by the sm_103a kernels.
+//
+// FP64 expressions that restate the reference's objective math use explicit
+// round-to-nearest intrinsics (__dadd_rn, __dmul_rn, __ddiv_rn) so the compiler can never
+// fuse a multiply and an add: each operation rounds exactly once, as in the reference
+// C++ (src/core/objective.cpp:264-356) compiled without contraction.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mpsb {
+
+constexpr int kSlots = 256;          // histogram slots per feature
+constexpr int kMissingSlot = 255;    // bin value of a missing row (features with missing)
+constexpr int kBlockFeatures = 32;   // features per column block of the bin matrix
+constexpr uint32_t kItemRowsMax = 65536;  // rows of one histogram work item (packing bound)
+constexpr int kCountShift = 47;      // fixed mode: count lives above bit 47 of the h word
+constexpr uint32_t kPartChunk = 4096;     // rows per partition chunk
+constexpr uint32_t kApplyChunk = 4096;    // rows per leaf-application chunk
+
+enum : int { kModeFixed = 0, kModeFloat = 1 };
+
+// Device status bits (ORed into TrainerState::error).
+enum : uint32_t {
+  kErrCountMismatch = 1u << 0,   // histogram count != node count (tree_split.cpp:179-181)
+  kErrNonFinite = 1u << 1,       // non-finite statistic, gain or leaf value
+  kErrHessian = 1u << 2,         // negative Hessian sum
+  kErrSubtraction = 1u << 3,     // child bin exceeds parent bin (tree_histogram.cpp:44-60)
+  kErrPartition = 1u << 4,       // partition counts differ (tree_split.cpp:286-289)
+  kErrMissing = 1u << 5,         // missing stats exceed parent (tree_split.cpp:186-189)
+  kErrCapacity = 1u << 6,        // an internal table overflowed
+  kErrGradient = 1u << 7,        // invalid label / prediction / weight / gradient
+  kErrPrefix = 1u << 8,          // prefix exceeded the non-missing parent (tree_split.cpp:212-214)
+};
+
+// Tree parameters resolved on the host (tree.hpp:47-72, tree_structure.cpp:54-62).
+struct TreeParams {
+  uint64_t min_samples_leaf;
+  double min_child_weight;
+  double reg_lambda;
+  double reg_alpha;
+  double max_delta_step;
+  double gamma;
+  double min_gain_to_split;
+  double learning_rate;
+  uint32_t max_depth;
+  uint32_t max_leaves;  // effective
+  uint32_t split_strategy;
+  uint32_t random_seed;
+  uint32_t has_monotonic;
+  uint32_t n_groups;
+  uint32_t path_words;  // ceil(features / 32)
+  uint32_t objective;
+  double objective_alpha;
+  double tweedie_variance_power;
+};
+
+// One node of a depth level. Statistics are exact int64 (fixed mode; g/h hold the FP64
+// images q * 2^-k) or FP64 (float mode).
+struct NodeRec {
+  uint32_t seg_off;
+  uint32_t seg_cnt;
+  uint32_t node_index;  // index in the tree's flat node array
+  uint32_t slot;        // histogram slot
+  uint64_t count;
+  long long qg, qh;
+  double g, h;
+  double lo, hi;        // monotone bounds of the node's leaf value
+  uint32_t tree;
+  uint32_t depth;
+};
+
+// Best split of a node or of a (node, feature chunk); the SplitCandidate of
+// tree_internal.hpp:32-45 with exact statistics.
+struct SplitRec {
+  double gain;
+  uint32_t valid, feature, threshold, default_left;
+  uint64_t lcount, rcount;
+  long long lqg, lqh, rqg, rqh;
+  double lg, lh, rg, rh;
+  double ll, lu, rl, ru;
+};
+
+// Output tree node, layout of mpsb_tree_node.
+struct TreeNodeOut {
+  uint32_t feature_index, threshold_bin, left_child, right_child;
+  double leaf_value, gain;
+  uint8_t default_left, flags, reserved[6];
+};
+
+// A segment whose rows receive a leaf update: constant leaf, or (split != 0) routed by
+// the parent's split to its two children (last level: no partition is needed).
+struct LeafSeg {
+  uint32_t tree, parity, seg_off, seg_cnt;
+  uint32_t split, feature, threshold, default_left;
+  double value, left_value, right_value;
+};
+
+// Histogram build entry: one node whose histogram is accumulated from its rows.
+struct BuildEntry {
+  uint32_t tree, parity, seg_off, seg_cnt, slot, pad;
+};
+
+// Sibling subtraction: slot_sibling := slot_parent - slot_built (in place on the parent).
+struct SubEntry {
+  uint32_t parent_slot, built_slot;
+};
+
+// Accepted split whose rows are partitioned into the next level's buffer.
+struct PartEntry {
+  uint32_t tree, parity, seg_off, seg_cnt;
+  uint32_t feature, threshold, default_left, lcount;
+};
+
+// Per-tree round state.
+struct TreeState {
+  uint32_t max_abs_g_bits;  // float bits of max |g| (non-negative floats order as uints)
+  uint32_t max_h_bits;
+  int32_t kg, kh;           // fixed-point exponents
+  double inv_g, inv_h;      // 2^-kg, 2^-kh
+  uint32_t n_tree_nodes;
+  uint32_t leaf_count;
+};
+
+// Whole-trainer control block (device memory).
+struct Control {
+  uint32_t error;          // kErr* bits
+  uint32_t n_nodes;        // nodes in the current level (all trees)
+  uint32_t n_build;        // build entries of the current level
+  uint32_t n_sub;          // subtraction pairs of the current level
+  uint32_t n_part;         // partition entries of the current level
+  uint32_t n_leafseg;      // leaf segments of the current round
+  uint32_t hist_items;     // build chunks x feature blocks
+  uint32_t hist_counter;   // work-stealing counter of the histogram kernel
+  uint32_t part_chunks;
+  uint32_t leaf_chunks;
+  uint32_t free_top;       // histogram-slot free stack
+  uint32_t split_items;    // nodes x feature chunks
+  unsigned long long cells;       // cumulative row x feature cells built (accounting)
+  unsigned long long rows_built;
+};
+
+// ---------------------------------------------------------------------------------
+// Exact FP64 objective math (objective.cpp:264-356, tree_structure.cpp:72-87).
+// Each returns false where the reference throws TrainingError.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ bool soft_threshold(double g, double alpha, double* out) {
+  if (!isfinite(g)) return false;
+  const double magnitude = __dadd_rn(fabs(g), -alpha);
+  *out = magnitude <= 0.0 ? 0.0 : copysign(magnitude, g);
+  return true;
+}
+
+__device__ __forceinline__ bool node_score(double g, double h, double lambda, double alpha,
+                                           double* out) {
+  double rg;
+  if (!soft_threshold(g, alpha, &rg)) return false;
+  if (!isfinite(h) || h < 0.0) return false;
+  const double d = __dadd_rn(h, lambda);
+  if (!isfinite(d) || d <= 0.0) return false;
+  *out = __ddiv_rn(__dmul_rn(rg, rg), d);
+  return isfinite(*out);
+}
+
+__device__ __forceinline__ bool leaf_weight(double g, double h, const TreeParams& p,
+                                            double* out) {
+  double rg;
+  if (!soft_threshold(g, p.reg_alpha, &rg)) return false;
+  if (!isfinite(h) || h < 0.0) return false;
+  const double d = __dadd_rn(h, p.reg_lambda);
+  if (!isfinite(d) || d <= 0.0) return false;
+  double w = __ddiv_rn(-rg, d);
+  if (p.max_delta_step != 0.0) w = fmax(-p.max_delta_step, fmin(p.max_delta_step, w));
+  *out = w;
+  return isfinite(w);
+}
+
+__device__ __forceinline__ double clamp_bounds(double v, double lo, double hi) {
+  return v < lo ? lo : (hi < v ? hi : v);  // std::clamp(v, lo, hi)
+}
+
+__device__ __forceinline__ bool split_gain(double lg, double lh, double rg, double rh,
+                                           const TreeParams& p, double* out) {
+  if (!isfinite(lh) || !isfinite(rh) || lh <= 0.0 || rh <= 0.0) return false;
+  const double pg = __dadd_rn(lg, rg), ph = __dadd_rn(lh, rh);
+  if (!isfinite(pg) || !isfinite(ph)) return false;
+  double sl, sr, sp;
+  if (!node_score(lg, lh, p.reg_lambda, p.reg_alpha, &sl)) return false;
+  if (!node_score(rg, rh, p.reg_lambda, p.reg_alpha, &sr)) return false;
+  if (!node_score(pg, ph, p.reg_lambda, p.reg_alpha, &sp)) return false;
+  const double gain = __dadd_rn(__dmul_rn(0.5, __dadd_rn(__dadd_rn(sl, sr), -sp)), -p.gamma);
+  *out = gain;
+  return isfinite(gain);
+}
+
+// StableRandomThreshold (tree_split.cpp:14-29).
+__device__ __forceinline__ uint32_t stable_random_threshold(uint32_t seed, uint32_t feature,
+                                                            uint32_t node, uint32_t depth,
+                                                            uint32_t candidates) {
+  unsigned long long v = seed;
+  v ^= (unsigned long long)feature + 0x9E3779B97F4A7C15ULL;
+  v *= 0xBF58476D1CE4E5B9ULL;
+  v ^= ((unsigned long long)node << 32) | depth;
+  v *= 0x94D049BB133111EBULL;
+  v ^= v >> 31;
+  return (uint32_t)(v % candidates);
+}
+
+// round_half_even(x * 2^k) for a finite float x, exactly, with integer arithmetic only.
+// Equals llrint(ldexp((double)x, k)) whenever the result fits in int64 (the scale rule
+// guarantees |result| < 2^62).
+__device__ __forceinline__ long long quantize_f32(float x, int k) {
+  const uint32_t bits = __float_as_uint(x);
+  const uint32_t e = (bits >> 23) & 0xFFu;
+  uint32_t mant = bits & 0x7FFFFFu;
+  int exp2;
+  if (e == 0) {
+    exp2 = -149;
+  } else {
+    mant |= 0x800000u;
+    exp2 = (int)e - 150;
+  }
+  const int shift = exp2 + k;
+  unsigned long long q;
+  if (shift >= 0) {
+    q = (unsigned long long)mant << shift;
+  } else if (shift < -25) {
+    q = 0;  // |x * 2^k| < 2^24 * 2^-26 = 1/4
+  } else {
+    const int s = -shift;
+    q = mant >> s;
+    const uint32_t rem = mant & ((1u << s) - 1u);
+    const uint32_t half = 1u << (s - 1);
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+  }
+  return (bits >> 31) ? -(long long)q : (long long)q;
+}
+
+__device__ __forceinline__ double q_image(long long q, double inv) {
+  return __dmul_rn(__ll2double_rn(q), inv);
+}
+
+// Total order of split candidates: IsBetterSplit (tree_split.cpp:31-45) with the missing
+// direction tried first (default_left = true) winning exact ties.
+__device__ __forceinline__ bool better_split(const SplitRec& a, const SplitRec& b) {
+  if (!a.valid) return false;
+  if (!b.valid) return true;
+  if (a.gain != b.gain) return a.gain > b.gain;
+  if (a.feature != b.feature) return a.feature < b.feature;
+  if (a.threshold != b.threshold) return a.threshold < b.threshold;
+  return a.default_left && !b.default_left;
+}
+
+}  // namespace mpsb

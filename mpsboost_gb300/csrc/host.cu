@@ -1,0 +1,827 @@
+// Host side of the CUDA backend: the C ABI of include/mpsb_cuda.h, the device-resident
+// dataset, the node-level entries of the reference backend contract
+// (include/mpsboost/backend.hpp:52-135) and the device-resident training session.
+//
+// One backend owns one CUDA stream. A training session keeps every input on the device
+// and runs each boosting round as a fixed sequence of kernels (gradients, then per depth
+// level: zero slots, histogram build, root stats or sibling subtraction, split scan,
+// finalize, partition; then leaf application), captured once as a CUDA graph and
+// replayed per round. No row ever returns to the host inside a round; the host reads
+// back only the finished trees.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "host_types.h"
+
+using namespace mpsb;
+
+namespace mpsb {
+
+thread_local std::string g_error;
+
+std::string describe_device_error(uint32_t bits) {
+  std::string m = "device reported:";
+  if (bits & kErrCountMismatch) m += " Histogram sample count does not match node statistics;";
+  if (bits & kErrNonFinite) m += " non-finite histogram, gain or leaf value;";
+  if (bits & kErrHessian) m += " Histogram G/H must be finite and Hessian non-negative;";
+  if (bits & kErrSubtraction) m += " Histogram subtraction child exceeded parent;";
+  if (bits & kErrPartition) m += " Sample partition counts do not match histogram statistics;";
+  if (bits & kErrMissing) m += " missing statistics exceed parent statistics;";
+  if (bits & kErrCapacity) m += " internal capacity exceeded;";
+  if (bits & kErrGradient) m += " invalid label, prediction, weight or gradient;";
+  if (bits & kErrPrefix) m += " non-missing histogram prefix exceeded parent;";
+  return m;
+}
+
+// ---- reference semantics evaluated on the host --------------------------------------
+void validate_tree_params(const mpsb_train_params& p, uint32_t features) {  // tree_structure.cpp:17-52
+  if (p.min_samples_leaf == 0) throw TrainingError("min_samples_leaf must be at least 1");
+  if (p.max_leaves == 1) throw TrainingError("max_leaves must be zero or at least 2");
+  if (p.max_active_leaves == 1) throw TrainingError("max_active_leaves must be zero or at least 2");
+  if (p.max_active_leaves != 0 && p.max_leaves != 0 && p.max_active_leaves > p.max_leaves)
+    throw TrainingError("max_active_leaves must not exceed max_leaves");
+  auto nonneg = [](double v, const char* what) {
+    if (!std::isfinite(v) || v < 0.0) throw TrainingError(std::string(what) + " must be finite and non-negative");
+  };
+  nonneg(p.min_child_weight, "min_child_weight");
+  nonneg(p.reg_lambda, "reg_lambda");
+  nonneg(p.reg_alpha, "reg_alpha");
+  nonneg(p.max_delta_step, "max_delta_step");
+  nonneg(p.gamma, "gamma");
+  nonneg(p.min_gain_to_split, "min_gain_to_split");
+  if (p.n_monotonic != 0 && p.n_monotonic != features)
+    throw TrainingError("monotonic_constraints length must match feature count");
+  for (uint32_t i = 0; i < p.n_monotonic; ++i)
+    if (p.monotonic_constraints[i] < -1 || p.monotonic_constraints[i] > 1)
+      throw TrainingError("monotonic_constraints values must be -1, 0, or 1");
+  for (uint32_t g = 0; g < p.n_interaction_groups; ++g) {  // tree_interactions.cpp:57-70
+    if (p.interaction_offsets[g + 1] == p.interaction_offsets[g])
+      throw TrainingError("interaction constraint groups must be non-empty");
+    for (uint32_t i = p.interaction_offsets[g]; i < p.interaction_offsets[g + 1]; ++i)
+      if (p.interaction_features[i] >= features)
+        throw TrainingError("interaction constraint feature index out of range");
+  }
+  if (p.split_strategy > 1) throw TrainingError("unknown split strategy");
+  if (p.growth_strategy != 0)
+    throw UnsupportedError("the CUDA backend grows trees level-wise only (growth_strategy=level_wise)");
+}
+
+void validate_training_params(const mpsb_train_params& p) {  // trainer.cpp:22-42
+  if (p.n_estimators == 0) throw TrainingError("n_estimators must be at least 1");
+  if (!std::isfinite(p.learning_rate) || p.learning_rate <= 0.0 || p.learning_rate > 1.0)
+    throw TrainingError("learning_rate must be in (0, 1]");
+  if (p.max_bins < 2 || p.max_bins > 65536) throw TrainingError("max_bins must be in [2, 65536]");
+  if (!std::isfinite(p.objective_alpha) || p.objective_alpha <= 0.0 || p.objective_alpha >= 1.0)
+    throw TrainingError("quantile alpha must be in (0, 1)");
+  if (!std::isfinite(p.tweedie_variance_power) || p.tweedie_variance_power <= 1.0 ||
+      p.tweedie_variance_power >= 2.0)
+    throw TrainingError("tweedie variance power must be in (1, 2)");
+  if (p.objective > 4) throw TrainingError("unknown training objective");
+}
+
+double validate_weights(const double* w, uint64_t n) {  // trainer.cpp:44-66
+  if (n == 0) throw TrainingError("labels must be non-empty");
+  double total = 0.0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const double x = w ? w[i] : 1.0;
+    if (!std::isfinite(x) || x < 0.0) throw TrainingError("sample weights must be finite non-negative values");
+    total += x;
+    if (!std::isfinite(total)) throw TrainingError("sample weight sum overflowed");
+  }
+  if (total <= 0.0) throw TrainingError("sample weights must contain positive total weight");
+  return total;
+}
+
+// InitialBaseScore (trainer.cpp:68-176) on host FP64 in row order. `cls` >= 0 selects the
+// one-vs-rest binary labels (label == cls).
+double base_score(const mpsb_train_params& p, const double* y, const double* w, uint64_t n,
+                  int64_t cls) {
+  const double total = validate_weights(w, n);
+  auto W = [&](uint64_t i) { return w ? w[i] : 1.0; };
+  auto Y = [&](uint64_t i) { return cls >= 0 ? (y[i] == double(cls) ? 1.0 : 0.0) : y[i]; };
+  switch (p.objective) {
+    case MPSB_SQUARED_ERROR: {
+      double s = 0.0;
+      for (uint64_t i = 0; i < n; ++i) {
+        if (!std::isfinite(Y(i))) throw TrainingError("Labels must be finite");
+        s += Y(i) * W(i);
+        if (!std::isfinite(s)) throw TrainingError("Label accumulation overflowed");
+      }
+      return s / total;
+    }
+    case MPSB_BINARY_LOGISTIC: {
+      double pos = 0.0;
+      for (uint64_t i = 0; i < n; ++i) {
+        const double l = Y(i);
+        if (l == 0.0) continue;
+        if (l == 1.0) { pos += W(i); continue; }
+        throw TrainingError("binary-logistic labels must be 0 or 1");
+      }
+      const double eps = 1e-15;
+      double prob = pos / total;
+      prob = std::min(1.0 - eps, std::max(eps, prob));
+      return std::log(prob / (1.0 - prob));
+    }
+    case MPSB_QUANTILE: {
+      std::vector<std::pair<double, double>> o(n);
+      for (uint64_t i = 0; i < n; ++i) {
+        if (!std::isfinite(Y(i))) throw TrainingError("label must be finite");
+        o[i] = {Y(i), W(i)};
+      }
+      std::sort(o.begin(), o.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+      const double thr = p.objective_alpha * total;
+      double cum = 0.0;
+      for (const auto& it : o) {
+        cum += it.second;
+        if (cum >= thr) return it.first;
+      }
+      return o.back().first;
+    }
+    default: {
+      const char* name = p.objective == MPSB_POISSON ? "poisson" : "tweedie";
+      double s = 0.0;
+      for (uint64_t i = 0; i < n; ++i) {
+        if (!std::isfinite(Y(i)) || Y(i) < 0.0) throw TrainingError(std::string(name) + " labels must be non-negative");
+        s += Y(i) * W(i);
+        if (!std::isfinite(s)) throw TrainingError(std::string(name) + " label sum overflowed");
+      }
+      return std::log(std::max(1e-15, s / total));
+    }
+  }
+}
+
+uint32_t effective_max_leaves(const mpsb_train_params& p) {  // tree_structure.cpp:54-62
+  if (p.max_leaves != 0) return p.max_leaves;
+  if (p.max_depth >= 31) return 0xFFFFFFFFu;
+  return 1u << p.max_depth;
+}
+
+// Fixed-point exponents of one set of FP32 pairs (same rule as the round_setup kernel).
+void fixed_scales(const float* pairs32, uint64_t n, uint64_t n_rows, int32_t* kg, int32_t* kh) {
+  float mg = 0.0f, mh = 0.0f;
+  for (uint64_t i = 0; i < n; ++i) {
+    mg = std::max(mg, std::fabs(pairs32[2 * i]));
+    mh = std::max(mh, std::max(pairs32[2 * i + 1], 0.0f));
+  }
+  int en = 0;
+  while (en < 63 && (uint64_t(1) << en) < n_rows) ++en;
+  int e;
+  std::frexp(mg, &e);
+  *kg = mg > 0.0f ? 61 - en - e : 0;
+  std::frexp(mh, &e);
+  *kh = mh > 0.0f ? 30 - e : 0;
+}
+
+}  // namespace mpsb
+
+// ======================================================================================
+// Backend
+// ======================================================================================
+extern "C" {
+
+const char* mpsb_cuda_last_error(void) { return g_error.c_str(); }
+int mpsb_cuda_abi_version(void) { return MPSB_CUDA_ABI_VERSION; }
+
+int mpsb_cuda_backend_create(int device, mpsb_cuda_backend** out) {
+  return guard([&] {
+    if (out == nullptr) throw TrainingError("output pointer must not be null");
+    int count = 0;
+    CK(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) throw BackendError("CUDA device index out of range");
+    std::unique_ptr<mpsb_cuda_backend> b(new mpsb_cuda_backend);
+    b->device = device;
+    CK(cudaSetDevice(device));
+    CK(cudaGetDeviceProperties(&b->prop, device));
+    if (b->prop.major != 10 || b->prop.minor != 3)
+      throw BackendError("the CUDA backend is built for sm_103a (GB300); device " +
+                         std::string(b->prop.name) + " has compute capability " +
+                         std::to_string(b->prop.major) + "." + std::to_string(b->prop.minor));
+    b->sm_count = b->prop.multiProcessorCount;
+    CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&b->t0));
+    CK(cudaEventCreate(&b->t1));
+    b->error.alloc(sizeof(uint32_t));
+    CK(cudaMemset(b->error.p, 0, sizeof(uint32_t)));
+    *out = b.release();
+  });
+}
+
+void mpsb_cuda_backend_destroy(mpsb_cuda_backend* b) { delete b; }
+
+int mpsb_cuda_backend_info(const mpsb_cuda_backend* b, mpsb_cuda_info* out) {
+  return guard([&] {
+    std::memset(out, 0, sizeof *out);
+    out->available = 1;
+    out->sm_count = uint32_t(b->sm_count);
+    out->cc_major = uint32_t(b->prop.major);
+    out->cc_minor = uint32_t(b->prop.minor);
+    out->total_memory = b->prop.totalGlobalMem;
+    std::snprintf(out->device_name, sizeof out->device_name, "%.95s", b->prop.name);
+  });
+}
+
+int mpsb_cuda_backend_set_hist_mode(mpsb_cuda_backend* b, int mode) {
+  return guard([&] {
+    if (mode != MPSB_HIST_FIXED && mode != MPSB_HIST_FLOAT) throw TrainingError("unknown histogram mode");
+    b->hist_mode = mode;
+  });
+}
+
+int mpsb_cuda_timer_begin(mpsb_cuda_backend* b) {
+  return guard([&] { CK(cudaEventRecord(b->t0, b->stream)); });
+}
+
+int mpsb_cuda_timer_end(mpsb_cuda_backend* b, float* ms) {
+  return guard([&] {
+    CK(cudaEventRecord(b->t1, b->stream));
+    CK(cudaEventSynchronize(b->t1));
+    CK(cudaEventElapsedTime(ms, b->t0, b->t1));
+  });
+}
+
+int mpsb_cuda_synchronize(mpsb_cuda_backend* b) {
+  return guard([&] { CK(cudaStreamSynchronize(b->stream)); });
+}
+
+int mpsb_cuda_host_register(void* p, uint64_t bytes) {
+  return guard([&] { CK(cudaHostRegister(p, bytes, cudaHostRegisterDefault)); });
+}
+
+int mpsb_cuda_host_unregister(void* p) {
+  return guard([&] { CK(cudaHostUnregister(p)); });
+}
+
+// ---- binning ---------------------------------------------------------------------------
+int mpsb_quantize_dense(const void* data, int scalar_type, uint64_t rows, uint32_t features,
+                        uint64_t rs, uint64_t cs, uint32_t max_bins, uint32_t n_threads,
+                        void* bins, uint8_t* missing, float* boundaries,
+                        uint64_t* boundary_offset, uint32_t* boundary_count,
+                        uint32_t* bin_count, uint64_t* missing_count) {
+  return guard([&] {
+    mpsb::quantize_dense(data, scalar_type, rows, features, rs, cs, max_bins, n_threads, bins,
+                         missing, boundaries, boundary_offset, boundary_count, bin_count,
+                         missing_count);
+  });
+}
+
+int mpsb_transform_dense(const void* data, int scalar_type, uint64_t rows, uint32_t features,
+                         uint64_t rs, uint64_t cs, uint32_t max_bins, const float* boundaries,
+                         const uint64_t* boundary_offset, const uint32_t* boundary_count,
+                         uint32_t n_threads, void* bins, uint8_t* missing) {
+  return guard([&] {
+    mpsb::transform_dense(data, scalar_type, rows, features, rs, cs, max_bins, boundaries,
+                          boundary_offset, boundary_count, n_threads, bins, missing);
+  });
+}
+
+// ---- dataset ---------------------------------------------------------------------------
+int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t width,
+                             const uint8_t* missing, uint64_t rows, uint32_t features,
+                             const uint32_t* bin_count, mpsb_cuda_dataset** out) {
+  return guard([&] {
+    if (!b || !bins || !bin_count || !out) throw TrainingError("null argument");
+    if (width != 1 && width != 2) throw DataError("bin width must be 1 or 2 bytes");
+    if (rows == 0 || features == 0) throw DataError("dataset must contain at least one row and one feature");
+    if (rows >= 0xFFFFFFFFull) throw UnsupportedError("the CUDA backend indexes rows with uint32");
+    b->activate();
+    std::unique_ptr<mpsb_cuda_dataset> d(new mpsb_cuda_dataset);
+    d->backend = b;
+    d->n_rows = uint32_t(rows);
+    d->features = features;
+    d->nfb = (features + kBlockFeatures - 1) / kBlockFeatures;
+    d->h_bin_count.assign(bin_count, bin_count + features);
+    d->h_has_missing.assign(features, 0);
+    for (uint32_t f = 0; f < features; ++f) {
+      if (bin_count[f] == 0) throw DataError("every feature needs at least one bin");
+      if (bin_count[f] > 256)
+        throw UnsupportedError("the CUDA backend supports at most 256 bins per feature");
+    }
+    if (missing) {
+      for (uint32_t f = 0; f < features; ++f) {
+        const uint8_t* m = missing + uint64_t(f) * rows;
+        for (uint64_t r = 0; r < rows; ++r)
+          if (m[r]) { d->h_has_missing[f] = 1; break; }
+        if (d->h_has_missing[f] && bin_count[f] > 255)
+          throw UnsupportedError("a feature with missing values may have at most 255 bins on the CUDA backend");
+      }
+    }
+    const size_t cells = size_t(rows) * features;
+    DevBuf src, miss;
+    src.alloc(cells * width);
+    CK(cudaMemcpyAsync(src.p, bins, cells * width, cudaMemcpyHostToDevice, b->stream));
+    if (missing) {
+      miss.alloc(cells);
+      CK(cudaMemcpyAsync(miss.p, missing, cells, cudaMemcpyHostToDevice, b->stream));
+    }
+    d->bin_count.alloc(features * sizeof(uint32_t));
+    d->has_missing.alloc(features);
+    CK(cudaMemcpyAsync(d->bin_count.p, bin_count, features * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(d->has_missing.p, d->h_has_missing.data(), features, cudaMemcpyHostToDevice, b->stream));
+    d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+    CK(launch_pack_bins(src.p, width, missing ? miss.as<uint8_t>() : nullptr,
+                        d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb,
+                        d->bins.as<uint8_t>(), b->error.as<uint32_t>(), b->stream));
+    if (b->take_error()) throw DataError("Binned value exceeds the feature histogram range");
+    *out = d.release();
+  });
+}
+
+void mpsb_cuda_dataset_destroy(mpsb_cuda_dataset* d) { delete d; }
+
+}  // extern "C"
+
+// ======================================================================================
+// Training session
+// ======================================================================================
+struct mpsb_cuda_trainer {
+  mpsb_cuda_backend* b = nullptr;
+  const mpsb_cuda_dataset* ds = nullptr;
+  mpsb_train_params params{};
+  uint32_t options = 0;
+  uint32_t depth = 0;
+  uint32_t n_trees = 1;
+  bool ovr = false;
+  TrainerDev dev{};
+  HistConfig hcfg;
+  std::vector<std::unique_ptr<DevBuf>> bufs;
+  std::vector<double> base_scores;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<cudaEvent_t> events;  // 2 per level (histogram build begin/end)
+  uint32_t rounds_enqueued = 0;
+  mpsb_cuda_stats stats{};
+  uint64_t kernels_per_round = 0;
+  uint64_t cells_base = 0, rows_base = 0;
+
+  template <class T>
+  T* alloc(size_t count) {
+    bufs.emplace_back(new DevBuf);
+    bufs.back()->alloc(count * sizeof(T));
+    return bufs.back()->as<T>();
+  }
+
+  ~mpsb_cuda_trainer() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+  }
+
+  int grid(int per_sm) const { return b->sm_count * per_sm; }
+
+  // Enqueue one boosting round. Returns the number of kernels enqueued.
+  uint64_t enqueue_round(bool record_events) {
+    cudaStream_t s = b->stream;
+    uint64_t k = 0;
+    CK(launch_round_begin(dev, s)); ++k;
+    CK(launch_gradients(dev, std::max(1, std::min(grid(4), int((dev.n_rows + 255) / 256))), s)); ++k;
+    CK(launch_round_setup(dev, s)); ++k;
+    const uint32_t levels = std::max<uint32_t>(depth, 1);
+    for (uint32_t d = 0; d < levels; ++d) {
+      const int parity = int(d & 1);
+      CK(launch_zero_build_slots(dev, grid(8), s)); ++k;
+      if (record_events) CK(cudaEventRecord(events[2 * d], s));
+      if (options & MPSB_OPT_PER_NODE) {
+        k += enqueue_hist_per_node(d);
+      } else {
+        CK(launch_hist_build(dev, hcfg, grid(1), s)); ++k;
+      }
+      if (record_events) CK(cudaEventRecord(events[2 * d + 1], s));
+      if (d == 0) {
+        CK(launch_root_stats(dev, s)); ++k;
+      } else {
+        CK(launch_subtract(dev, grid(8), s)); ++k;
+      }
+      if (depth > 0) {
+        CK(launch_split_scan(dev, parity, grid(4), s)); ++k;
+      }
+      CK(launch_finalize(dev, parity, d, s)); ++k;
+      if (d + 1 < depth) {
+        CK(launch_partition(dev, grid(4), s)); k += kPartitionKernels;
+      }
+    }
+    CK(launch_apply_leaves(dev, grid(8), s)); ++k;
+    CK(launch_round_end(dev, s)); ++k;
+    return k;
+  }
+
+  // Plain path: the host reads the level's build list and launches one histogram build
+  // per node, waiting for each level (the per-node submit/wait of mps_histogram.mm:62-80).
+  uint64_t enqueue_hist_per_node(uint32_t d) {
+    (void)d;
+    cudaStream_t s = b->stream;
+    Control c;
+    CK(cudaMemcpyAsync(&c, dev.ctl, sizeof c, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<uint32_t> prefix(c.n_build + 1);
+    CK(cudaMemcpyAsync(prefix.data(), dev.build_prefix, prefix.size() * sizeof(uint32_t),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    uint64_t k = 0;
+    for (uint32_t e = 0; e < c.n_build; ++e) {
+      TrainerDev one = dev;
+      one.item_begin = prefix[e] * dev.nfb;
+      one.item_end = prefix[e + 1] * dev.nfb;
+      CK(cudaMemsetAsync(&dev.ctl->hist_counter, 0, sizeof(uint32_t), s));
+      CK(launch_hist_build(one, hcfg, grid(1), s));
+      ++k;
+      CK(cudaStreamSynchronize(s));
+    }
+    return k;
+  }
+
+  void run(uint32_t rounds) {
+    b->activate();
+    if (rounds_enqueued + rounds > dev.max_rounds)
+      throw TrainingError("training session round capacity exceeded");
+    const bool timing = options & MPSB_OPT_TIMING;
+    const bool use_graph = !(options & (MPSB_OPT_NO_GRAPH | MPSB_OPT_PER_NODE));
+    for (uint32_t r = 0; r < rounds; ++r) {
+      if (use_graph) {
+        if (!graph_exec) {
+          CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+          uint64_t k = 0;
+          try {
+            k = enqueue_round(timing);
+          } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(b->stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+          }
+          CK(cudaStreamEndCapture(b->stream, &graph));
+          CK(cudaGraphInstantiate(&graph_exec, graph, 0));
+          kernels_per_round = k;
+        }
+        CK(cudaGraphLaunch(graph_exec, b->stream));
+        stats.kernel_launches += kernels_per_round;
+      } else {
+        stats.kernel_launches += enqueue_round(timing);
+      }
+      stats.hist_launches += (options & MPSB_OPT_PER_NODE) ? 0 : std::max<uint32_t>(depth, 1);
+      ++rounds_enqueued;
+      ++stats.rounds;
+      if (timing) {
+        CK(cudaStreamSynchronize(b->stream));
+        for (uint32_t d = 0; d < std::max<uint32_t>(depth, 1); ++d) {
+          float ms = 0.0f;
+          CK(cudaEventElapsedTime(&ms, events[2 * d], events[2 * d + 1]));
+          stats.hist_ms += ms;
+          ++stats.hist_timed_launches;
+        }
+      }
+    }
+  }
+
+  void synchronize() {
+    b->activate();
+    CK(cudaStreamSynchronize(b->stream));
+    Control c;
+    CK(cudaMemcpy(&c, dev.ctl, sizeof c, cudaMemcpyDeviceToHost));
+    stats.hist_cells = c.cells - cells_base;
+    stats.hist_rows = c.rows_built - rows_base;
+    if (c.error) throw TrainingError(describe_device_error(c.error));
+  }
+};
+
+namespace {
+
+void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
+                   const double* labels, const double* weights, uint64_t n,
+                   const mpsb_train_params* p, uint32_t options, uint32_t n_classes) {
+  if (!b || !ds || !labels || !p) throw TrainingError("null argument");
+  validate_training_params(*p);
+  validate_tree_params(*p, ds->features);
+  if (n != ds->n_rows) throw TrainingError("Training data, labels, or max_bins contract does not match");
+  validate_weights(weights, n);
+  b->activate();
+  t->b = b;
+  t->ds = ds;
+  t->params = *p;
+  t->options = options;
+  t->depth = p->max_depth;
+  t->ovr = n_classes > 0;
+  t->n_trees = t->ovr ? n_classes : 1;
+  if (t->ovr && p->objective != MPSB_BINARY_LOGISTIC)
+    throw TrainingError("one-vs-rest training uses the binary_logistic objective");
+  const uint32_t T = t->n_trees;
+  const uint32_t F = ds->features;
+  const uint32_t D = p->max_depth;
+  if (D > 24) throw UnsupportedError("max_depth above 24 is not supported by the CUDA backend");
+  const uint64_t max_leaves_eff = effective_max_leaves(*p);
+  const uint64_t by_rows = std::max<uint64_t>(1, (n + p->min_samples_leaf - 1) / p->min_samples_leaf);
+  const uint64_t leaves = std::min<uint64_t>({uint64_t(1) << std::min<uint32_t>(D, 30), max_leaves_eff, by_rows});
+  const uint64_t level_nodes = std::max<uint64_t>(1, std::min<uint64_t>(D ? (uint64_t(1) << (D - 1)) : 1, leaves));
+  const uint64_t tree_nodes = 2 * leaves + 1;
+  TrainerDev& a = t->dev;
+  a = TrainerDev{};
+  a.bins = ds->bins.as<uint8_t>();
+  a.bin_count = ds->bin_count.as<uint32_t>();
+  a.has_missing = ds->has_missing.as<uint8_t>();
+  a.n_rows = ds->n_rows;
+  a.features = F;
+  a.nfb = ds->nfb;
+  a.n_trees = T;
+  a.objective = p->objective;
+  a.ovr = t->ovr ? 1 : 0;
+  a.mode = (options & MPSB_OPT_FLOAT_HIST) ? kModeFloat : kModeFixed;
+  a.scan_threads = 512;
+  a.n_fchunks = (F + a.scan_threads / 32 - 1) / (a.scan_threads / 32);
+  // rows per histogram work item: enough items to fill the GPU, <= 65536 (packing bound)
+  {
+    const uint64_t target_items = uint64_t(b->sm_count) * 4;
+    uint64_t per = (uint64_t(n) * ds->nfb + target_items - 1) / target_items;
+    per = std::max<uint64_t>(per, 2048);
+    per = (per + 511) / 512 * 512;
+    a.item_rows = uint32_t(std::min<uint64_t>(per, kItemRowsMax));
+  }
+  TreeParams& tp = a.params;
+  tp.min_samples_leaf = p->min_samples_leaf;
+  tp.min_child_weight = p->min_child_weight;
+  tp.reg_lambda = p->reg_lambda;
+  tp.reg_alpha = p->reg_alpha;
+  tp.max_delta_step = p->max_delta_step;
+  tp.gamma = p->gamma;
+  tp.min_gain_to_split = p->min_gain_to_split;
+  tp.learning_rate = p->learning_rate;
+  tp.max_depth = D;
+  tp.max_leaves = uint32_t(std::min<uint64_t>(max_leaves_eff, 0xFFFFFFFFull));
+  tp.split_strategy = p->split_strategy;
+  tp.random_seed = p->random_seed;
+  tp.has_monotonic = p->n_monotonic ? 1 : 0;
+  tp.n_groups = p->n_interaction_groups;
+  tp.path_words = (F + 31) / 32;
+  tp.objective = p->objective;
+  tp.objective_alpha = p->objective_alpha;
+  tp.tweedie_variance_power = p->tweedie_variance_power;
+  cudaStream_t s = b->stream;
+  const uint32_t W = tp.path_words;
+
+  // inputs
+  double* d_labels = t->alloc<double>(n);
+  CK(cudaMemcpyAsync(d_labels, labels, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  a.labels = d_labels;
+  if (weights) {
+    double* d_w = t->alloc<double>(n);
+    CK(cudaMemcpyAsync(d_w, weights, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    a.weights = d_w;
+  }
+  t->base_scores.resize(T);
+  std::vector<double> init(static_cast<size_t>(n));
+  a.preds = t->alloc<double>(size_t(T) * n);
+  for (uint32_t k = 0; k < T; ++k) {
+    t->base_scores[k] = base_score(*p, labels, weights, n, t->ovr ? int64_t(k) : -1);
+    std::fill(init.begin(), init.end(), t->base_scores[k]);
+    CK(cudaMemcpyAsync(a.preds + size_t(k) * n, init.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  if (p->n_monotonic) {
+    int8_t* m = t->alloc<int8_t>(F);
+    CK(cudaMemcpyAsync(m, p->monotonic_constraints, F, cudaMemcpyHostToDevice, s));
+    a.monotonic = m;
+  }
+  if (p->n_interaction_groups) {
+    std::vector<uint32_t> masks(size_t(p->n_interaction_groups) * W, 0);
+    for (uint32_t g = 0; g < p->n_interaction_groups; ++g)
+      for (uint32_t i = p->interaction_offsets[g]; i < p->interaction_offsets[g + 1]; ++i) {
+        const uint32_t f = p->interaction_features[i];
+        masks[size_t(g) * W + f / 32] |= 1u << (f % 32);
+      }
+    uint32_t* gm = t->alloc<uint32_t>(masks.size());
+    CK(cudaMemcpyAsync(gm, masks.data(), masks.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    a.group_masks = gm;
+  }
+  // working state
+  a.gh = t->alloc<float2>(size_t(T) * n);
+  a.rows = t->alloc<uint32_t>(size_t(T) * 2 * n);
+  a.trees = t->alloc<TreeState>(T);
+  a.max_level_nodes = uint32_t(T * level_nodes);
+  a.n_slots = a.max_level_nodes;
+  const uint64_t slot_words = uint64_t(F) * kSlots * 3;
+  a.hist = t->alloc<unsigned long long>(uint64_t(a.n_slots) * slot_words);
+  a.free_stack = t->alloc<uint32_t>(a.n_slots);
+  for (int q = 0; q < 2; ++q) {
+    a.nodes[q] = t->alloc<NodeRec>(a.max_level_nodes);
+    a.node_path[q] = t->alloc<uint32_t>(size_t(a.max_level_nodes) * W);
+    a.node_allowed[q] = t->alloc<uint32_t>(size_t(a.max_level_nodes) * W);
+  }
+  a.partial = t->alloc<SplitRec>(size_t(a.max_level_nodes) * a.n_fchunks);
+  a.build = t->alloc<BuildEntry>(a.max_level_nodes);
+  a.build_prefix = t->alloc<uint32_t>(a.max_level_nodes + 1);
+  a.sub = t->alloc<SubEntry>(a.max_level_nodes);
+  a.part = t->alloc<PartEntry>(a.max_level_nodes);
+  a.part_prefix = t->alloc<uint32_t>(a.max_level_nodes + 1);
+  a.max_part_chunks = uint32_t(T * ((n + kPartChunk - 1) / kPartChunk + level_nodes + 1));
+  a.part_counts = t->alloc<uint32_t>(a.max_part_chunks);
+  a.part_offsets = t->alloc<uint32_t>(a.max_part_chunks);
+  a.part_flags = t->alloc<uint32_t>(size_t(a.max_part_chunks) * (kPartChunk / 32));
+  a.max_leafsegs = uint32_t(T * (leaves + 1));
+  a.leafseg = t->alloc<LeafSeg>(a.max_leafsegs);
+  a.leaf_prefix = t->alloc<uint32_t>(a.max_leafsegs + 1);
+  a.max_tree_nodes = uint32_t(tree_nodes);
+  a.tree_nodes = t->alloc<TreeNodeOut>(size_t(T) * tree_nodes);
+  a.ctl = t->alloc<Control>(1);
+  CK(cudaMemsetAsync(a.ctl, 0, sizeof(Control), s));
+  a.scratch_flags = t->alloc<uint32_t>(a.max_level_nodes);
+  a.scratch_prefix = t->alloc<uint32_t>(a.max_level_nodes);
+  a.scratch_aux = t->alloc<uint32_t>(a.max_level_nodes);
+  a.tree_scratch = t->alloc<uint32_t>(size_t(T) * 4);
+  a.max_rounds = p->n_estimators;
+  a.model_nodes = t->alloc<TreeNodeOut>(size_t(a.max_rounds) * T * tree_nodes);
+  a.model_counts = t->alloc<uint32_t>(size_t(a.max_rounds) * T);
+  a.round_counter = t->alloc<uint32_t>(1);
+  CK(cudaMemsetAsync(a.round_counter, 0, sizeof(uint32_t), s));
+  a.item_begin = a.item_end = 0;
+  if (options & MPSB_OPT_TIMING) {
+    t->events.resize(2 * std::max<uint32_t>(D, 1));
+    for (auto& e : t->events) CK(cudaEventCreate(&e));
+  }
+  CK(cudaStreamSynchronize(s));
+}
+
+mpsb_cuda_model* export_model(mpsb_cuda_trainer* t, uint32_t tree_index) {
+  const TrainerDev& a = t->dev;
+  uint32_t rounds = 0;
+  CK(cudaMemcpy(&rounds, a.round_counter, sizeof rounds, cudaMemcpyDeviceToHost));
+  std::vector<uint32_t> counts(size_t(rounds) * a.n_trees);
+  if (!counts.empty())
+    CK(cudaMemcpy(counts.data(), a.model_counts, counts.size() * 4, cudaMemcpyDeviceToHost));
+  std::unique_ptr<mpsb_cuda_model> m(new mpsb_cuda_model);
+  m->base = t->base_scores[tree_index];
+  m->learning_rate = t->params.learning_rate;
+  m->n_trees = rounds;
+  m->trees.resize(rounds);
+  for (uint32_t r = 0; r < rounds; ++r) {
+    const uint32_t c = counts[size_t(r) * a.n_trees + tree_index];
+    m->trees[r].resize(c);
+    CK(cudaMemcpy(m->trees[r].data(),
+                  a.model_nodes + (size_t(r) * a.n_trees + tree_index) * a.max_tree_nodes,
+                  size_t(c) * sizeof(mpsb_tree_node), cudaMemcpyDeviceToHost));
+  }
+  m->train_predictions.resize(a.n_rows);
+  CK(cudaMemcpy(m->train_predictions.data(), a.preds + size_t(tree_index) * a.n_rows,
+                size_t(a.n_rows) * sizeof(double), cudaMemcpyDeviceToHost));
+  return m.release();
+}
+
+static_assert(sizeof(mpsb_tree_node) == sizeof(TreeNodeOut), "tree node layout");
+
+}  // namespace
+
+extern "C" {
+
+int mpsb_cuda_trainer_create(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
+                             const double* labels, const double* weights, uint64_t n,
+                             const mpsb_train_params* p, uint32_t options,
+                             mpsb_cuda_trainer** out) {
+  return guard([&] {
+    std::unique_ptr<mpsb_cuda_trainer> t(new mpsb_cuda_trainer);
+    setup_trainer(t.get(), b, ds, labels, weights, n, p, options, 0);
+    *out = t.release();
+  });
+}
+
+int mpsb_cuda_trainer_run(mpsb_cuda_trainer* t, uint32_t rounds) {
+  return guard([&] { t->run(rounds); });
+}
+
+int mpsb_cuda_trainer_synchronize(mpsb_cuda_trainer* t) {
+  return guard([&] { t->synchronize(); });
+}
+
+int mpsb_cuda_trainer_stats(const mpsb_cuda_trainer* t, mpsb_cuda_stats* out) {
+  return guard([&] { *out = t->stats; });
+}
+
+int mpsb_cuda_trainer_reset_stats(mpsb_cuda_trainer* t) {
+  return guard([&] {
+    t->synchronize();
+    Control c;
+    CK(cudaMemcpy(&c, t->dev.ctl, sizeof c, cudaMemcpyDeviceToHost));
+    t->cells_base = c.cells;
+    t->rows_base = c.rows_built;
+    t->stats = mpsb_cuda_stats{};
+  });
+}
+
+int mpsb_cuda_trainer_export(mpsb_cuda_trainer* t, mpsb_cuda_model** out) {
+  return guard([&] {
+    t->synchronize();
+    *out = export_model(t, 0);
+  });
+}
+
+void mpsb_cuda_trainer_destroy(mpsb_cuda_trainer* t) { delete t; }
+
+int mpsb_cuda_train_regressor(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
+                              const double* labels, const double* weights, uint64_t n,
+                              const mpsb_train_params* p, uint32_t options,
+                              mpsb_cuda_model** out) {
+  return guard([&] {
+    std::unique_ptr<mpsb_cuda_trainer> t(new mpsb_cuda_trainer);
+    setup_trainer(t.get(), b, ds, labels, weights, n, p, options, 0);
+    t->run(p->n_estimators);
+    t->synchronize();
+    *out = export_model(t.get(), 0);
+  });
+}
+
+int mpsb_cuda_train_ovr(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
+                        const double* labels, const double* weights, uint64_t n,
+                        uint32_t n_classes, const mpsb_train_params* p, uint32_t options,
+                        mpsb_cuda_model** out) {
+  return guard([&] {
+    if (n_classes < 2) throw TrainingError("one-vs-rest needs at least two classes");
+    for (uint64_t i = 0; i < n; ++i) {
+      const double y = labels[i];
+      if (!(y >= 0.0 && y < double(n_classes) && std::floor(y) == y))
+        throw TrainingError("one-vs-rest labels must be class ids in [0, n_classes)");
+    }
+    std::unique_ptr<mpsb_cuda_trainer> t(new mpsb_cuda_trainer);
+    setup_trainer(t.get(), b, ds, labels, weights, n, p, options, n_classes);
+    t->run(p->n_estimators);
+    t->synchronize();
+    for (uint32_t k = 0; k < n_classes; ++k) out[k] = export_model(t.get(), k);
+  });
+}
+
+int mpsb_cuda_model_create(double base, double lr, uint32_t n_trees, const uint32_t* counts,
+                           const mpsb_tree_node* nodes, mpsb_cuda_model** out) {
+  return guard([&] {
+    if (!std::isfinite(base) || !std::isfinite(lr) || lr <= 0.0 || lr > 1.0)
+      throw TrainingError("Model base score, learning rate, or tree count is invalid");
+    std::unique_ptr<mpsb_cuda_model> m(new mpsb_cuda_model);
+    m->base = base;
+    m->learning_rate = lr;
+    m->n_trees = n_trees;
+    m->trees.resize(n_trees);
+    size_t k = 0;
+    for (uint32_t t = 0; t < n_trees; ++t) {
+      if (counts[t] == 0) throw TrainingError("Tree model has no root node");
+      m->trees[t].assign(nodes + k, nodes + k + counts[t]);
+      k += counts[t];
+    }
+    *out = m.release();
+  });
+}
+
+uint32_t mpsb_cuda_model_tree_count(const mpsb_cuda_model* m) { return m->n_trees; }
+double mpsb_cuda_model_base_score(const mpsb_cuda_model* m) { return m->base; }
+double mpsb_cuda_model_learning_rate(const mpsb_cuda_model* m) { return m->learning_rate; }
+uint32_t mpsb_cuda_model_tree_node_count(const mpsb_cuda_model* m, uint32_t t) {
+  return t < m->trees.size() ? uint32_t(m->trees[t].size()) : 0;
+}
+int mpsb_cuda_model_tree_nodes(const mpsb_cuda_model* m, uint32_t t, mpsb_tree_node* out) {
+  return guard([&] {
+    if (t >= m->trees.size()) throw TrainingError("tree index out of range");
+    std::memcpy(out, m->trees[t].data(), m->trees[t].size() * sizeof(mpsb_tree_node));
+  });
+}
+int mpsb_cuda_model_train_predictions(const mpsb_cuda_model* m, double* out) {
+  return guard([&] {
+    std::memcpy(out, m->train_predictions.data(), m->train_predictions.size() * sizeof(double));
+  });
+}
+
+int mpsb_cuda_model_predict(mpsb_cuda_backend* b, const mpsb_cuda_model* m,
+                            const mpsb_cuda_dataset* ds, double* out) {
+  return guard([&] {
+    b->activate();
+    std::vector<uint32_t> offsets(m->trees.size() + 1, 0);
+    for (size_t t = 0; t < m->trees.size(); ++t) {
+      offsets[t + 1] = offsets[t] + uint32_t(m->trees[t].size());
+      for (const mpsb_tree_node& nd : m->trees[t])
+        if (!(nd.flags & 1u) && nd.feature_index >= ds->features)
+          throw TrainingError("Prediction feature count does not match the tree model");
+    }
+    std::vector<mpsb_tree_node> flat(offsets.back() ? offsets.back() : 1);
+    for (size_t t = 0; t < m->trees.size(); ++t)
+      std::copy(m->trees[t].begin(), m->trees[t].end(), flat.begin() + offsets[t]);
+    DevBuf d_nodes, d_off, d_out;
+    d_nodes.alloc(flat.size() * sizeof(mpsb_tree_node));
+    d_off.alloc(offsets.size() * sizeof(uint32_t));
+    d_out.alloc(size_t(ds->n_rows) * sizeof(double));
+    cudaStream_t s = b->stream;
+    CK(cudaMemcpyAsync(d_nodes.p, flat.data(), flat.size() * sizeof(mpsb_tree_node), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_off.p, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(launch_predict(ds->bins.as<uint8_t>(), ds->n_rows, ds->nfb, ds->has_missing.as<uint8_t>(),
+                      d_nodes.as<TreeNodeOut>(), d_off.as<uint32_t>(), uint32_t(m->trees.size()),
+                      m->base, m->learning_rate, d_out.as<double>(), b->error.as<uint32_t>(), s));
+    CK(cudaMemcpyAsync(out, d_out.p, size_t(ds->n_rows) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (b->take_error()) throw TrainingError("Tree node index is out of bounds or the structure contains a cycle");
+  });
+}
+
+void mpsb_cuda_model_destroy(mpsb_cuda_model* m) { delete m; }
+
+}  // extern "C"

@@ -1,0 +1,114 @@
+// Private host-side types of the CUDA backend (shared by host.cu and node_entries.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mpsb_cuda.h"
+#include "host_errors.h"
+#include "kernels.h"
+
+namespace mpsb {
+
+extern thread_local std::string g_error;
+
+template <class F>
+int guard(F&& body) {
+  try {
+    body();
+    g_error.clear();
+    return MPSB_OK;
+  } catch (const Error& e) {
+    g_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_error = "out of host memory";
+    return MPSB_ERR_BACKEND;
+  } catch (const std::exception& e) {
+    g_error = e.what();
+    return MPSB_ERR_BACKEND;
+  }
+}
+
+inline void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw BackendError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(expr) ::mpsb::cuda_check((expr), #expr)
+
+// Owning device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void alloc(size_t n) {
+    reset();
+    if (n == 0) n = 16;
+    const cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw BackendError("cudaMalloc of " + std::to_string(n) + " bytes failed: " +
+                         cudaGetErrorString(e));
+    }
+    bytes = n;
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+std::string describe_device_error(uint32_t bits);
+void fixed_scales(const float* pairs32, uint64_t n, uint64_t n_rows, int32_t* kg, int32_t* kh);
+void validate_tree_params(const mpsb_train_params& p, uint32_t features);
+
+}  // namespace mpsb
+
+struct mpsb_cuda_backend {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  int hist_mode = MPSB_HIST_FIXED;
+  int sm_count = 0;
+  cudaDeviceProp prop{};
+  mpsb::DevBuf error;  // one uint32 status word for standalone kernels
+
+  void activate() const { CK(cudaSetDevice(device)); }
+  uint32_t take_error() {
+    uint32_t e = 0;
+    CK(cudaMemcpyAsync(&e, error.p, sizeof e, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (e) CK(cudaMemsetAsync(error.p, 0, sizeof(uint32_t), stream));
+    return e;
+  }
+  ~mpsb_cuda_backend() {
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+struct mpsb_cuda_dataset {
+  mpsb_cuda_backend* backend = nullptr;
+  uint32_t n_rows = 0, features = 0, nfb = 0;
+  mpsb::DevBuf bins, bin_count, has_missing;
+  std::vector<uint32_t> h_bin_count;
+  std::vector<uint8_t> h_has_missing;
+};
+
+struct mpsb_cuda_model {
+  uint32_t n_trees = 0;
+  double base = 0.0, learning_rate = 0.1;
+  std::vector<std::vector<mpsb_tree_node>> trees;
+  std::vector<double> train_predictions;
+};
+

@@ -1,0 +1,1346 @@
+// Training-loop kernels for sm_103a (everything except the histogram build).
+//
+//   gradients      ComputeObjectiveGradients + ApplySampleWeights (trainer.cpp:178-216),
+//                  FP64 math rounded once to FP32 pairs, plus per-tree max|g| / max h for
+//                  the fixed-point scales.
+//   round_setup    fixed-point exponents, root node, level-0 build list.
+//   root_stats     root statistics from the root histogram; root leaf value
+//                  (TreeTrainingAccess::Create, tree_structure.cpp:104-116).
+//   subtract       SubtractHistograms (tree_histogram.cpp:16-66): exact int64 in fixed
+//                  mode, FP64 with the Hessian clamp in float mode.
+//   split_scan     FindBestSplit (tree_split.cpp:142-234): one warp per (node, feature),
+//                  warp-shuffle prefix over the 256 slots, FP64 gains with both missing
+//                  directions, random threshold, monotone and interaction rules.
+//   finalize       the per-level bookkeeping of TrainLevelWiseRegressionTree
+//                  (tree.cpp:67-145): acceptance under max_leaves, ApplySplit
+//                  (tree_structure.cpp:118-148), smaller-child selection, next level.
+//   partition      PrepareSplitRows' stable partition (tree_split.cpp:273-289) as a
+//                  ballot/popc compaction: count, per-node scan, scatter.
+//   apply_leaves   predictions += lr * leaf (trainer.cpp:256-262) from the final row
+//                  segments: no tree traversal.
+#include <algorithm>
+#include <cfloat>
+#include <type_traits>
+
+#include "device.cuh"
+#include "kernels.h"
+
+namespace mpsb {
+namespace {
+
+__device__ __forceinline__ void raise(Control* ctl, uint32_t bits) { atomicOr(&ctl->error, bits); }
+
+__device__ __forceinline__ uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+
+// Exponent e with x < 2^e (frexp convention) of a positive finite float.
+__device__ __forceinline__ int exponent_above(float x) {
+  int e;
+  frexpf(x, &e);
+  return e;
+}
+
+// Block-wide exclusive scan of N values per thread. `sh` holds >= 33*N words.
+template <int N>
+__device__ void block_scan(uint32_t (&v)[N], uint32_t (&total)[N], uint32_t* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  uint32_t incl[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    uint32_t x = v[k];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    incl[k] = x;
+    if (lane == 31) sh[warp * N + k] = x;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      uint32_t x = lane < nwarps ? sh[lane * N + k] : 0u;
+      const uint32_t own = x;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+      }
+      if (lane < nwarps) sh[lane * N + k] = x - own;
+      if (lane == 31) sh[32 * N + k] = x;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    total[k] = sh[32 * N + k];
+    v[k] = sh[warp * N + k] + incl[k] - v[k];
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------------------
+// Round begin / gradients / setup
+// ------------------------------------------------------------------------------------
+__global__ void round_begin_kernel(TrainerDev a) {
+  for (uint32_t i = threadIdx.x; i < a.n_slots; i += blockDim.x) a.free_stack[i] = a.n_slots - 1 - i;
+  for (uint32_t t = threadIdx.x; t < a.n_trees; t += blockDim.x) {
+    a.trees[t].max_abs_g_bits = 0;
+    a.trees[t].max_h_bits = 0;
+    a.trees[t].n_tree_nodes = 1;
+    a.trees[t].leaf_count = 1;
+  }
+  if (threadIdx.x == 0) {
+    a.ctl->free_top = a.n_slots;
+    a.ctl->n_leafseg = 0;
+    a.ctl->leaf_chunks = 0;
+    a.leaf_prefix[0] = 0;
+  }
+}
+
+__device__ __forceinline__ double logistic_probability(double m) {  // objective.cpp:309-317
+  if (m >= 0.0) {
+    const double e = exp(-m);
+    return __ddiv_rn(1.0, __dadd_rn(1.0, e));
+  }
+  const double e = exp(m);
+  return __ddiv_rn(e, __dadd_rn(1.0, e));
+}
+
+// Objective gradient of one row (objective.cpp:290-429). Returns false on a reference
+// TrainingError condition.
+__device__ __forceinline__ bool objective_pair(uint32_t objective, double y, double p,
+                                               const TreeParams& prm, double* g, double* h) {
+  if (!isfinite(y) || !isfinite(p)) return false;
+  switch (objective) {
+    case 0:
+      *g = __dadd_rn(p, -y);
+      *h = 1.0;
+      return isfinite(*g);
+    case 1: {
+      if (y != 0.0 && y != 1.0) return false;
+      const double prob = logistic_probability(p);
+      *g = __dadd_rn(prob, -y);
+      *h = __dmul_rn(prob, __dadd_rn(1.0, -prob));
+      return isfinite(*g) && isfinite(*h) && *h >= 0.0;
+    }
+    case 2:
+      *g = p < y ? -prm.objective_alpha : __dadd_rn(1.0, -prm.objective_alpha);
+      *h = 1.0;
+      return true;
+    case 3: {
+      if (y < 0.0 || p > 709.0) return false;
+      const double mean = exp(p);
+      *g = __dadd_rn(mean, -y);
+      *h = mean;
+      return isfinite(*g) && isfinite(*h) && *h > 0.0;
+    }
+    case 4: {
+      const double rho = prm.tweedie_variance_power;
+      const double a1 = __dmul_rn(__dadd_rn(2.0, -rho), p);
+      const double a2 = __dmul_rn(__dadd_rn(1.0, -rho), p);
+      if (y < 0.0 || a1 > 709.0 || a2 > 709.0) return false;
+      const double first = exp(a1), second = exp(a2);
+      *g = __dadd_rn(first, -__dmul_rn(y, second));
+      *h = __dadd_rn(__dmul_rn(__dadd_rn(2.0, -rho), first),
+                     -__dmul_rn(__dmul_rn(__dadd_rn(1.0, -rho), y), second));
+      return isfinite(*g) && isfinite(*h) && *h > 0.0;
+    }
+    default:
+      return false;
+  }
+}
+
+// grid = (x, n_trees): blockIdx.y is the tree, so a block's maxima belong to one tree.
+__global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
+  __shared__ uint32_t sg[8], shh[8];
+  const uint32_t t = blockIdx.y;
+  const size_t tree_off = size_t(t) * a.n_rows;
+  uint32_t mg = 0, mh = 0, bad = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_rows; i += gridDim.x * blockDim.x) {
+    double y = a.labels[i];
+    if (a.ovr) y = (y == double(t)) ? 1.0 : 0.0;
+    const double p = a.preds[tree_off + i];
+    double g = 0.0, h = 0.0;
+    if (!objective_pair(a.objective, y, p, a.params, &g, &h)) bad = 1;
+    if (a.weights != nullptr) {
+      const double w = a.weights_per_tree ? a.weights[tree_off + i] : a.weights[i];
+      g = __dmul_rn(g, w);
+      h = __dmul_rn(h, w);
+      if (!isfinite(g) || !isfinite(h) || h < 0.0) bad = 1;
+    }
+    const float g32 = __double2float_rn(g), h32 = __double2float_rn(h);
+    if (!isfinite(g32) || !isfinite(h32)) bad = 1;
+    a.gh[tree_off + i] = make_float2(g32, h32);
+    a.rows[size_t(t) * 2 * a.n_rows + i] = i;
+    mg = max(mg, __float_as_uint(fabsf(g32)));
+    mh = max(mh, __float_as_uint(fmaxf(h32, 0.0f)));
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    mg = max(mg, __shfl_xor_sync(0xffffffffu, mg, off));
+    mh = max(mh, __shfl_xor_sync(0xffffffffu, mh, off));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    sg[warp] = mg;
+    shh[warp] = mh;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < int(blockDim.x >> 5); ++w) {
+      mg = max(mg, sg[w]);
+      mh = max(mh, shh[w]);
+    }
+    atomicMax(&a.trees[t].max_abs_g_bits, mg);
+    atomicMax(&a.trees[t].max_h_bits, mh);
+  }
+  if (bad) raise(a.ctl, kErrGradient);
+}
+
+__global__ void round_setup_kernel(TrainerDev a) {
+  int en = 0;
+  while (en < 63 && (1ull << en) < uint64_t(a.n_rows)) ++en;
+  const uint32_t chunks_per_tree = ceil_div(a.n_rows, a.item_rows);
+  for (uint32_t base = 0; base < a.n_trees; base += blockDim.x) {
+    const uint32_t t = base + threadIdx.x;
+    if (t < a.n_trees) {
+      TreeState& s = a.trees[t];
+      const float mg = __uint_as_float(s.max_abs_g_bits), mh = __uint_as_float(s.max_h_bits);
+      s.kg = mg > 0.0f ? 61 - en - exponent_above(mg) : 0;
+      s.kh = mh > 0.0f ? 30 - exponent_above(mh) : 0;
+      s.inv_g = ldexp(1.0, -s.kg);
+      s.inv_h = ldexp(1.0, -s.kh);
+      const uint32_t slot = a.free_stack[a.n_slots - 1 - t];
+      NodeRec r;
+      r.seg_off = 0;
+      r.seg_cnt = a.n_rows;
+      r.node_index = 0;
+      r.slot = slot;
+      r.count = 0;
+      r.qg = r.qh = 0;
+      r.g = r.h = 0.0;
+      r.lo = -INFINITY;
+      r.hi = INFINITY;
+      r.tree = t;
+      r.depth = 0;
+      a.nodes[0][t] = r;
+      for (uint32_t w = 0; w < a.params.path_words; ++w) {
+        uint32_t allowed = 0xffffffffu;
+        if (a.params.n_groups > 0) {  // empty path: any group containing the feature
+          allowed = 0;
+          for (uint32_t g = 0; g < a.params.n_groups; ++g)
+            allowed |= a.group_masks[g * a.params.path_words + w];
+        }
+        if (a.tree_feature_masks != nullptr)
+          allowed &= a.tree_feature_masks[t * a.params.path_words + w];
+        a.node_path[0][t * a.params.path_words + w] = 0;
+        a.node_allowed[0][t * a.params.path_words + w] = allowed;
+      }
+      BuildEntry e;
+      e.tree = t;
+      e.parity = 0;
+      e.seg_off = 0;
+      e.seg_cnt = a.n_rows;
+      e.slot = slot;
+      e.pad = 0;
+      a.build[t] = e;
+      a.build_prefix[t] = t * chunks_per_tree;
+    }
+  }
+  if (threadIdx.x == 0) {
+    a.build_prefix[a.n_trees] = a.n_trees * chunks_per_tree;
+    a.ctl->free_top = a.n_slots - a.n_trees;
+    a.ctl->n_nodes = a.n_trees;
+    a.ctl->n_build = a.n_trees;
+    a.ctl->n_sub = 0;
+    a.ctl->n_part = 0;
+    a.ctl->hist_items = a.n_trees * chunks_per_tree * a.nfb;
+    a.ctl->hist_counter = 0;
+    a.ctl->split_items = a.n_trees * a.n_fchunks;
+  }
+}
+
+// Zero the histogram slots of the current build list.
+__global__ void zero_build_slots_kernel(TrainerDev a) {
+  const uint64_t words_per_slot = uint64_t(a.features) * kSlots * 3;
+  const uint64_t total = uint64_t(a.ctl->n_build) * (words_per_slot / 2);
+  for (uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; idx < total;
+       idx += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t e = uint32_t(idx / (words_per_slot / 2));
+    const uint64_t w = idx % (words_per_slot / 2);
+    reinterpret_cast<ulonglong2*>(a.hist + a.build[e].slot * words_per_slot)[w] =
+        make_ulonglong2(0, 0);
+  }
+}
+
+// Root statistics: the total of feature 0's slots (all rows, exact in fixed mode).
+__global__ void root_stats_kernel(TrainerDev a) {
+  const int lane = threadIdx.x & 31;
+  for (uint32_t t = threadIdx.x >> 5; t < a.n_trees; t += blockDim.x >> 5) {
+    NodeRec& r = a.nodes[0][t];
+    const unsigned long long* base = a.hist + size_t(r.slot) * a.features * kSlots * 3;
+    unsigned long long cnt = 0;
+    long long qg = 0, qh = 0;
+    for (int s = lane; s < kSlots; s += 32) {
+      cnt += base[s * 3 + 0];
+      qg += (long long)base[s * 3 + 1];
+      qh += (long long)base[s * 3 + 2];
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+      qg += __shfl_xor_sync(0xffffffffu, qg, off);
+      qh += __shfl_xor_sync(0xffffffffu, qh, off);
+    }
+    if (lane == 0) {
+      const TreeState& st = a.trees[t];
+      r.count = cnt;
+      if (a.mode == kModeFixed) {
+        r.qg = qg;
+        r.qh = qh;
+        r.g = q_image(qg, st.inv_g);
+        r.h = q_image(qh, st.inv_h);
+      } else {  // FP64 total in slot order
+        double g = 0.0, h = 0.0;
+        for (int s = 0; s < kSlots; ++s) {
+          g = __dadd_rn(g, __longlong_as_double((long long)base[s * 3 + 1]));
+          h = __dadd_rn(h, __longlong_as_double((long long)base[s * 3 + 2]));
+        }
+        r.g = g;
+        r.h = h;
+      }
+      if (cnt != r.seg_cnt) raise(a.ctl, kErrCountMismatch);
+      double leaf = 0.0;
+      if (!leaf_weight(r.g, r.h, a.params, &leaf)) raise(a.ctl, kErrNonFinite);
+      TreeNodeOut n;
+      n.feature_index = 0;
+      n.threshold_bin = 0;
+      n.left_child = 0xffffffffu;
+      n.right_child = 0xffffffffu;
+      n.leaf_value = leaf;
+      n.gain = 0.0;
+      n.default_left = 1;
+      n.flags = 1;
+      for (int k = 0; k < 6; ++k) n.reserved[k] = 0;
+      a.tree_nodes[size_t(t) * a.max_tree_nodes] = n;
+    }
+  }
+}
+
+// slot_parent := slot_parent - slot_built for every pair (the parent slot becomes the
+// sibling's histogram).
+__global__ void subtract_kernel(TrainerDev a) {
+  const uint64_t bins_per_slot = uint64_t(a.features) * kSlots;
+  const uint64_t total = uint64_t(a.ctl->n_sub) * bins_per_slot;
+  uint32_t err = 0;
+  for (uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; idx < total;
+       idx += uint64_t(gridDim.x) * blockDim.x) {
+    const SubEntry e = a.sub[idx / bins_per_slot];
+    const uint64_t b = idx % bins_per_slot;
+    unsigned long long* p = a.hist + (e.parent_slot * bins_per_slot + b) * 3;
+    const unsigned long long* c = a.hist + (e.built_slot * bins_per_slot + b) * 3;
+    const unsigned long long pc = p[0], cc = c[0];
+    if (cc > pc) err |= kErrSubtraction;
+    p[0] = pc - cc;
+    if (a.mode == kModeFixed) {
+      p[1] = p[1] - c[1];
+      p[2] = p[2] - c[2];
+    } else {
+      const double pg = __longlong_as_double((long long)p[1]);
+      const double cg = __longlong_as_double((long long)c[1]);
+      const double g = __dadd_rn(pg, -cg);
+      if (!isfinite(pg) || !isfinite(cg) || !isfinite(g)) err |= kErrNonFinite;
+      const double ph = __longlong_as_double((long long)p[2]);
+      const double ch = __longlong_as_double((long long)c[2]);
+      if (!isfinite(ph) || !isfinite(ch) || ph < 0.0 || ch < 0.0) err |= kErrHessian;
+      const double diff = __dadd_rn(ph, -ch);
+      const double tol = __dmul_rn(1e-5, fmax(1.0, fmax(fabs(ph), fabs(ch))));
+      if (diff < -tol) err |= kErrSubtraction;
+      p[1] = (unsigned long long)__double_as_longlong(g);
+      p[2] = (unsigned long long)__double_as_longlong(diff < 0.0 ? 0.0 : diff);
+    }
+  }
+  if (err) raise(a.ctl, err);
+}
+
+// ------------------------------------------------------------------------------------
+// Split scan
+// ------------------------------------------------------------------------------------
+// Node statistics of the scan: exact int64 (fixed) or FP64 (float).
+template <bool FIXED>
+struct Stat {
+  using V = typename std::conditional<FIXED, long long, double>::type;
+  unsigned long long count;
+  V g, h;
+};
+
+template <bool FIXED>
+__device__ __forceinline__ Stat<FIXED> stat_zero() {
+  Stat<FIXED> r;
+  r.count = 0;
+  r.g = 0;
+  r.h = 0;
+  return r;
+}
+
+template <bool FIXED>
+__device__ __forceinline__ Stat<FIXED> stat_add(Stat<FIXED> x, Stat<FIXED> y) {
+  Stat<FIXED> r;
+  r.count = x.count + y.count;
+  if constexpr (FIXED) {
+    r.g = x.g + y.g;
+    r.h = x.h + y.h;
+  } else {
+    r.g = __dadd_rn(x.g, y.g);
+    r.h = __dadd_rn(x.h, y.h);
+  }
+  return r;
+}
+
+template <bool FIXED>
+__device__ __forceinline__ Stat<FIXED> stat_sub(Stat<FIXED> x, Stat<FIXED> y) {
+  Stat<FIXED> r;
+  r.count = x.count - y.count;
+  if constexpr (FIXED) {
+    r.g = x.g - y.g;
+    r.h = x.h - y.h;
+  } else {
+    r.g = __dadd_rn(x.g, -y.g);
+    r.h = __dadd_rn(x.h, -y.h);
+  }
+  return r;
+}
+
+template <bool FIXED>
+__device__ __forceinline__ Stat<FIXED> shfl_up_stat(Stat<FIXED> s, int off) {
+  Stat<FIXED> r;
+  r.count = __shfl_up_sync(0xffffffffu, s.count, off);
+  r.g = __shfl_up_sync(0xffffffffu, s.g, off);
+  r.h = __shfl_up_sync(0xffffffffu, s.h, off);
+  return r;
+}
+
+template <bool FIXED>
+__device__ __forceinline__ Stat<FIXED> shfl_stat(Stat<FIXED> s, int src) {
+  Stat<FIXED> r;
+  r.count = __shfl_sync(0xffffffffu, s.count, src);
+  r.g = __shfl_sync(0xffffffffu, s.g, src);
+  r.h = __shfl_sync(0xffffffffu, s.h, src);
+  return r;
+}
+
+template <bool FIXED>
+__device__ __forceinline__ double image(typename Stat<FIXED>::V v, double inv) {
+  if constexpr (FIXED) return q_image(v, inv);
+  else return v;
+}
+
+// ConsiderMissingDirection (tree_split.cpp:65-115) + MonotonicBoundsForSplit
+// (tree_monotonic.cpp:12-58).
+template <bool FIXED>
+__device__ __forceinline__ void consider(const TreeParams& p, const Stat<FIXED>& cl,
+                                         const Stat<FIXED>& cr, double inv_g, double inv_h,
+                                         int8_t mono, double plo, double phi, uint32_t feature,
+                                         uint32_t threshold, uint32_t default_left,
+                                         SplitRec& best, uint32_t& err) {
+  if (cl.count < p.min_samples_leaf || cr.count < p.min_samples_leaf) return;
+  const double lh = image<FIXED>(cl.h, inv_h), rh = image<FIXED>(cr.h, inv_h);
+  if (lh < p.min_child_weight || rh < p.min_child_weight || lh <= 0.0 || rh <= 0.0) return;
+  const double lg = image<FIXED>(cl.g, inv_g), rg = image<FIXED>(cr.g, inv_g);
+  double gain;
+  if (!split_gain(lg, lh, rg, rh, p, &gain)) {
+    err |= kErrNonFinite;
+    return;
+  }
+  if (gain <= 0.0 || gain < p.min_gain_to_split) return;
+  double ll = plo, lu = phi, rl = plo, ru = phi;
+  if (mono != 0) {
+    double lv, rv;
+    if (!leaf_weight(lg, lh, p, &lv) || !leaf_weight(rg, rh, p, &rv)) {
+      err |= kErrNonFinite;
+      return;
+    }
+    lv = clamp_bounds(lv, plo, phi);
+    rv = clamp_bounds(rv, plo, phi);
+    if (mono > 0) {
+      if (lv > rv) return;
+      lu = (rv < lu) ? rv : lu;  // std::min(lu, rv)
+      rl = (rl < lv) ? lv : rl;  // std::max(rl, lv)
+    } else {
+      if (lv < rv) return;
+      ll = (ll < rv) ? rv : ll;  // std::max(ll, rv)
+      ru = (lv < ru) ? lv : ru;  // std::min(ru, lv)
+    }
+  }
+  SplitRec c;
+  c.gain = gain;
+  c.valid = 1;
+  c.feature = feature;
+  c.threshold = threshold;
+  c.default_left = default_left;
+  c.lcount = cl.count;
+  c.rcount = cr.count;
+  if constexpr (FIXED) {
+    c.lqg = cl.g;
+    c.lqh = cl.h;
+    c.rqg = cr.g;
+    c.rqh = cr.h;
+  } else {
+    c.lqg = c.lqh = c.rqg = c.rqh = 0;
+  }
+  c.lg = lg;
+  c.lh = lh;
+  c.rg = rg;
+  c.rh = rh;
+  c.ll = ll;
+  c.lu = lu;
+  c.rl = rl;
+  c.ru = ru;
+  if (better_split(c, best)) best = c;
+}
+
+// One warp per (node, feature); a CTA covers one node and blockDim/32 features and
+// writes the best split of its features to partial[node][chunk].
+template <bool FIXED>
+__global__ void split_scan_kernel(TrainerDev a, int parity) {
+  using V = typename Stat<FIXED>::V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SplitRec* warp_best = reinterpret_cast<SplitRec*>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const TreeParams& P = a.params;
+  const uint32_t n_chunks = a.n_fchunks;
+  const uint32_t items = a.ctl->n_nodes * n_chunks;
+  for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
+    const uint32_t i = item / n_chunks, c = item % n_chunks;
+    const NodeRec node = a.nodes[parity][i];
+    const double inv_g = a.trees[node.tree].inv_g, inv_h = a.trees[node.tree].inv_h;
+    const uint32_t f = c * uint32_t(nwarps) + uint32_t(warp);
+    SplitRec best;
+    best.valid = 0;
+    best.gain = 0.0;
+    best.feature = f;
+    best.threshold = 0;
+    best.default_left = 1;
+    uint32_t err = 0;
+    bool active = f < a.features;
+    if (active) {
+      const uint32_t allowed = a.node_allowed[parity][i * P.path_words + (f >> 5)];
+      active = (allowed >> (f & 31)) & 1u;
+    }
+    if (active) {  // warp-uniform
+      const uint32_t nb = a.bin_count[f];
+      const bool hm = a.has_missing[f] != 0;
+      const unsigned long long* base =
+          a.hist + (size_t(node.slot) * a.features + f) * kSlots * 3;
+      // Lane totals of 8 consecutive slots (the missing slot excluded from the scan).
+      Stat<FIXED> sum = stat_zero<FIXED>(), miss = stat_zero<FIXED>();
+      unsigned long long total_count = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int s = lane * 8 + k;
+        Stat<FIXED> b;
+        b.count = base[s * 3 + 0];
+        if constexpr (FIXED) {
+          b.g = (long long)base[s * 3 + 1];
+          b.h = (long long)base[s * 3 + 2];
+        } else {
+          b.g = __longlong_as_double((long long)base[s * 3 + 1]);
+          b.h = __longlong_as_double((long long)base[s * 3 + 2]);
+          if (!isfinite(b.g) || !isfinite(b.h) || b.h < 0.0) err |= kErrNonFinite;
+        }
+        total_count += b.count;
+        if (hm && s == kMissingSlot) {
+          miss = b;
+        } else {
+          sum = stat_add<FIXED>(sum, b);
+        }
+      }
+      miss = shfl_stat<FIXED>(miss, 31);
+      for (int off = 16; off > 0; off >>= 1)
+        total_count += __shfl_xor_sync(0xffffffffu, total_count, off);
+      Stat<FIXED> incl = sum;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const Stat<FIXED> y = shfl_up_stat<FIXED>(incl, off);
+        if (lane >= off) incl = stat_add<FIXED>(y, incl);
+      }
+      Stat<FIXED> left = shfl_up_stat<FIXED>(incl, 1);
+      if (lane == 0) left = stat_zero<FIXED>();
+      if (total_count != node.count) err |= kErrCountMismatch;
+      Stat<FIXED> parent;
+      parent.count = node.count;
+      if constexpr (FIXED) {
+        parent.g = node.qg;
+        parent.h = node.qh;
+      } else {
+        parent.g = node.g;
+        parent.h = node.h;
+      }
+      if (nb >= 2 && total_count == node.count) {
+        if (miss.count > parent.count || image<FIXED>(miss.h, inv_h) > image<FIXED>(parent.h, inv_h))
+          err |= kErrMissing;
+        const Stat<FIXED> nmp = stat_sub<FIXED>(parent, miss);
+        const int8_t mono = P.has_monotonic ? a.monotonic[f] : 0;
+        const uint32_t rnd =
+            P.split_strategy == 1
+                ? stable_random_threshold(P.random_seed, f, node.node_index, node.depth, nb - 1)
+                : 0xffffffffu;
+#pragma unroll 1
+        for (int k = 0; k < 8; ++k) {
+          const int s = lane * 8 + k;
+          if (!(hm && s == kMissingSlot)) {  // reload the slot (L1-resident)
+            Stat<FIXED> b;
+            b.count = base[s * 3 + 0];
+            if constexpr (FIXED) {
+              b.g = (long long)base[s * 3 + 1];
+              b.h = (long long)base[s * 3 + 2];
+            } else {
+              b.g = __longlong_as_double((long long)base[s * 3 + 1]);
+              b.h = __longlong_as_double((long long)base[s * 3 + 2]);
+            }
+            left = stat_add<FIXED>(left, b);
+          }
+          const uint32_t t = uint32_t(s);
+          if (t + 1 >= nb) continue;
+          const Stat<FIXED> right = stat_sub<FIXED>(nmp, left);
+          if (left.count > nmp.count) {
+            err |= kErrPrefix;
+            continue;
+          }
+          if (left.count == 0 && right.count == 0) continue;
+          if (P.split_strategy == 1 && t != rnd) continue;
+          consider<FIXED>(P, stat_add<FIXED>(left, miss), right, inv_g, inv_h, mono, node.lo,
+                          node.hi, f, t, 1u, best, err);
+          if (miss.count > 0)
+            consider<FIXED>(P, left, stat_add<FIXED>(right, miss), inv_g, inv_h, mono, node.lo,
+                            node.hi, f, t, 0u, best, err);
+        }
+      }
+    }
+    if (err) raise(a.ctl, err);
+    // Warp argmax (all lanes share the feature): every lane ends with the winner's id.
+    uint32_t win = uint32_t(lane);
+    {
+      double g = best.gain;
+      uint32_t v = best.valid, thr = best.threshold, dl = best.default_left;
+      for (int off = 16; off > 0; off >>= 1) {
+        const double og = __shfl_xor_sync(0xffffffffu, g, off);
+        const uint32_t ov = __shfl_xor_sync(0xffffffffu, v, off);
+        const uint32_t ot = __shfl_xor_sync(0xffffffffu, thr, off);
+        const uint32_t od = __shfl_xor_sync(0xffffffffu, dl, off);
+        const uint32_t ow = __shfl_xor_sync(0xffffffffu, win, off);
+        bool take;
+        if (ov != v) take = ov > v;
+        else if (!v) take = ow < win;
+        else if (og != g) take = og > g;
+        else if (ot != thr) take = ot < thr;
+        else if (od != dl) take = od > dl;
+        else take = ow < win;
+        if (take) {
+          g = og;
+          v = ov;
+          thr = ot;
+          dl = od;
+          win = ow;
+        }
+      }
+    }
+    if (uint32_t(lane) == win) warp_best[warp] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      SplitRec b = warp_best[0];
+      for (int w = 1; w < nwarps; ++w)
+        if (better_split(warp_best[w], b)) b = warp_best[w];
+      a.partial[size_t(i) * n_chunks + c] = b;
+    }
+    __syncthreads();
+  }
+  (void)sizeof(V);
+}
+
+// ------------------------------------------------------------------------------------
+// Level finalize (one CTA)
+// ------------------------------------------------------------------------------------
+__device__ void write_leaf(TreeNodeOut* dst, double value) {
+  TreeNodeOut n;
+  n.feature_index = 0;
+  n.threshold_bin = 0;
+  n.left_child = 0xffffffffu;
+  n.right_child = 0xffffffffu;
+  n.leaf_value = value;
+  n.gain = 0.0;
+  n.default_left = 1;
+  n.flags = 1;
+  for (int k = 0; k < 6; ++k) n.reserved[k] = 0;
+  *dst = n;
+}
+
+__device__ bool bounded_leaf(const TreeParams& p, double g, double h, double lo, double hi,
+                             double* out) {
+  if (lo > hi) return false;
+  double w;
+  if (!leaf_weight(g, h, p, &w)) return false;
+  *out = clamp_bounds(w, lo, hi);
+  return true;
+}
+
+__global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity, uint32_t depth) {
+  __shared__ uint32_t sh[33 * 6];
+  Control* ctl = a.ctl;
+  const TreeParams& P = a.params;
+  const uint32_t n = ctl->n_nodes;
+  const uint32_t W = P.path_words;
+  const bool last = depth + 1 >= P.max_depth;  // children are leaves
+  const uint32_t* tree_base = a.tree_scratch;                 // [T] valid prefix at first node
+  uint32_t* tree_acc_base = a.tree_scratch + a.n_trees;       // [T] accepted prefix at first node
+  uint32_t* tree_acc = a.tree_scratch + 2 * a.n_trees;        // [T] accepted count
+  uint32_t* tree_vbase = a.tree_scratch;
+  for (uint32_t t = threadIdx.x; t < a.n_trees; t += blockDim.x) tree_acc[t] = 0;
+  __syncthreads();
+
+  // Phase A: best split per node, valid flags, valid prefix.
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < n; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t v[1] = {0};
+    uint32_t tree = 0;
+    bool first = false;
+    if (i < n) {
+      if (depth < P.max_depth) {  // nodes at max_depth never split (tree.cpp:152-154)
+        SplitRec b = a.partial[size_t(i) * a.n_fchunks];
+        for (uint32_t c = 1; c < a.n_fchunks; ++c) {
+          const SplitRec x = a.partial[size_t(i) * a.n_fchunks + c];
+          if (better_split(x, b)) b = x;
+        }
+        a.partial[size_t(i) * a.n_fchunks] = b;
+        v[0] = b.valid;
+      }
+      tree = a.nodes[parity][i].tree;
+      first = i == 0 || a.nodes[parity][i - 1].tree != tree;
+    }
+    uint32_t tot[1];
+    const uint32_t own = v[0];
+    block_scan<1>(v, tot, sh);
+    if (i < n) {
+      a.scratch_flags[i] = own;
+      a.scratch_prefix[i] = carry + v[0];
+      if (first) tree_vbase[tree] = carry + v[0];
+    }
+    carry += tot[0];
+    __syncthreads();
+  }
+  __syncthreads();
+
+  // Phase B1: acceptance under max_leaves, accepted prefix, chunk prefixes.
+  // Scanned values: 0 accepted, 1 build chunks, 2 partition chunks, 3 leaf segments,
+  // 4 leaf chunks, 5 freed slots.
+  uint32_t carry6[6] = {0, 0, 0, 0, 0, 0};
+  const uint32_t leafseg_base = ctl->n_leafseg;
+  const uint32_t leafchunk_base = ctl->leaf_chunks;
+  for (uint32_t base = 0; base < n; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t v[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t tree = 0;
+    bool first = false;
+    if (i < n) {
+      const NodeRec node = a.nodes[parity][i];
+      tree = node.tree;
+      first = i == 0 || a.nodes[parity][i - 1].tree != tree;
+      const uint32_t within = a.scratch_prefix[i] - tree_base[tree];
+      const bool acc = a.scratch_flags[i] && (a.trees[tree].leaf_count + within < P.max_leaves);
+      v[0] = acc;
+      if (acc) {
+        const SplitRec& b = a.partial[size_t(i) * a.n_fchunks];
+        const uint32_t built = uint32_t(b.lcount <= b.rcount ? b.lcount : b.rcount);
+        if (!last) {
+          v[1] = ceil_div(built, a.item_rows);
+          v[2] = ceil_div(node.seg_cnt, kPartChunk);
+        }
+      }
+      const bool leafseg = !acc || last;
+      v[3] = leafseg;
+      v[4] = leafseg ? ceil_div(node.seg_cnt, kApplyChunk) : 0;
+      v[5] = (!acc && !last) ? 1u : 0u;
+    }
+    const uint32_t own0 = v[0];
+    uint32_t tot[6];
+    block_scan<6>(v, tot, sh);
+    if (i < n) {
+      a.scratch_flags[i] = own0;
+      a.scratch_prefix[i] = carry6[0] + v[0];
+      a.scratch_aux[i] = carry6[5] + v[5];
+      if (first) tree_acc_base[tree] = carry6[0] + v[0];
+      if (own0) {
+        const uint32_t k = carry6[0] + v[0];
+        if (!last) {
+          a.build_prefix[k] = carry6[1] + v[1];
+          a.part_prefix[k] = carry6[2] + v[2];
+        }
+      }
+      if (!own0 || last) a.leaf_prefix[leafseg_base + carry6[3] + v[3]] = leafchunk_base + carry6[4] + v[4];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) carry6[k] += tot[k];
+    __syncthreads();
+  }
+  const uint32_t n_acc = carry6[0];
+  const uint32_t free_top = ctl->free_top;
+  __syncthreads();
+
+  // Phase B2: apply splits, next-level nodes, build / subtract / partition / leaf lists.
+  uint32_t err = 0;
+  NodeRec* next = a.nodes[parity ^ 1];
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const NodeRec node = a.nodes[parity][i];
+    const uint32_t t = node.tree;
+    TreeNodeOut* tn = a.tree_nodes + size_t(t) * a.max_tree_nodes;
+    const bool acc = a.scratch_flags[i] != 0;
+    if (acc) {
+      const SplitRec b = a.partial[size_t(i) * a.n_fchunks];
+      const uint32_t k = a.scratch_prefix[i];
+      const uint32_t kt = k - tree_acc_base[t];
+      atomicAdd(&tree_acc[t], 1u);
+      const uint32_t li = a.trees[t].n_tree_nodes + 2 * kt, ri = li + 1;
+      if (ri >= a.max_tree_nodes) {
+        err |= kErrCapacity;
+        continue;
+      }
+      double lv = 0.0, rv = 0.0;
+      if (!bounded_leaf(P, b.lg, b.lh, b.ll, b.lu, &lv)) err |= kErrNonFinite;
+      if (!bounded_leaf(P, b.rg, b.rh, b.rl, b.ru, &rv)) err |= kErrNonFinite;
+      write_leaf(&tn[li], lv);
+      write_leaf(&tn[ri], rv);
+      TreeNodeOut& pn = tn[node.node_index];
+      pn.feature_index = b.feature;
+      pn.threshold_bin = b.threshold;
+      pn.left_child = li;
+      pn.right_child = ri;
+      pn.leaf_value = 0.0;
+      pn.gain = b.gain;
+      pn.default_left = uint8_t(b.default_left);
+      pn.flags = 0;
+      if (b.lcount + b.rcount != node.seg_cnt) err |= kErrPartition;
+      if (!last) {
+        const bool build_left = b.lcount <= b.rcount;
+        const uint32_t new_slot = a.free_stack[free_top - 1 - k];
+        NodeRec L, R;
+        L.seg_off = node.seg_off;
+        L.seg_cnt = uint32_t(b.lcount);
+        R.seg_off = node.seg_off + uint32_t(b.lcount);
+        R.seg_cnt = uint32_t(b.rcount);
+        L.node_index = li;
+        R.node_index = ri;
+        L.slot = build_left ? new_slot : node.slot;
+        R.slot = build_left ? node.slot : new_slot;
+        L.count = b.lcount;
+        R.count = b.rcount;
+        L.qg = b.lqg;
+        L.qh = b.lqh;
+        R.qg = b.rqg;
+        R.qh = b.rqh;
+        L.g = b.lg;
+        L.h = b.lh;
+        R.g = b.rg;
+        R.h = b.rh;
+        L.lo = b.ll;
+        L.hi = b.lu;
+        R.lo = b.rl;
+        R.hi = b.ru;
+        L.tree = R.tree = t;
+        L.depth = R.depth = node.depth + 1;
+        next[2 * k] = L;
+        next[2 * k + 1] = R;
+        for (uint32_t w = 0; w < W; ++w) {
+          uint32_t path = a.node_path[parity][i * W + w];
+          if ((b.feature >> 5) == w) path |= 1u << (b.feature & 31);
+          a.node_path[parity ^ 1][(2 * k) * W + w] = path;
+          a.node_path[parity ^ 1][(2 * k + 1) * W + w] = path;
+        }
+        for (uint32_t w = 0; w < W; ++w) {
+          uint32_t allowed = 0xffffffffu;
+          if (P.n_groups > 0) {  // InteractionAllowsFeature (tree_interactions.cpp:32-45)
+            allowed = 0;
+            for (uint32_t g = 0; g < P.n_groups; ++g) {
+              bool subset = true;
+              for (uint32_t u = 0; u < W && subset; ++u) {
+                const uint32_t gm = a.group_masks[g * W + u];
+                subset = (a.node_path[parity ^ 1][(2 * k) * W + u] & ~gm) == 0;
+              }
+              if (subset) allowed |= a.group_masks[g * W + w];
+            }
+          }
+          if (a.tree_feature_masks != nullptr) allowed &= a.tree_feature_masks[t * W + w];
+          a.node_allowed[parity ^ 1][(2 * k) * W + w] = allowed;
+          a.node_allowed[parity ^ 1][(2 * k + 1) * W + w] = allowed;
+        }
+        BuildEntry be;
+        be.tree = t;
+        be.parity = uint32_t(parity ^ 1);
+        be.seg_off = build_left ? L.seg_off : R.seg_off;
+        be.seg_cnt = build_left ? L.seg_cnt : R.seg_cnt;
+        be.slot = new_slot;
+        be.pad = 0;
+        a.build[k] = be;
+        SubEntry se;
+        se.parent_slot = node.slot;
+        se.built_slot = new_slot;
+        a.sub[k] = se;
+        PartEntry pe;
+        pe.tree = t;
+        pe.parity = uint32_t(parity);
+        pe.seg_off = node.seg_off;
+        pe.seg_cnt = node.seg_cnt;
+        pe.feature = b.feature;
+        pe.threshold = b.threshold;
+        pe.default_left = b.default_left;
+        pe.lcount = uint32_t(b.lcount);
+        a.part[k] = pe;
+      }
+      if (last) {
+        // leaf segment index: number of leaf segments before node i in this level
+        // equals i (every node of the last level produces one).
+        LeafSeg ls;
+        ls.tree = t;
+        ls.parity = uint32_t(parity);
+        ls.seg_off = node.seg_off;
+        ls.seg_cnt = node.seg_cnt;
+        ls.split = 1;
+        ls.feature = b.feature;
+        ls.threshold = b.threshold;
+        ls.default_left = b.default_left;
+        ls.value = 0.0;
+        ls.left_value = lv;
+        ls.right_value = rv;
+        if (leafseg_base + i < a.max_leafsegs) a.leafseg[leafseg_base + i] = ls;
+        else err |= kErrCapacity;
+      }
+    } else {
+      // Node stays a leaf: its rows keep the current leaf value.
+      const uint32_t before_acc = a.scratch_prefix[i];
+      const uint32_t idx = last ? i : (i - before_acc);  // leaf segments before i
+      LeafSeg ls;
+      ls.tree = t;
+      ls.parity = uint32_t(parity);
+      ls.seg_off = node.seg_off;
+      ls.seg_cnt = node.seg_cnt;
+      ls.split = 0;
+      ls.feature = ls.threshold = ls.default_left = 0;
+      ls.value = tn[node.node_index].leaf_value;
+      ls.left_value = ls.right_value = 0.0;
+      if (leafseg_base + idx < a.max_leafsegs) a.leafseg[leafseg_base + idx] = ls;
+      else err |= kErrCapacity;
+    }
+  }
+  __syncthreads();
+  // Phase C: free slots of nodes that stopped (non-last levels), counters.
+  if (!last) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      if (!a.scratch_flags[i]) {
+        const uint32_t j = a.scratch_aux[i];
+        a.free_stack[free_top - n_acc + j] = a.nodes[parity][i].slot;
+      }
+    }
+  }
+  __syncthreads();
+  for (uint32_t t = threadIdx.x; t < a.n_trees; t += blockDim.x) {
+    a.trees[t].n_tree_nodes += 2 * tree_acc[t];
+    a.trees[t].leaf_count += tree_acc[t];
+  }
+  if (err) raise(ctl, err);
+  if (threadIdx.x == 0) {
+    const uint32_t n_leafseg_level = carry6[3];
+    ctl->n_leafseg = leafseg_base + n_leafseg_level;
+    ctl->leaf_chunks = leafchunk_base + carry6[4];
+    if (leafseg_base + n_leafseg_level <= a.max_leafsegs)
+      a.leaf_prefix[leafseg_base + n_leafseg_level] = leafchunk_base + carry6[4];
+    if (last) {
+      ctl->n_nodes = 0;
+      ctl->n_build = 0;
+      ctl->n_sub = 0;
+      ctl->n_part = 0;
+      ctl->hist_items = 0;
+      ctl->part_chunks = 0;
+      ctl->split_items = 0;
+    } else {
+      ctl->free_top = free_top - n_acc + (n - n_acc);
+      ctl->n_nodes = 2 * n_acc;
+      ctl->n_build = n_acc;
+      ctl->n_sub = n_acc;
+      ctl->n_part = n_acc;
+      a.build_prefix[n_acc] = carry6[1];
+      a.part_prefix[n_acc] = carry6[2];
+      ctl->hist_items = carry6[1] * a.nfb;
+      ctl->part_chunks = carry6[2];
+      ctl->split_items = 2 * n_acc * a.n_fchunks;
+    }
+    ctl->hist_counter = 0;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Partition
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t find_entry(const uint32_t* prefix, uint32_t n, uint32_t c) {
+  uint32_t lo = 0, hi = n;  // last entry with prefix <= c
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (prefix[mid] <= c) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ bool row_goes_left(const TrainerDev& a, uint32_t row, uint32_t f,
+                                              uint32_t thr, uint32_t dl) {
+  const uint8_t b =
+      a.bins[(size_t(f >> 5) * a.n_rows + row) * kBlockFeatures + (f & 31)];
+  if (a.has_missing[f] && b == kMissingSlot) return dl != 0;
+  return b <= thr;
+}
+
+constexpr int kPartThreads = 512;
+constexpr int kPartPerThread = kPartChunk / kPartThreads;  // 8
+
+__global__ void __launch_bounds__(kPartThreads) partition_count_kernel(TrainerDev a) {
+  __shared__ uint32_t warp_counts[kPartThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t c = blockIdx.x; c < a.ctl->part_chunks; c += gridDim.x) {
+    const uint32_t e = find_entry(a.part_prefix, a.ctl->n_part, c);
+    const PartEntry pe = a.part[e];
+    const uint32_t lc = c - a.part_prefix[e];
+    const uint32_t start = lc * kPartChunk;
+    const uint32_t count = min(kPartChunk, pe.seg_cnt - start);
+    const uint32_t* rows = a.rows + (size_t(pe.tree) * 2 + pe.parity) * a.n_rows + pe.seg_off + start;
+    uint32_t mine = 0;
+#pragma unroll
+    for (int k = 0; k < kPartPerThread; ++k) {
+      const uint32_t p = uint32_t(k * kPartThreads) + threadIdx.x;
+      bool left = false;
+      if (p < count) {
+        const uint32_t r = rows[p];
+        left = r < a.n_rows && row_goes_left(a, r, pe.feature, pe.threshold, pe.default_left);
+      }
+      const uint32_t word = __ballot_sync(0xffffffffu, left);
+      if (lane == 0) a.part_flags[size_t(c) * (kPartChunk / 32) + k * (kPartThreads / 32) + warp] = word;
+      mine += left;
+    }
+    for (int off = 16; off > 0; off >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, off);
+    if (lane == 0) warp_counts[warp] = mine;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t s = 0;
+      for (int w = 0; w < kPartThreads / 32; ++w) s += warp_counts[w];
+      a.part_counts[c] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// Exclusive prefix of the chunk counts of each partitioned node.
+__global__ void __launch_bounds__(1024) partition_scan_kernel(TrainerDev a) {
+  __shared__ uint32_t sh[33];
+  uint32_t err = 0;
+  for (uint32_t e = blockIdx.x; e < a.ctl->n_part; e += gridDim.x) {
+    const uint32_t c0 = a.part_prefix[e], c1 = a.part_prefix[e + 1];
+    uint32_t carry = 0;
+    for (uint32_t base = c0; base < c1; base += blockDim.x) {
+      const uint32_t c = base + threadIdx.x;
+      uint32_t v[1] = {c < c1 ? a.part_counts[c] : 0u};
+      uint32_t tot[1];
+      block_scan<1>(v, tot, sh);
+      if (c < c1) a.part_offsets[c] = carry + v[0];
+      carry += tot[0];
+    }
+    if (carry != a.part[e].lcount) err |= kErrPartition;
+    __syncthreads();
+  }
+  if (err && threadIdx.x == 0) raise(a.ctl, err);
+}
+
+__global__ void __launch_bounds__(kPartThreads) partition_scatter_kernel(TrainerDev a) {
+  constexpr int kWords = kPartChunk / 32;  // 128
+  __shared__ uint32_t word_prefix[kWords];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t err = 0;
+  for (uint32_t c = blockIdx.x; c < a.ctl->part_chunks; c += gridDim.x) {
+    const uint32_t e = find_entry(a.part_prefix, a.ctl->n_part, c);
+    const PartEntry pe = a.part[e];
+    const uint32_t lc = c - a.part_prefix[e];
+    const uint32_t start = lc * kPartChunk;
+    const uint32_t count = min(kPartChunk, pe.seg_cnt - start);
+    const uint32_t* flags = a.part_flags + size_t(c) * kWords;
+    // Exclusive prefix of the word popcounts, in position order.
+    if (warp == 0) {
+      uint32_t cnt[4], s = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        cnt[q] = __popc(flags[lane * 4 + q]);
+        s += cnt[q];
+      }
+      uint32_t x = s;
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+      }
+      uint32_t run = x - s;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        word_prefix[lane * 4 + q] = run;
+        run += cnt[q];
+      }
+    }
+    __syncthreads();
+    const uint32_t* src = a.rows + (size_t(pe.tree) * 2 + pe.parity) * a.n_rows + pe.seg_off + start;
+    uint32_t* dst = a.rows + (size_t(pe.tree) * 2 + (pe.parity ^ 1)) * a.n_rows + pe.seg_off;
+    const uint32_t left_before_chunk = a.part_offsets[c];
+    const uint32_t right_before_chunk = start - left_before_chunk;
+#pragma unroll
+    for (int k = 0; k < kPartPerThread; ++k) {
+      const uint32_t p = uint32_t(k * kPartThreads) + threadIdx.x;
+      const int wi = k * (kPartThreads / 32) + warp;
+      const uint32_t word = flags[wi];
+      if (p < count) {
+        const uint32_t below = __popc(word & ((1u << lane) - 1u));
+        const uint32_t lpos = word_prefix[wi] + below;  // left rows before p in the chunk
+        const bool left = (word >> lane) & 1u;
+        const uint32_t r = src[p];
+        const uint32_t rel = left ? left_before_chunk + lpos : pe.lcount + right_before_chunk + (p - lpos);
+        if (rel < pe.seg_cnt) dst[rel] = r;  // always true when the counts agree
+        else err = kErrPartition;
+      }
+    }
+    __syncthreads();
+  }
+  if (err) raise(a.ctl, err);
+}
+
+// ------------------------------------------------------------------------------------
+// Leaf application and round end
+// ------------------------------------------------------------------------------------
+__global__ void apply_leaves_kernel(TrainerDev a) {
+  const double lr = a.params.learning_rate;
+  uint32_t err = 0;
+  const uint32_t n_seg = a.ctl->n_leafseg;
+  const uint32_t chunks = a.ctl->leaf_chunks;
+  for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+    const uint32_t s = find_entry(a.leaf_prefix, n_seg, c);
+    const LeafSeg ls = a.leafseg[s];
+    const uint32_t start = (c - a.leaf_prefix[s]) * kApplyChunk;
+    const uint32_t count = min(kApplyChunk, ls.seg_cnt - start);
+    const uint32_t* rows = a.rows + (size_t(ls.tree) * 2 + ls.parity) * a.n_rows + ls.seg_off + start;
+    double* pred = a.preds + size_t(ls.tree) * a.n_rows;
+    for (uint32_t p = threadIdx.x; p < count; p += blockDim.x) {
+      const uint32_t r = rows[p];
+      if (r >= a.n_rows) {
+        err = kErrCapacity;
+        continue;
+      }
+      double v = ls.value;
+      if (ls.split)
+        v = row_goes_left(a, r, ls.feature, ls.threshold, ls.default_left) ? ls.left_value
+                                                                           : ls.right_value;
+      const double out = __dadd_rn(pred[r], __dmul_rn(lr, v));
+      if (!isfinite(out)) err = kErrNonFinite;
+      pred[r] = out;
+    }
+  }
+  if (err) raise(a.ctl, err);
+}
+
+__global__ void round_end_kernel(TrainerDev a) {
+  const uint32_t round = *a.round_counter;
+  if (round >= a.max_rounds) {
+    if (threadIdx.x == 0) raise(a.ctl, kErrCapacity);
+    return;
+  }
+  for (uint32_t t = 0; t < a.n_trees; ++t) {
+    const uint32_t cnt = a.trees[t].n_tree_nodes;
+    const TreeNodeOut* src = a.tree_nodes + size_t(t) * a.max_tree_nodes;
+    TreeNodeOut* dst = a.model_nodes + (size_t(round) * a.n_trees + t) * a.max_tree_nodes;
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) dst[i] = src[i];
+    if (threadIdx.x == 0) a.model_counts[size_t(round) * a.n_trees + t] = cnt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *a.round_counter = round + 1;
+}
+
+// ------------------------------------------------------------------------------------
+// Standalone entries
+// ------------------------------------------------------------------------------------
+__global__ void squared_error_kernel(const double* labels, const double* preds, uint64_t n,
+                                     double* out, uint32_t* error) {
+  uint32_t bad = 0;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    const double y = labels[i], p = preds[i];
+    const double g = __dadd_rn(p, -y);
+    if (!isfinite(y) || !isfinite(p) || !isfinite(g)) bad = 1;
+    out[2 * i] = g;
+    out[2 * i + 1] = 1.0;
+  }
+  if (bad) atomicOr(error, kErrGradient);
+}
+
+// RegressionModel::Predict (trainer.cpp:268-282): per row, trees in order,
+// result += lr * leaf; traversal of RegressionTree::Predict (tree.cpp:179-214).
+__global__ void predict_kernel(const uint8_t* bins, uint32_t n_rows, const uint8_t* has_missing,
+                               const TreeNodeOut* nodes, const uint32_t* tree_offsets,
+                               uint32_t n_trees, double base, double lr, double* out,
+                               uint32_t* error) {
+  uint32_t bad = 0;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+    double acc = base;
+    for (uint32_t t = 0; t < n_trees; ++t) {
+      const TreeNodeOut* tn = nodes + tree_offsets[t];
+      const uint32_t size = tree_offsets[t + 1] - tree_offsets[t];
+      uint32_t node = 0, visited = 0;
+      for (;;) {
+        if (node >= size || ++visited > size) {
+          bad = 1;
+          break;
+        }
+        const TreeNodeOut nd = tn[node];
+        if (nd.flags & 1u) {
+          acc = __dadd_rn(acc, __dmul_rn(lr, nd.leaf_value));
+          break;
+        }
+        const uint32_t f = nd.feature_index;
+        const uint8_t b = bins[(size_t(f >> 5) * n_rows + r) * kBlockFeatures + (f & 31)];
+        const bool left = (has_missing[f] && b == kMissingSlot) ? nd.default_left != 0
+                                                                 : b <= nd.threshold_bin;
+        node = left ? nd.left_child : nd.right_child;
+      }
+    }
+    out[r] = acc;
+  }
+  if (bad) atomicOr(error, kErrCapacity);
+}
+
+// Feature-major [features][rows] bins (u8 or u16) + optional missing mask ->
+// column-blocked u8 [nfb][rows][32] with missing rows at slot 255. Out-of-range bins
+// raise kErrGradient-free data errors through `error` (bit 0).
+__global__ void pack_bins_kernel(const void* src, uint32_t width, const uint8_t* missing,
+                                 const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
+                                 uint32_t nfb, uint8_t* out, uint32_t* error) {
+  __shared__ uint8_t tile[32][129];
+  const uint32_t fb = blockIdx.y;
+  uint32_t bad = 0;
+  for (uint32_t r0 = blockIdx.x * 128; r0 < n_rows; r0 += gridDim.x * 128) {
+    // load 32 features x 128 rows (coalesced along rows)
+    for (uint32_t k = threadIdx.x; k < 32 * 128; k += blockDim.x) {
+      const uint32_t c = k / 128, r = k % 128;
+      const uint32_t f = fb * 32 + c, row = r0 + r;
+      uint8_t v = 0;
+      if (f < features && row < n_rows) {
+        const size_t idx = size_t(f) * n_rows + row;
+        const uint32_t b = width == 1 ? static_cast<const uint8_t*>(src)[idx]
+                                      : static_cast<const uint16_t*>(src)[idx];
+        const bool miss = missing != nullptr && missing[idx] != 0;
+        if (miss) {
+          if (bin_count[f] > 255) bad = 1;
+          v = uint8_t(kMissingSlot);
+        } else {
+          if (b >= bin_count[f]) bad = 1;
+          v = uint8_t(b);
+        }
+      }
+      tile[c][r] = v;
+    }
+    __syncthreads();
+    // store 128 rows x 32 bytes (coalesced along the block row)
+    for (uint32_t k = threadIdx.x; k < 32 * 128; k += blockDim.x) {
+      const uint32_t r = k / 32, c = k % 32;
+      const uint32_t row = r0 + r;
+      if (row < n_rows) out[(size_t(fb) * n_rows + row) * kBlockFeatures + c] = tile[c][r];
+    }
+    __syncthreads();
+  }
+  if (bad) atomicOr(error, 1u);
+}
+
+}  // namespace
+
+cudaError_t launch_round_begin(const TrainerDev& a, cudaStream_t s) {
+  round_begin_kernel<<<1, 1024, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_gradients(const TrainerDev& a, int grid, cudaStream_t s) {
+  gradients_kernel<<<dim3(grid, a.n_trees), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_round_setup(const TrainerDev& a, cudaStream_t s) {
+  round_setup_kernel<<<1, 1024, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_zero_build_slots(const TrainerDev& a, int grid, cudaStream_t s) {
+  zero_build_slots_kernel<<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_root_stats(const TrainerDev& a, cudaStream_t s) {
+  root_stats_kernel<<<1, 1024, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t s) {
+  subtract_kernel<<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStream_t s) {
+  const int threads = int(a.scan_threads);
+  const size_t smem = sizeof(SplitRec) * (threads / 32);
+  if (a.mode == kModeFixed) split_scan_kernel<true><<<grid, threads, smem, s>>>(a, parity);
+  else split_scan_kernel<false><<<grid, threads, smem, s>>>(a, parity);
+  return cudaGetLastError();
+}
+cudaError_t launch_finalize(const TrainerDev& a, int parity, uint32_t depth, cudaStream_t s) {
+  finalize_kernel<<<1, 1024, 0, s>>>(a, parity, depth);
+  return cudaGetLastError();
+}
+cudaError_t launch_partition(const TrainerDev& a, int grid, cudaStream_t s) {
+  partition_count_kernel<<<grid, kPartThreads, 0, s>>>(a);
+  partition_scan_kernel<<<grid, 1024, 0, s>>>(a);
+  partition_scatter_kernel<<<grid, kPartThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_partition_count(const TrainerDev& a, int grid, cudaStream_t s) {
+  partition_count_kernel<<<grid, kPartThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_partition_finish(const TrainerDev& a, int grid, cudaStream_t s) {
+  partition_scan_kernel<<<grid, 1024, 0, s>>>(a);
+  partition_scatter_kernel<<<grid, kPartThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_apply_leaves(const TrainerDev& a, int grid, cudaStream_t s) {
+  apply_leaves_kernel<<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_round_end(const TrainerDev& a, cudaStream_t s) {
+  round_end_kernel<<<1, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_squared_error(const double* labels, const double* preds, uint64_t n,
+                                 double* out, uint32_t* error, cudaStream_t s) {
+  const int grid = int(std::min<uint64_t>((n + 255) / 256, 152ull * 16));
+  squared_error_kernel<<<grid > 0 ? grid : 1, 256, 0, s>>>(labels, preds, n, out, error);
+  return cudaGetLastError();
+}
+cudaError_t launch_pack_bins(const void* src, uint32_t width, const uint8_t* missing,
+                             const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
+                             uint32_t nfb, uint8_t* out, uint32_t* error, cudaStream_t s) {
+  const uint32_t gx = std::min<uint32_t>((n_rows + 127) / 128, 4096u);
+  pack_bins_kernel<<<dim3(gx > 0 ? gx : 1, nfb), 256, 0, s>>>(src, width, missing, bin_count,
+                                                              n_rows, features, nfb, out, error);
+  return cudaGetLastError();
+}
+cudaError_t launch_predict(const uint8_t* bins, uint32_t n_rows, uint32_t nfb,
+                           const uint8_t* has_missing, const TreeNodeOut* nodes,
+                           const uint32_t* tree_offsets, uint32_t n_trees, double base,
+                           double lr, double* out, uint32_t* error, cudaStream_t s) {
+  (void)nfb;
+  const int grid = int(std::min<uint64_t>((n_rows + 255) / 256, 152ull * 16));
+  predict_kernel<<<grid > 0 ? grid : 1, 256, 0, s>>>(bins, n_rows, has_missing, nodes,
+                                                      tree_offsets, n_trees, base, lr, out, error);
+  return cudaGetLastError();
+}
+
+}  // namespace mpsb

@@ -1,0 +1,109 @@
+// Launch interface of the sm_103a kernels (host and device code include this).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace mpsb {
+
+// Device pointers and sizes of one training session, passed by value to every kernel.
+struct TrainerDev {
+  // dataset
+  const uint8_t* bins;          // [nfb][n_rows][32] column-blocked u8 bins
+  const uint32_t* bin_count;    // [features]
+  const uint8_t* has_missing;   // [features]
+  uint32_t n_rows, features, nfb, n_trees;
+  // per-tree arrays
+  const double* labels;         // [n_rows]
+  const double* weights;        // [n_rows], [n_trees][n_rows] or null (unit weights)
+  uint32_t weights_per_tree;
+  uint32_t objective;
+  double* preds;                // [n_trees][n_rows]
+  float2* gh;                   // [n_trees][n_rows]
+  uint32_t* rows;               // [n_trees][2][n_rows]
+  TreeState* trees;             // [n_trees]
+  TreeParams params;
+  const int8_t* monotonic;      // [features] or null
+  const uint32_t* group_masks;  // [n_groups][path_words]
+  const uint32_t* tree_feature_masks;  // [n_trees][path_words] or null
+  // histogram slots: [n_slots][features][256] x {count, g, h} 64-bit words
+  unsigned long long* hist;
+  uint32_t* free_stack;         // [n_slots]
+  uint32_t n_slots;
+  // level buffers (index = level parity)
+  NodeRec* nodes[2];            // [max_level_nodes]
+  uint32_t* node_path[2];       // [max_level_nodes][path_words]
+  uint32_t* node_allowed[2];    // [max_level_nodes][path_words]
+  uint32_t max_level_nodes;
+  SplitRec* partial;            // [max_level_nodes][n_fchunks]
+  uint32_t n_fchunks;           // feature chunks of the split scan (32 features each)
+  BuildEntry* build;            // [max_level_nodes]
+  uint32_t* build_prefix;       // [max_level_nodes + 1] chunk prefix
+  SubEntry* sub;                // [max_level_nodes]
+  PartEntry* part;              // [max_level_nodes]
+  uint32_t* part_prefix;        // [max_level_nodes + 1] chunk prefix
+  uint32_t* part_counts;        // [max_part_chunks] left rows per chunk
+  uint32_t* part_offsets;       // [max_part_chunks] left rows before the chunk in its node
+  uint32_t* part_flags;         // [max_part_chunks][kPartChunk / 32]
+  uint32_t max_part_chunks;
+  LeafSeg* leafseg;             // [max_leafsegs]
+  uint32_t* leaf_prefix;        // [max_leafsegs + 1]
+  uint32_t max_leafsegs;
+  TreeNodeOut* tree_nodes;      // [n_trees][max_tree_nodes]
+  uint32_t max_tree_nodes;
+  Control* ctl;
+  uint32_t item_rows;           // rows per histogram work item (<= kItemRowsMax)
+  uint32_t mode;                // kModeFixed / kModeFloat
+  uint32_t ovr;                 // labels are class ids; tree t fits class t (logistic)
+  uint32_t scan_threads;        // block size of the split scan (multiple of 32)
+  // finalize scratch
+  uint32_t* scratch_flags;      // [max_level_nodes]
+  uint32_t* scratch_prefix;     // [max_level_nodes] valid-prefix, then accepted-prefix
+  uint32_t* scratch_aux;        // [max_level_nodes] free-slot prefix
+  uint32_t* tree_scratch;       // [n_trees][4]
+  // model output: per round, per tree, max_tree_nodes nodes + node counts
+  TreeNodeOut* model_nodes;     // [max_rounds][n_trees][max_tree_nodes]
+  uint32_t* model_counts;       // [max_rounds][n_trees]
+  uint32_t* round_counter;      // rounds completed (device)
+  uint32_t max_rounds;
+  // Histogram item range of one launch: [item_begin, item_end); item_end 0 = the whole
+  // level (ctl->hist_items). Per-node launches of the plain path set a node's range.
+  uint32_t item_begin, item_end;
+};
+
+struct HistConfig {
+  int threads = 512;
+  int stages = 3;
+};
+
+cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,
+                              cudaStream_t stream);
+cudaError_t launch_round_begin(const TrainerDev& a, cudaStream_t stream);
+cudaError_t launch_gradients(const TrainerDev& a, int grid, cudaStream_t stream);
+cudaError_t launch_round_setup(const TrainerDev& a, cudaStream_t stream);
+cudaError_t launch_zero_build_slots(const TrainerDev& a, int grid, cudaStream_t stream);
+cudaError_t launch_root_stats(const TrainerDev& a, cudaStream_t stream);
+cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t stream);
+cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStream_t stream);
+cudaError_t launch_finalize(const TrainerDev& a, int parity, uint32_t depth, cudaStream_t stream);
+cudaError_t launch_partition(const TrainerDev& a, int grid, cudaStream_t stream);
+cudaError_t launch_partition_count(const TrainerDev& a, int grid, cudaStream_t stream);
+cudaError_t launch_partition_finish(const TrainerDev& a, int grid, cudaStream_t stream);
+cudaError_t launch_apply_leaves(const TrainerDev& a, int grid, cudaStream_t stream);
+cudaError_t launch_round_end(const TrainerDev& a, cudaStream_t stream);
+cudaError_t launch_squared_error(const double* labels, const double* preds, uint64_t n,
+                                 double* out_pairs, uint32_t* error, cudaStream_t stream);
+cudaError_t launch_predict(const uint8_t* bins, uint32_t n_rows, uint32_t nfb,
+                           const uint8_t* has_missing, const TreeNodeOut* nodes,
+                           const uint32_t* tree_offsets, uint32_t n_trees, double base,
+                           double learning_rate, double* out, uint32_t* error,
+                           cudaStream_t stream);
+cudaError_t launch_pack_bins(const void* src, uint32_t width, const uint8_t* missing,
+                             const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
+                             uint32_t nfb, uint8_t* out, uint32_t* error, cudaStream_t stream);
+// Number of kernels each launch_* helper enqueues (launch accounting).
+constexpr int kPartitionKernels = 3;
+
+}  // namespace mpsb

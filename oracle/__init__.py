@@ -271,17 +271,17 @@ class Oracle:
             raise ValueError(kind)
         self.kind = kind
         self.lib = C.CDLL(path)
-        self.lib[self.prefix + "last_error"].restype = C.c_char_p
+        getattr(self.lib, self.prefix + "last_error").restype = C.c_char_p
         for name in ("tree_node_count", "model_tree_count", "model_tree_node_count"):
             self._fn(name).restype = C.c_uint32
         self._fn("model_base_score").restype = C.c_double
 
     def _fn(self, name: str):
-        return self.lib[self.prefix + name]
+        return getattr(self.lib, self.prefix + name)
 
     def _check(self, rc: int) -> None:
         if rc != 0:
-            msg = self.lib[self.prefix + "last_error"]().decode()
+            msg = getattr(self.lib, self.prefix + "last_error")().decode()
             raise OracleError(rc, msg)
 
     # -- datasets -------------------------------------------------------------------

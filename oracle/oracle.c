@@ -561,7 +561,7 @@ static int32_t exponent_above(double x) {
 
 /* Fixed-point scale rule of the CUDA path (mpsboost_gb300/csrc):
  *   kg = 61 - ceil(log2 n) - e(max|g|)  so that every sum over <= n rows stays < 2^61;
- *   kh = 31 - e(max h)                   so that one row's q_h < 2^31 and a work item of
+ *   kh = 30 - e(max h)                   so that one row's q_h <= 2^30 and a work item of
  *                                        <= 2^16 rows packs its h-sum into 47 bits.
  * A zero maximum gives exponent 0. */
 int orc_fixed_scales(const float* pairs32, uint64_t n, int32_t* kg, int32_t* kh) {
@@ -576,7 +576,7 @@ int orc_fixed_scales(const float* pairs32, uint64_t n, int32_t* kg, int32_t* kh)
   int32_t en = 0;
   while (en < 63 && ((uint64_t)1 << en) < n) ++en;
   *kg = mg > 0.0f ? 61 - en - exponent_above(mg) : 0;
-  *kh = mh > 0.0f ? 31 - exponent_above(mh) : 0;
+  *kh = mh > 0.0f ? 30 - exponent_above(mh) : 0;
   return ORC_OK;
 }
 

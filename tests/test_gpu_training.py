@@ -1,0 +1,201 @@
+"""The device-resident trainer against the oracle through the C ABI.
+
+* Fixed-point mode is bit-exact to the oracle's fixed-point replica: every tree node
+  (feature, threshold, missing direction, children, leaf value, gain) and every training
+  prediction, round after round.
+* Against the FP64 reference restatement: identical tree structures on these seeded
+  inputs, leaf values and predictions within 1e-5 relative (a floor of 1e-9 absolute for
+  values near zero), training RMSE within 1e-4.
+* The plain float path: same structures on well-separated data, predictions within 1e-4.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import mpsboost_gb300 as mb
+import oracle
+from conftest import seeded_matrix
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(seed, rows, feats, nan=0.0, ints=0, objective="squared_error"):
+    x = seeded_matrix(seed, rows, feats, nan, ints)
+    rng = np.random.default_rng(seed + 1)
+    xs = np.nan_to_num(x)
+    y = np.sin(xs[:, 0]) + xs[:, 1] * xs[:, 2 % feats] + 0.5 * xs[:, 3 % feats] ** 2 + rng.normal(size=rows) * 0.1
+    if objective == "binary_logistic":
+        y = (y > np.median(y)).astype(np.float64)
+    w = rng.uniform(0.5, 1.5, rows)
+    return x, y, w
+
+
+def _structure(trees):
+    return [[(int(n["feature_index"]), int(n["threshold_bin"]), int(n["default_left"]),
+              int(n["left_child"]), int(n["right_child"]), int(n["flags"])) for n in t] for t in trees]
+
+
+FIXED_CASES = {
+    "weighted": dict(seed=21, rows=5000, feats=8, nan=0.0, ints=2, max_bins=255,
+                     params=dict(n_estimators=4, learning_rate=0.1, max_depth=6, min_samples_leaf=3)),
+    "missing": dict(seed=22, rows=4000, feats=6, nan=0.1, ints=1, max_bins=128,
+                    params=dict(n_estimators=3, learning_rate=0.2, max_depth=5, min_samples_leaf=5,
+                                min_child_weight=0.5)),
+    "regularized": dict(seed=23, rows=3000, feats=5, nan=0.05, ints=0, max_bins=64,
+                        params=dict(n_estimators=3, learning_rate=0.3, max_depth=4, reg_lambda=2.0,
+                                    reg_alpha=0.3, max_delta_step=0.4, gamma=0.001)),
+    "monotone": dict(seed=24, rows=3000, feats=4, nan=0.0, ints=0, max_bins=64,
+                     params=dict(n_estimators=3, learning_rate=0.3, max_depth=4,
+                                 monotonic_constraints=[1, -1, 0, 1])),
+    "interaction": dict(seed=25, rows=3000, feats=5, nan=0.0, ints=0, max_bins=64,
+                        params=dict(n_estimators=3, learning_rate=0.3, max_depth=5,
+                                    interaction_constraints=[[0, 1, 2], [2, 3], [4]])),
+    "random_threshold": dict(seed=26, rows=2000, feats=4, nan=0.0, ints=0, max_bins=32,
+                             params=dict(n_estimators=3, learning_rate=0.5, max_depth=4,
+                                         split_strategy="random_threshold", random_seed=11)),
+    "max_leaves": dict(seed=27, rows=2000, feats=4, nan=0.0, ints=0, max_bins=32,
+                       params=dict(n_estimators=2, learning_rate=0.5, max_depth=6, max_leaves=7)),
+    "depth0": dict(seed=28, rows=500, feats=3, nan=0.0, ints=0, max_bins=16,
+                   params=dict(n_estimators=2, learning_rate=0.5, max_depth=0)),
+    "depth1": dict(seed=29, rows=500, feats=3, nan=0.2, ints=0, max_bins=16,
+                   params=dict(n_estimators=2, learning_rate=0.5, max_depth=1)),
+    "deep": dict(seed=30, rows=20000, feats=33, nan=0.02, ints=3, max_bins=255,
+                 params=dict(n_estimators=2, learning_rate=0.1, max_depth=10, min_samples_leaf=2)),
+    "quantile": dict(seed=31, rows=2000, feats=4, nan=0.0, ints=0, max_bins=64, objective="quantile",
+                     params=dict(n_estimators=3, learning_rate=0.3, max_depth=4, objective_alpha=0.7)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FIXED_CASES))
+def test_fixed_point_bit_exact_to_replica(backend, port, name):
+    c = FIXED_CASES[name]
+    objective = c.get("objective", "squared_error")
+    x, y, w = _data(c["seed"], c["rows"], c["feats"], c["nan"], c["ints"], objective)
+    params = dict(c["params"], objective=objective)
+    binned = mb.quantize_dense(x, c["max_bins"])
+    model = mb.train_regressor(backend, binned, y, w, **params)
+    ds = port.quantize_dense(x, c["max_bins"])
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FIXED, **params)
+    assert float(model.base_score).hex() == float(want.base_score).hex()
+    assert len(model.trees) == len(want.trees)
+    for got, exp in zip(model.trees, want.trees):
+        assert got.tobytes() == exp.tobytes()
+    assert model.train_predictions.tobytes() == want.predict(ds).tobytes()
+    assert model.predict(backend, binned).tobytes() == want.predict(ds).tobytes()
+
+
+@pytest.mark.parametrize("name", ["weighted", "missing", "regularized", "monotone", "interaction", "deep"])
+def test_against_fp64_reference(backend, port, name):
+    c = FIXED_CASES[name]
+    x, y, w = _data(c["seed"], c["rows"], c["feats"], c["nan"], c["ints"])
+    binned = mb.quantize_dense(x, c["max_bins"])
+    ds = port.quantize_dense(x, c["max_bins"])
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FP64, **c["params"])
+    model = mb.train_regressor(backend, binned, y, w, **c["params"])
+    assert _structure(model.trees) == _structure(want.trees)
+    for got, exp in zip(model.trees, want.trees):
+        np.testing.assert_allclose(got["leaf_value"], exp["leaf_value"], rtol=1e-5, atol=1e-9)
+    ref_pred = want.predict(ds)
+    np.testing.assert_allclose(model.train_predictions, ref_pred, rtol=1e-5, atol=1e-9)
+    rmse = lambda p: float(np.sqrt(np.mean((p - y) ** 2)))  # noqa: E731
+    assert abs(rmse(model.train_predictions) - rmse(ref_pred)) <= 1e-4
+
+
+def test_float_path_against_reference(backend, port):
+    c = FIXED_CASES["weighted"]
+    x, y, w = _data(c["seed"], c["rows"], c["feats"], c["nan"], c["ints"])
+    binned = mb.quantize_dense(x, c["max_bins"])
+    ds = port.quantize_dense(x, c["max_bins"])
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FP64, **c["params"])
+    model = mb.train_regressor(backend, binned, y, w, hist_mode="float", **c["params"])
+    assert _structure(model.trees) == _structure(want.trees)
+    np.testing.assert_allclose(model.train_predictions, want.predict(ds), rtol=1e-4, atol=1e-6)
+
+
+def test_paths_agree(backend):
+    """Batched graph, batched without graph and per-node launches give identical trees."""
+    x, y, w = _data(40, 30000, 20, 0.05, 2)
+    binned = mb.quantize_dense(x, 255)
+    params = dict(n_estimators=3, learning_rate=0.1, max_depth=7, min_samples_leaf=2)
+    a = mb.train_regressor(backend, binned, y, w, **params)
+    b = mb.train_regressor(backend, binned, y, w, graph=False, **params)
+    c = mb.train_regressor(backend, binned, y, w, batched=False, **params)
+    for t1, t2, t3 in zip(a.trees, b.trees, c.trees):
+        assert t1.tobytes() == t2.tobytes() == t3.tobytes()
+    assert a.train_predictions.tobytes() == c.train_predictions.tobytes()
+
+
+def test_logistic_against_replica(backend, port):
+    x, y, w = _data(41, 6000, 8, 0.1, 2, "binary_logistic")
+    params = dict(n_estimators=3, learning_rate=0.2, max_depth=5, min_samples_leaf=4,
+                  objective="binary_logistic")
+    binned = mb.quantize_dense(x, 255)
+    ds = port.quantize_dense(x, 255)
+    model = mb.train_regressor(backend, binned, y, w, **params)
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FIXED, **params)
+    assert _structure(model.trees) == _structure(want.trees)
+    for got, exp in zip(model.trees, want.trees):
+        np.testing.assert_allclose(got["leaf_value"], exp["leaf_value"], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(model.train_predictions, want.predict(ds), rtol=1e-9, atol=1e-12)
+
+
+def test_ovr_equals_independent_binary_fits(backend, port):
+    rng = np.random.default_rng(42)
+    x = rng.normal(size=(4000, 6)).astype(np.float32)
+    scores = x @ rng.normal(size=(6, 4)) + rng.gumbel(size=(4000, 4))
+    labels = scores.argmax(axis=1).astype(np.float64)
+    binned = mb.quantize_dense(x, 64)
+    params = dict(n_estimators=2, learning_rate=0.3, max_depth=4, min_samples_leaf=3)
+    models = mb.train_ovr(backend, binned, labels, 4, **params)
+    assert len(models) == 4
+    for k, m in enumerate(models):
+        single = mb.train_regressor(backend, binned, (labels == k).astype(np.float64),
+                                    objective="binary_logistic", **params)
+        assert m.base_score == single.base_score
+        for t1, t2 in zip(m.trees, single.trees):
+            assert t1.tobytes() == t2.tobytes()
+
+
+def test_training_errors(backend):
+    x, y, w = _data(43, 300, 3)
+    binned = mb.quantize_dense(x, 16)
+    bad = y.copy()
+    bad[5] = np.nan
+    with pytest.raises(mb.TrainingError):
+        mb.train_regressor(backend, binned, bad, n_estimators=1, max_depth=2)
+    with pytest.raises(mb.TrainingError, match="weights"):
+        mb.train_regressor(backend, binned, y, -w, n_estimators=1, max_depth=2)
+    with pytest.raises(mb.TrainingError, match="learning_rate"):
+        mb.train_regressor(backend, binned, y, learning_rate=0.0)
+    with pytest.raises(mb.UnsupportedError, match="level-wise"):
+        mb.train_regressor(backend, binned, y, growth_strategy="leaf_wise", n_estimators=1)
+    with pytest.raises(mb.TrainingError, match="binary"):
+        mb.train_regressor(backend, binned, y, objective="binary_logistic", n_estimators=1)
+
+
+def test_scale_properties(backend):
+    """Size-independent properties at 2M rows: count conservation, determinism of the
+    fixed-point path, session == one-shot training."""
+    n, f = 2_000_000, 32
+    rng = np.random.default_rng(44)
+    x = rng.normal(size=(n, f)).astype(np.float32)
+    y = np.sin(x[:, 0]) + x[:, 1] * x[:, 2] + rng.normal(size=n) * 0.1
+    binned = mb.quantize_dense(x, 255)
+    params = dict(n_estimators=2, learning_rate=0.1, max_depth=8, min_samples_leaf=20)
+    a = mb.train_regressor(backend, binned, y, **params)
+    b = mb.train_regressor(backend, binned, y, **params)
+    for t1, t2 in zip(a.trees, b.trees):
+        assert t1.tobytes() == t2.tobytes()
+    assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
+    hist = backend.histograms_from_pairs(binned, np.column_stack([y, np.ones(n)]), np.arange(n))
+    assert all(int(h["count"].sum()) == n for h in hist)
+    t = mb.Trainer(backend, binned, y, **params)
+    t.run(2)
+    t.synchronize()
+    m = t.export()
+    for t1, t2 in zip(a.trees, m.trees):
+        assert t1.tobytes() == t2.tobytes()
+    stats = t.stats()
+    assert stats["rounds"] == 2 and stats["kernel_launches"] > 0 and stats["hist_cells"] >= n * f

@@ -1,0 +1,89 @@
+"""The plain-C oracle against the reference's own compiled core on seeded inputs (CPU).
+
+Skipped where the reference sources are absent; ``test_golden.py`` carries the same pin
+through committed fixtures there.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import seeded_matrix
+
+CASES = [
+    dict(rows=2000, feats=6, nan=0.0, ints=2, max_bins=255, objective="squared_error",
+         params=dict(max_depth=6, min_samples_leaf=1)),
+    dict(rows=1500, feats=5, nan=0.1, ints=1, max_bins=64, objective="squared_error",
+         params=dict(max_depth=5, min_samples_leaf=5, reg_alpha=0.2, max_delta_step=0.5)),
+    dict(rows=1200, feats=4, nan=0.05, ints=0, max_bins=256, objective="binary_logistic",
+         params=dict(max_depth=4, min_samples_leaf=2, min_child_weight=0.1)),
+    dict(rows=800, feats=3, nan=0.0, ints=0, max_bins=16, objective="quantile",
+         params=dict(max_depth=3, objective_alpha=0.8)),
+    dict(rows=900, feats=3, nan=0.0, ints=0, max_bins=32, objective="poisson",
+         params=dict(max_depth=3)),
+    dict(rows=900, feats=3, nan=0.0, ints=0, max_bins=32, objective="tweedie",
+         params=dict(max_depth=3, tweedie_variance_power=1.3)),
+    dict(rows=1000, feats=4, nan=0.0, ints=0, max_bins=32, objective="squared_error",
+         params=dict(max_depth=4, monotonic_constraints=[1, -1, 0, 1])),
+    dict(rows=1000, feats=5, nan=0.0, ints=0, max_bins=32, objective="squared_error",
+         params=dict(max_depth=5, interaction_constraints=[[0, 1, 2], [2, 3], [4]])),
+    dict(rows=700, feats=3, nan=0.0, ints=0, max_bins=32, objective="squared_error",
+         params=dict(max_depth=4, split_strategy="random_threshold", random_seed=7)),
+    dict(rows=700, feats=3, nan=0.0, ints=0, max_bins=32, objective="squared_error",
+         params=dict(max_depth=6, max_leaves=9, gamma=0.001, min_gain_to_split=0.0001)),
+    dict(rows=300, feats=2, nan=0.3, ints=0, max_bins=300, objective="squared_error",
+         params=dict(max_depth=3)),
+]
+
+
+def _labels(x, objective, rng):
+    base = np.nan_to_num(x[:, 0]) + 0.5 * np.nan_to_num(x[:, 1]) ** 2 + rng.normal(size=len(x)) * 0.1
+    if objective == "binary_logistic":
+        return (base > np.median(base)).astype(float)
+    if objective in ("poisson", "tweedie"):
+        return np.floor(np.exp(np.clip(base, -3, 2)))
+    return base
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_port_matches_reference(port, reference, case):
+    c = CASES[case]
+    x = seeded_matrix(1000 + case, c["rows"], c["feats"], c["nan"], c["ints"])
+    rng = np.random.default_rng(2000 + case)
+    y = _labels(x, c["objective"], rng)
+    w = rng.uniform(0.5, 1.5, c["rows"])
+    dp, dr = port.quantize_dense(x, c["max_bins"]), reference.quantize_dense(x, c["max_bins"])
+    assert np.array_equal(dp.bins, dr.bins) and np.array_equal(dp.missing, dr.missing)
+    assert dp.boundaries_flat.tobytes() == dr.boundaries_flat.tobytes()
+    assert np.array_equal(dp.bin_counts, dr.bin_counts)
+    kw = dict(n_estimators=3, learning_rate=0.3, objective=c["objective"], **c["params"])
+    mp = port.train_regressor(dp, y, w, hist_mode=oracle.HIST_FP64, **kw)
+    mr = reference.train_regressor(dr, y, w, **kw)
+    assert float(mp.base_score).hex() == float(mr.base_score).hex()
+    assert len(mp.trees) == len(mr.trees)
+    for tp, tr in zip(mp.trees, mr.trees):
+        assert tp.tobytes() == tr.tobytes()
+    assert mp.predict(dp).tobytes() == mr.predict(dr).tobytes()
+
+
+def test_histograms_and_transform_match_reference(port, reference):
+    x = seeded_matrix(77, 3000, 7, 0.1, 3)
+    dp, dr = port.quantize_dense(x, 255), reference.quantize_dense(x, 255)
+    rng = np.random.default_rng(5)
+    pairs = np.column_stack([rng.normal(size=3000), rng.uniform(0, 2, 3000)])
+    rows = np.sort(rng.choice(3000, 1700, replace=False)).astype(np.uint64)
+    for a, b in zip(port.histograms(dp, pairs, rows), reference.histograms(dr, pairs, rows)):
+        assert a.tobytes() == b.tobytes()
+    x2 = seeded_matrix(78, 500, 7, 0.2)
+    tp, tr = port.transform_dense(dp, x2), reference.transform_dense(dr, x2)
+    assert np.array_equal(tp.bins, tr.bins) and np.array_equal(tp.missing, tr.missing)
+
+
+def test_gradients_match_reference(port, reference):
+    rng = np.random.default_rng(9)
+    y = rng.integers(0, 2, 500).astype(float)
+    p = rng.normal(size=500) * 3
+    for obj in ("squared_error", "binary_logistic", "quantile", "poisson", "tweedie"):
+        assert port.gradients(obj, y, p, 0.3, 1.4).tobytes() == reference.gradients(obj, y, p, 0.3, 1.4).tobytes()

@@ -186,7 +186,7 @@ def run_ours(args, rank, world):
     from mpsboost_gb300 import _lib
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    xf, y, w = make_data(ROWS)
+    xf, y, w = make_data(args.rows)
     t0 = time.perf_counter()
     binned = mb.quantize_dense(xf.T, BINS)
     t_bin = time.perf_counter() - t0
@@ -215,6 +215,13 @@ def run_ours(args, rank, world):
     st = trainer.stats()
     ms_max = reduce_max(ms, world)
     value = world * args.steps / (ms_max / 1e3)
+    if args.only_train:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "trees/s", "rows": args.rows,
+                              "steps": args.steps, "warmup": args.warmup,
+                              "gpu_launches": int(st["kernel_launches"]), "only_train": True}), flush=True)
+        trainer.close()
+        return
 
     # Roofline pass: the same rounds with CUDA events around every histogram launch.
     timed = mb.Trainer(backend, binned, y, w, n_estimators=n_rounds, options=_lib.OPT_TIMING, **PARAMS)
@@ -325,6 +332,10 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=500_000)
     ap.add_argument("--ref-rows", type=int, default=500_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rows", type=int, default=ROWS,
+                    help="rows of the synthetic workload (profiling runs use fewer)")
+    ap.add_argument("--only-train", action="store_true",
+                    help="time the training rounds only (for launch lists and ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -134,7 +134,7 @@ class BinnedDataset:
     def transform(self, matrix, n_threads: int = 0) -> "BinnedDataset":
         """Bin new data with this schema (TransformDense, binned_dataset.cpp:190-238)."""
 
-        x, st = _as_matrix(matrix)
+        x, st, rs, cs = _as_matrix(matrix)
         if x.shape[1] != self.features:
             raise _lib.DataError("Prediction input feature count does not match the binned schema")
         rows, feats = x.shape
@@ -145,7 +145,7 @@ class BinnedDataset:
         bnd = np.ascontiguousarray(self.boundaries_flat, np.float32)
         check(
             lib.mpsb_transform_dense(
-                ptr(x), st, rows, feats, x.strides[0], x.strides[1], self.max_bins, ptr(bnd),
+                ptr(x), st, rows, feats, rs, cs, self.max_bins, ptr(bnd),
                 ptr(self.boundary_offsets), ptr(self.boundary_counts), n_threads, ptr(bins), ptr(missing),
             )
         )
@@ -156,7 +156,12 @@ class BinnedDataset:
         )
 
 
-def _as_matrix(matrix) -> tuple[np.ndarray, int]:
+def _as_matrix(matrix) -> tuple[np.ndarray, int, int, int]:
+    """``(array, scalar type, row stride, column stride)`` of a 2-D float view.
+
+    Size-1 axes get their natural stride (numpy may report 0 for them); broadcast or
+    reversed views are read from a dense copy."""
+
     x = np.asarray(matrix)
     if x.dtype not in (np.float32, np.float64):
         x = x.astype(np.float32)
@@ -164,15 +169,23 @@ def _as_matrix(matrix) -> tuple[np.ndarray, int]:
         raise _lib.DataError("Input matrix must be two-dimensional")
     if x.shape[0] == 0 or x.shape[1] == 0:
         raise _lib.DataError("Input matrix must contain at least one row and one feature")
-    if min(x.strides) < x.itemsize:  # broadcast or reversed views: read a dense copy
-        x = np.ascontiguousarray(x)
-    return x, 1 if x.dtype == np.float32 else 2
+
+    def strides(a):
+        rs = a.strides[0] if a.shape[0] > 1 else a.itemsize * a.shape[1]
+        cs = a.strides[1] if a.shape[1] > 1 else a.itemsize
+        return rs, cs
+
+    rs, cs = strides(x)
+    if rs < x.itemsize or cs < x.itemsize:
+        x = np.array(x, order="C")
+        rs, cs = strides(x)
+    return x, 1 if x.dtype == np.float32 else 2, rs, cs
 
 
 def quantize_dense(matrix, max_bins: int = 256, n_threads: int = 0) -> BinnedDataset:
     """Quantile-bin a float32/float64 matrix (QuantizeDense, binned_dataset.cpp:126-188)."""
 
-    x, st = _as_matrix(matrix)
+    x, st, rs, cs = _as_matrix(matrix)
     rows, feats = x.shape
     if not 2 <= max_bins <= 65536:
         raise _lib.DataError("max_bins must be in [2, 65536]")
@@ -187,7 +200,7 @@ def quantize_dense(matrix, max_bins: int = 256, n_threads: int = 0) -> BinnedDat
     lib = _lib.load()
     check(
         lib.mpsb_quantize_dense(
-            ptr(x), st, rows, feats, x.strides[0], x.strides[1], max_bins, n_threads, ptr(bins),
+            ptr(x), st, rows, feats, rs, cs, max_bins, n_threads, ptr(bins),
             ptr(missing), ptr(bnd), ptr(off), ptr(cnt), ptr(binc), ptr(miss),
         )
     )

@@ -14,8 +14,7 @@ namespace mpsb {
 constexpr int kSlots = 256;          // histogram slots per feature
 constexpr int kMissingSlot = 255;    // bin value of a missing row (features with missing)
 constexpr int kBlockFeatures = 32;   // features per column block of the bin matrix
-constexpr uint32_t kItemRowsMax = 65536;  // rows of one histogram work item (packing bound)
-constexpr int kCountShift = 47;      // fixed mode: count lives above bit 47 of the h word
+constexpr uint32_t kItemRowsMax = 65536;  // rows of one histogram work item (limb bound)
 constexpr uint32_t kPartChunk = 4096;     // rows per partition chunk
 constexpr uint32_t kApplyChunk = 4096;    // rows per leaf-application chunk
 

@@ -7,16 +7,19 @@
 //  * Persistent CTAs (one per SM) pull work items (build node, row chunk <= 65536 rows,
 //    feature block) from a device counter; every frontier node of every tree of a level
 //    is in the same launch.
-//  * A 3-stage cp.async pipeline stages the row ids' bin sectors and FP32 g/h pairs;
-//    row ids are prefetched one tile ahead in registers.
-//  * The CTA-private histogram lives in shared memory laid out [bin][feature]: in one
-//    atomic instruction the 16 lanes of a half-warp update 16 different features of 16
-//    different rows (feature index rotated by the row), so their words fall in 16
-//    different bank pairs for any bin values: conflict-free shared atomics.
-//  * Fixed mode: q_g = rne(g * 2^kg) accumulated as int64; q_h + 2^47 accumulated as one
-//    int64 word, so count (bits 47..63) and the h-sum (bits 0..46, < 2^46 for <= 2^16
-//    rows) need one atomic: two 64-bit shared atomics per cell. Exact and
-//    order-independent. Float mode: u32 count + two FP32 atomics per cell.
+//  * A multi-stage cp.async pipeline stages each gathered row's 32-byte bin sector; the
+//    staging thread also writes the row's quantized g/h (computed once per row) next to
+//    it. Row ids are prefetched two tiles ahead and g/h one tile ahead in registers.
+//  * The CTA-private histogram lives in shared memory laid out [bin][feature] and lane l
+//    of every warp owns feature l: per row a warp does one byte load, one broadcast load
+//    of the row's values and one red.shared per accumulator; the 32 lanes hit 32
+//    different features, so their words fall in different banks for any bin values.
+//  * Only 32-bit integer shared reductions are native on sm_103 (64-bit and FP32 ones run
+//    several times slower), so fixed mode splits each quantized value q (|q| <= 2^30) into
+//    a 16-bit unsigned low limb and a signed high limb and accumulates count, g_lo, g_hi,
+//    h_lo, h_hi as five u32 red.shared per cell. Over <= 2^16 rows no limb sum leaves 32
+//    bits, so the int64 sum hi * 2^16 + lo is exact and order-independent. Float mode
+//    (the plain path): a u32 count and two FP32 reductions per cell.
 //  * The CTA flushes its non-empty cells into the node's global slot with 64-bit
 //    red.global adds (exact integer adds in fixed mode; FP64 adds in float mode).
 #include "device.cuh"
@@ -29,63 +32,59 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
 }
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
-}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
 
-// Rotate a 16-byte vector right by s bytes (s in [0, 16)): byte j of the result is byte
-// (j + s) mod 16 of the input.
-__device__ __forceinline__ uint4 rotate_bytes(uint4 v, uint32_t s) {
-  const uint32_t ws = s >> 2, bs = (s & 3u) * 8u;
-  uint32_t x0 = v.x, x1 = v.y, x2 = v.z, x3 = v.w;
-  if (ws & 1u) { const uint32_t t = x0; x0 = x1; x1 = x2; x2 = x3; x3 = t; }
-  if (ws & 2u) { uint32_t t = x0; x0 = x2; x2 = t; t = x1; x1 = x3; x3 = t; }
-  uint4 r;
-  r.x = __funnelshift_r(x0, x1, bs);
-  r.y = __funnelshift_r(x1, x2, bs);
-  r.z = __funnelshift_r(x2, x3, bs);
-  r.w = __funnelshift_r(x3, x0, bs);
-  return r;
+template <uint32_t OFF = 0>
+__device__ __forceinline__ void red_shared_u32(uint32_t addr, uint32_t v) {
+  asm volatile("red.shared.add.u32 [%0+%2], %1;\n" ::"r"(addr), "r"(v), "n"(OFF));
+}
+template <uint32_t OFF = 0>
+__device__ __forceinline__ void red_shared_f32(uint32_t addr, float v) {
+  asm volatile("red.shared.add.f32 [%0+%2], %1;\n" ::"r"(addr), "f"(v), "n"(OFF));
 }
 
 template <int MODE>
 struct HistSmem;
 
 template <>
-struct HistSmem<kModeFixed> {
-  static constexpr size_t kBytes = 2ull * kSlots * kBlockFeatures * sizeof(long long);
+struct HistSmem<kModeFixed> {  // count, g_lo, g_hi, h_lo, h_hi: five u32 words per cell
+  static constexpr size_t kBytes = 5ull * kSlots * kBlockFeatures * sizeof(uint32_t);
 };
 template <>
 struct HistSmem<kModeFloat> {
   static constexpr size_t kBytes = 3ull * kSlots * kBlockFeatures * sizeof(uint32_t);
 };
 
+// Per staged row: 32 bin bytes (cp.async) and 8 bytes of per-row values written by the
+// staging thread: fixed mode the limbs {g_lo | h_lo << 16, g_hi | h_hi << 16} (16-bit
+// each), float mode {g, h}.
+constexpr int kRowBytes = 32 + 8;
+
 template <int MODE, int THREADS, int NSTAGE>
 __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
   constexpr int TILE = THREADS;
   constexpr int WARPS = THREADS / 32;
-  constexpr int ROWS_PER_STEP = WARPS * 16;
+  constexpr int RPW = TILE / WARPS;  // rows per warp per tile (32)
   constexpr int CELLS = kSlots * kBlockFeatures;
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* hist_smem = smem;
-  uint4* stage_bins = reinterpret_cast<uint4*>(smem + HistSmem<MODE>::kBytes);  // [NSTAGE][TILE][2]
-  float2* stage_gh = reinterpret_cast<float2*>(stage_bins + NSTAGE * TILE * 2);  // [NSTAGE][TILE]
+  uint8_t* stage_bins = smem + HistSmem<MODE>::kBytes;               // [NSTAGE][TILE][32]
+  uint2* stage_val = reinterpret_cast<uint2*>(stage_bins + size_t(NSTAGE) * TILE * 32);  // [NSTAGE][TILE]
 
   __shared__ uint32_t s_item, s_entry;
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int warp = tid >> 5;
-  const uint32_t half = lane >> 4;
-  const uint32_t r16 = lane & 15;
   const uint32_t n = a.n_rows;
   const uint32_t nfb = a.nfb;
+  const uint32_t hist_base = static_cast<uint32_t>(__cvta_generic_to_shared(hist_smem));
+  // lane = feature of the block: its cell (bin b) lives at word b * 32 + lane
+  const uint32_t lane_base = hist_base + uint32_t(lane) * 4u;
 
   for (;;) {
     const uint32_t limit = a.item_end ? a.item_end : a.ctl->hist_items;
@@ -125,19 +124,42 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
     __syncthreads();
 
     const int ntiles = int((row_count + TILE - 1) / TILE);
-    uint32_t r_next = (uint32_t(tid) < row_count) ? __ldg(rows + tid) : 0u;
+    // Register pipeline: row ids two tiles ahead, g/h one tile ahead.
+    auto row_at = [&](uint32_t pos) -> uint32_t {
+      if (pos >= row_count) return 0u;
+      const uint32_t r = __ldg(rows + pos);
+      return r < n ? r : 0u;  // row ids are < n by construction
+    };
+    uint32_t r_cur = row_at(uint32_t(tid));
+    uint32_t r_nxt = row_at(uint32_t(TILE + tid));
+    float2 g_cur = (uint32_t(tid) < row_count) ? __ldg(gh + r_cur) : make_float2(0.f, 0.f);
     for (int t = 0; t < ntiles + NSTAGE - 1; ++t) {
       if (t < ntiles) {
         const int s = t % NSTAGE;
         const uint32_t pos = uint32_t(t) * TILE + tid;
-        const uint32_t r = r_next < n ? r_next : 0u;  // row ids are < n by construction
-        const uint32_t pos_next = pos + TILE;
-        r_next = (pos_next < row_count) ? __ldg(rows + pos_next) : 0u;
+        const uint32_t r = r_cur;
+        const float2 p = g_cur;
+        const uint32_t r_far = row_at(pos + 2u * TILE);
+        g_cur = (pos + TILE < row_count) ? __ldg(gh + r_nxt) : make_float2(0.f, 0.f);
+        r_cur = r_nxt;
+        r_nxt = r_far;
         if (pos < row_count) {
           const uint8_t* src = bins + size_t(r) * kBlockFeatures;
-          cp_async16(&stage_bins[(s * TILE + tid) * 2 + 0], src);
-          cp_async16(&stage_bins[(s * TILE + tid) * 2 + 1], src + 16);
-          cp_async8(&stage_gh[s * TILE + tid], gh + r);
+          cp_async16(stage_bins + (size_t(s) * TILE + tid) * 32, src);
+          cp_async16(stage_bins + (size_t(s) * TILE + tid) * 32 + 16, src + 16);
+          uint2 v;
+          if constexpr (MODE == kModeFixed) {
+            // |q| <= 2^30: low limb = q & 0xFFFF (unsigned), high limb = q >> 16 (signed,
+            // |hi| <= 2^14 fits in 16 bits).
+            const long long qg = quantize_f32(p.x, kg);
+            const long long qh = quantize_f32(p.y, kh);
+            const uint32_t glo = uint32_t(qg) & 0xFFFFu, ghi = uint32_t(qg >> 16) & 0xFFFFu;
+            const uint32_t hlo = uint32_t(qh) & 0xFFFFu, hhi = uint32_t(qh >> 16) & 0xFFFFu;
+            v = make_uint2(glo | (hlo << 16), ghi | (hhi << 16));
+          } else {
+            v = make_uint2(__float_as_uint(p.x), __float_as_uint(p.y));
+          }
+          stage_val[s * TILE + tid] = v;
         }
       }
       cp_async_commit();
@@ -147,43 +169,37 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
         const int ct = t - (NSTAGE - 1);
         const int s = ct % NSTAGE;
         const int tile_rows = min(TILE, int(row_count) - ct * TILE);
-#pragma unroll 1
-        for (int step = 0; step < TILE / ROWS_PER_STEP; ++step) {
-          const int rl = step * ROWS_PER_STEP + warp * 16 + int(r16);
-          if (rl < tile_rows) {
-            const uint4 v = rotate_bytes(stage_bins[(s * TILE + rl) * 2 + half], r16);
-            const float2 p = stage_gh[s * TILE + rl];
-            const uint32_t words[4] = {v.x, v.y, v.z, v.w};
-            if constexpr (MODE == kModeFixed) {
-              unsigned long long* hg = reinterpret_cast<unsigned long long*>(hist_smem);
-              unsigned long long* hhc = hg + CELLS;
-              const unsigned long long qg = (unsigned long long)quantize_f32(p.x, kg);
-              const unsigned long long qhc =
-                  (unsigned long long)quantize_f32(p.y, kh) + (1ull << kCountShift);
-#pragma unroll
-              for (int j = 0; j < 16; ++j) {
-                const uint32_t b = (words[j >> 2] >> ((j & 3) * 8)) & 0xFFu;
-                const uint32_t f = half * 16u + ((r16 + uint32_t(j)) & 15u);
-                const uint32_t idx = b * kBlockFeatures + f;
-                atomicAdd(&hg[idx], qg);
-                atomicAdd(&hhc[idx], qhc);
-              }
-            } else {
-              uint32_t* hc = reinterpret_cast<uint32_t*>(hist_smem);
-              float* hgf = reinterpret_cast<float*>(hc + CELLS);
-              float* hhf = hgf + CELLS;
-#pragma unroll
-              for (int j = 0; j < 16; ++j) {
-                const uint32_t b = (words[j >> 2] >> ((j & 3) * 8)) & 0xFFu;
-                const uint32_t f = half * 16u + ((r16 + uint32_t(j)) & 15u);
-                const uint32_t idx = b * kBlockFeatures + f;
-                atomicAdd(&hc[idx], 1u);
-                atomicAdd(&hgf[idx], p.x);
-                atomicAdd(&hhf[idx], p.y);
-              }
-            }
+        const uint8_t* sb = stage_bins + size_t(s) * TILE * 32;
+        const uint2* sv = stage_val + s * TILE;
+        const int row0 = warp * RPW;
+        const int nrows = max(0, min(RPW, tile_rows - row0));
+        auto accumulate = [&](uint32_t b, uint2 q) {
+          const uint32_t addr = lane_base + b * (kBlockFeatures * 4u);
+          if constexpr (MODE == kModeFixed) {
+            red_shared_u32<0>(addr, 1u);
+            red_shared_u32<1u * CELLS * 4u>(addr, q.x & 0xFFFFu);
+            red_shared_u32<2u * CELLS * 4u>(addr, uint32_t(int32_t(int16_t(q.y & 0xFFFFu))));
+            red_shared_u32<3u * CELLS * 4u>(addr, q.x >> 16);
+            red_shared_u32<4u * CELLS * 4u>(addr, q.y >> 16);
+          } else {
+            red_shared_u32<0>(addr, 1u);
+            red_shared_f32<CELLS * 4u>(addr, __uint_as_float(q.x));
+            red_shared_f32<2u * CELLS * 4u>(addr, __uint_as_float(q.y));
           }
+        };
+        int j = 0;
+        for (; j + 4 <= nrows; j += 4) {
+          uint32_t b[4];
+          uint2 q[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            b[u] = sb[(row0 + j + u) * 32 + lane];
+            q[u] = sv[row0 + j + u];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) accumulate(b[u], q[u]);
         }
+        for (; j < nrows; ++j) accumulate(sb[(row0 + j) * 32 + lane], sv[row0 + j]);
         __syncthreads();
       }
     }
@@ -196,13 +212,14 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
       if (fb * kBlockFeatures + f >= a.features) continue;
       unsigned long long* dst = dst_base + (size_t(f) * kSlots + b) * 3;
       if constexpr (MODE == kModeFixed) {
-        const unsigned long long* hg = reinterpret_cast<const unsigned long long*>(hist_smem);
-        const unsigned long long hcw = hg[CELLS + idx];
-        const unsigned long long cnt = hcw >> kCountShift;
+        const uint32_t* w = reinterpret_cast<const uint32_t*>(hist_smem);
+        const uint32_t cnt = w[idx];
         if (cnt == 0) continue;
-        atomicAdd(dst + 0, cnt);
-        atomicAdd(dst + 1, hg[idx]);
-        atomicAdd(dst + 2, hcw & ((1ull << kCountShift) - 1ull));
+        const long long g = (long long)int32_t(w[2 * CELLS + idx]) * 65536 + (long long)w[CELLS + idx];
+        const long long hh = (long long)w[4 * CELLS + idx] * 65536 + (long long)w[3 * CELLS + idx];
+        atomicAdd(dst + 0, (unsigned long long)cnt);
+        atomicAdd(dst + 1, (unsigned long long)g);
+        atomicAdd(dst + 2, (unsigned long long)hh);
       } else {
         const uint32_t* hc = reinterpret_cast<const uint32_t*>(hist_smem);
         const float* hgf = reinterpret_cast<const float*>(hc + CELLS);
@@ -224,7 +241,7 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
 
 template <int MODE, int THREADS, int NSTAGE>
 size_t hist_smem_bytes() {
-  return HistSmem<MODE>::kBytes + size_t(NSTAGE) * THREADS * (32 + 8);
+  return HistSmem<MODE>::kBytes + size_t(NSTAGE) * THREADS * kRowBytes;
 }
 
 template <int MODE, int THREADS, int NSTAGE>
@@ -246,14 +263,15 @@ cudaError_t launch_variant(const TrainerDev& a, int grid, cudaStream_t stream) {
 
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,
                               cudaStream_t stream) {
+  // Shared memory: 160 KB (fixed) / 96 KB (float) histogram + stages x threads x 40 B.
   if (a.mode == kModeFixed) {
-    if (cfg.threads == 1024) return launch_variant<kModeFixed, 1024, 2>(a, grid, stream);
-    if (cfg.stages == 4) return launch_variant<kModeFixed, 512, 4>(a, grid, stream);
+    if (cfg.threads == 768) return launch_variant<kModeFixed, 768, 2>(a, grid, stream);
+    if (cfg.threads == 640) return launch_variant<kModeFixed, 640, 2>(a, grid, stream);
     if (cfg.stages == 2) return launch_variant<kModeFixed, 512, 2>(a, grid, stream);
     return launch_variant<kModeFixed, 512, 3>(a, grid, stream);
   }
   if (cfg.threads == 1024) return launch_variant<kModeFloat, 1024, 2>(a, grid, stream);
-  if (cfg.stages == 4) return launch_variant<kModeFloat, 512, 4>(a, grid, stream);
+  if (cfg.threads == 768) return launch_variant<kModeFloat, 768, 2>(a, grid, stream);
   if (cfg.stages == 2) return launch_variant<kModeFloat, 512, 2>(a, grid, stream);
   return launch_variant<kModeFloat, 512, 3>(a, grid, stream);
 }

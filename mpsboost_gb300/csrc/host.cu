@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -173,11 +174,10 @@ void fixed_scales(const float* pairs32, uint64_t n, uint64_t n_rows, int32_t* kg
     mg = std::max(mg, std::fabs(pairs32[2 * i]));
     mh = std::max(mh, std::max(pairs32[2 * i + 1], 0.0f));
   }
-  int en = 0;
-  while (en < 63 && (uint64_t(1) << en) < n_rows) ++en;
+  (void)n_rows;
   int e;
   std::frexp(mg, &e);
-  *kg = mg > 0.0f ? 61 - en - e : 0;
+  *kg = mg > 0.0f ? 30 - e : 0;
   std::frexp(mh, &e);
   *kh = mh > 0.0f ? 30 - e : 0;
 }
@@ -444,7 +444,8 @@ struct mpsb_cuda_trainer {
     if (rounds_enqueued + rounds > dev.max_rounds)
       throw TrainingError("training session round capacity exceeded");
     const bool timing = options & MPSB_OPT_TIMING;
-    const bool use_graph = !(options & (MPSB_OPT_NO_GRAPH | MPSB_OPT_PER_NODE));
+    // Events captured into a graph cannot be timed, so timing runs launch directly.
+    const bool use_graph = !(options & (MPSB_OPT_NO_GRAPH | MPSB_OPT_PER_NODE | MPSB_OPT_TIMING));
     for (uint32_t r = 0; r < rounds; ++r) {
       if (use_graph) {
         if (!graph_exec) {
@@ -544,6 +545,12 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     per = (per + 511) / 512 * 512;
     a.item_rows = uint32_t(std::min<uint64_t>(per, kItemRowsMax));
   }
+  // Tile-shape overrides (used by the tuning sweeps): threads per CTA, pipeline stages,
+  // rows per work item.
+  if (const char* v = std::getenv("MPSB_HIST_THREADS")) t->hcfg.threads = std::atoi(v);
+  if (const char* v = std::getenv("MPSB_HIST_STAGES")) t->hcfg.stages = std::atoi(v);
+  if (const char* v = std::getenv("MPSB_ITEM_ROWS"))
+    a.item_rows = uint32_t(std::min<long>(std::max<long>(std::atol(v), 512), long(kItemRowsMax)));
   TreeParams& tp = a.params;
   tp.min_samples_leaf = p->min_samples_leaf;
   tp.min_child_weight = p->min_child_weight;

@@ -199,15 +199,14 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
 }
 
 __global__ void round_setup_kernel(TrainerDev a) {
-  int en = 0;
-  while (en < 63 && (1ull << en) < uint64_t(a.n_rows)) ++en;
   const uint32_t chunks_per_tree = ceil_div(a.n_rows, a.item_rows);
   for (uint32_t base = 0; base < a.n_trees; base += blockDim.x) {
     const uint32_t t = base + threadIdx.x;
     if (t < a.n_trees) {
       TreeState& s = a.trees[t];
       const float mg = __uint_as_float(s.max_abs_g_bits), mh = __uint_as_float(s.max_h_bits);
-      s.kg = mg > 0.0f ? 61 - en - exponent_above(mg) : 0;
+      // every row's |q| <= 2^30: the histogram's 32-bit limb sums cannot overflow
+      s.kg = mg > 0.0f ? 30 - exponent_above(mg) : 0;
       s.kh = mh > 0.0f ? 30 - exponent_above(mh) : 0;
       s.inv_g = ldexp(1.0, -s.kg);
       s.inv_h = ldexp(1.0, -s.kh);

@@ -74,8 +74,8 @@ struct TrainerDev {
 };
 
 struct HistConfig {
-  int threads = 512;
-  int stages = 3;
+  int threads = 768;
+  int stages = 2;
 };
 
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,

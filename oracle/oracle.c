@@ -560,10 +560,11 @@ static int32_t exponent_above(double x) {
 }
 
 /* Fixed-point scale rule of the CUDA path (mpsboost_gb300/csrc):
- *   kg = 61 - ceil(log2 n) - e(max|g|)  so that every sum over <= n rows stays < 2^61;
- *   kh = 30 - e(max h)                   so that one row's q_h <= 2^30 and a work item of
- *                                        <= 2^16 rows packs its h-sum into 47 bits.
- * A zero maximum gives exponent 0. */
+ *   kg = 30 - e(max|g|),  kh = 30 - e(max h)   so every row's |q| <= 2^30.
+ * The device accumulates each 64-bit sum as two 32-bit limbs (low 16 bits unsigned, the
+ * rest signed) over work items of <= 2^16 rows; the per-row bound keeps every limb sum
+ * inside 32 bits, and every node sum over < 2^31 rows inside int64. A zero maximum gives
+ * exponent 0. */
 int orc_fixed_scales(const float* pairs32, uint64_t n, int32_t* kg, int32_t* kh) {
   float mg = 0.0f, mh = 0.0f;
   for (uint64_t i = 0; i < n; ++i) {
@@ -573,9 +574,7 @@ int orc_fixed_scales(const float* pairs32, uint64_t n, int32_t* kg, int32_t* kh)
     if (g > mg) mg = g;
     if (h > mh) mh = h;
   }
-  int32_t en = 0;
-  while (en < 63 && ((uint64_t)1 << en) < n) ++en;
-  *kg = mg > 0.0f ? 61 - en - exponent_above(mg) : 0;
+  *kg = mg > 0.0f ? 30 - exponent_above(mg) : 0;
   *kh = mh > 0.0f ? 30 - exponent_above(mh) : 0;
   return ORC_OK;
 }

@@ -237,6 +237,28 @@ int mpsb_cuda_partition_rows(mpsb_cuda_backend* backend, const mpsb_cuda_dataset
                              uint32_t threshold_bin, int default_left, uint64_t* left_out,
                              uint64_t* right_out, uint64_t* n_left);
 
+/* Histogram build that allocates no device memory (no counterpart in the reference).
+   For callers that must not call cudaMalloc -- a plugin inside a process whose device
+   memory belongs to that process's own pool allocator, or a serving loop that cannot
+   afford cudaMalloc's implicit synchronisation. All inputs and the output are the
+   caller's device buffers:
+     bins   column-blocked u8 [ceil(features/32)][dataset_rows][32] (feature f of row r at
+            ((f/32)*dataset_rows + r)*32 + f%32; padding features 0; a missing value may
+            use bin 255 and then lands in slot 255),
+     rows   u32 [n_rows] row ids of the node (< dataset_rows),
+     pairs  FP32 [dataset_rows][2] gradient/hessian pairs (hessian >= 0),
+     out    [features][256] bins: exact fixed-point count/G/H as FP64 (same scale rule and
+            kernel as mpsb_cuda_build_histograms).
+   Work is enqueued on `stream` (a cudaStream_t; NULL = default stream) and not waited for.
+   Intermediates live in a fixed 2 MiB array inside the library that every GPU keeps
+   until the process exits; features above 256 are rejected. The first call on a device
+   looks the array up (make it before any stream capture); every call shares the array,
+   so calls that overlap on the GPU race. */
+int mpsb_cuda_build_histogram_noalloc(const uint8_t* bins, uint32_t dataset_rows,
+                                      uint32_t features, const uint32_t* rows,
+                                      uint32_t n_rows, const float* pairs,
+                                      mpsb_histogram_bin* out, void* stream);
+
 /* ---- training ------------------------------------------------------------------ */
 /* weights may be NULL (unit weights). options: MPSB_OPT_* bits. */
 int mpsb_cuda_train_regressor(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,

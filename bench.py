@@ -231,6 +231,9 @@ def run_ours(args, rank, world):
     timed.run(args.steps)
     timed.synchronize()
     ts = timed.stats()
+    levels = [{"depth": d, "ms_per_launch": ms / args.steps, "cells_per_launch": cells // args.steps,
+               "cells_per_s": cells / (ms / 1e3) if ms else None}
+              for d, (ms, cells) in enumerate(timed.level_stats(DEPTH))]
     timed.close()
     per_launch_ms = ts["hist_ms"] / max(ts["hist_timed_launches"], 1)
     alg_bytes = ts["hist_cells"] + 12 * ts["hist_rows"]  # bins + row id + g/h per built row
@@ -271,7 +274,7 @@ def run_ours(args, rank, world):
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                      "kernel": "hist_build_kernel<fixed>",
                      "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
-                     "cells_per_s": ts["hist_cells"] / (ts["hist_ms"] / 1e3)},
+                     "cells_per_s": ts["hist_cells"] / (ts["hist_ms"] / 1e3), "levels": levels},
         "plain_fp32_per_node": {"value": plain_steps / (plain_ms / 1e3), "unit": "trees/s",
                                 "speedup_of_fixed_batched": value / world / (plain_steps / (plain_ms / 1e3))},
         "cpu_baseline": cpu,

@@ -299,6 +299,10 @@ int mpsb_cuda_trainer_run(mpsb_cuda_trainer* trainer, uint32_t rounds);
 int mpsb_cuda_trainer_synchronize(mpsb_cuda_trainer* trainer);
 int mpsb_cuda_trainer_stats(const mpsb_cuda_trainer* trainer, mpsb_cuda_stats* out);
 int mpsb_cuda_trainer_reset_stats(mpsb_cuda_trainer* trainer);
+/* Per depth level (MPSB_OPT_TIMING): summed histogram-build milliseconds and cells since
+   the last reset; n_levels entries are written (levels beyond the tree depth get 0). */
+int mpsb_cuda_trainer_level_stats(const mpsb_cuda_trainer* trainer, uint32_t n_levels,
+                                  double* milliseconds, uint64_t* cells);
 int mpsb_cuda_trainer_export(mpsb_cuda_trainer* trainer, mpsb_cuda_model** out);
 void mpsb_cuda_trainer_destroy(mpsb_cuda_trainer* trainer);
 

@@ -155,6 +155,7 @@ SIGNATURES = {
     "mpsb_cuda_trainer_synchronize": (_I32, [_VP]),
     "mpsb_cuda_trainer_stats": (_I32, [_VP, C.POINTER(Stats)]),
     "mpsb_cuda_trainer_reset_stats": (_I32, [_VP]),
+    "mpsb_cuda_trainer_level_stats": (_I32, [_VP, _U32, _VP, _VP]),
     "mpsb_cuda_trainer_export": (_I32, [_VP, C.POINTER(_VP)]),
     "mpsb_cuda_trainer_destroy": (None, [_VP]),
 }

@@ -526,6 +526,13 @@ class Trainer:
     def reset_stats(self) -> None:
         check(_lib.load().mpsb_cuda_trainer_reset_stats(self.handle))
 
+    def level_stats(self, n_levels: int = 32) -> list[tuple[float, int]]:
+        """Per depth level: (histogram-build ms, cells) since the last reset (timing mode)."""
+        ms = np.zeros(n_levels, np.float64)
+        cells = np.zeros(n_levels, np.uint64)
+        check(_lib.load().mpsb_cuda_trainer_level_stats(self.handle, n_levels, ptr(ms), ptr(cells)))
+        return [(float(a), int(c)) for a, c in zip(ms, cells) if c or a]
+
     def export(self) -> RegressionModel:
         lib = _lib.load()
         h = C.c_void_p()

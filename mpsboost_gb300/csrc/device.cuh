@@ -136,6 +136,7 @@ struct Control {
   uint32_t leaf_chunks;
   uint32_t free_top;       // histogram-slot free stack
   uint32_t split_items;    // nodes x feature chunks
+  uint32_t item_rows;      // rows per histogram work item of the current level
   unsigned long long cells;       // cumulative row x feature cells built (accounting)
   unsigned long long rows_built;
 };

@@ -2,8 +2,11 @@
 //
 // Replaces the two-stage Metal histogram (src/mps/kernels/histogram.metal:34-182 driven
 // by src/mps/mps_histogram.mm:82-256). Design:
-//  * Bins are column-blocked u8, [feature_block][row][32]: one row of a block is one
-//    32-byte sector, gathered with two 16-byte cp.async copies.
+//  * Bins are u8 rows padded to a multiple of 32 features; a work item reads its 32-byte
+//    feature block of each gathered row with two 16-byte cp.async copies. The CTAs of the
+//    4 feature blocks of a row chunk run together, so one HBM fetch of a row's line
+//    serves all of them through L2. g/h arrive in the node's row order (the partition
+//    moves them along with the row ids), so they stream instead of being gathered.
 //  * Persistent CTAs (one per SM) pull work items (build node, row chunk <= 65536 rows,
 //    feature block) from a device counter; every frontier node of every tree of a level
 //    is in the same launch.
@@ -107,11 +110,15 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
     const uint32_t fb = item % nfb;
     const uint32_t chunk = item / nfb;
     const BuildEntry e = a.build[s_entry];
-    const uint32_t row_begin = (chunk - a.build_prefix[s_entry]) * a.item_rows;
-    const uint32_t row_count = row_begin < e.seg_cnt ? min(a.item_rows, e.seg_cnt - row_begin) : 0u;
-    const uint32_t* rows = a.rows + (size_t(e.tree) * 2 + e.parity) * n + e.seg_off + row_begin;
-    const float2* gh = a.gh + size_t(e.tree) * n;
-    const uint8_t* bins = a.bins + size_t(fb) * n * kBlockFeatures;
+    const uint32_t item_rows = a.item_rows ? a.item_rows : a.ctl->item_rows;
+    const uint32_t row_begin = (chunk - a.build_prefix[s_entry]) * item_rows;
+    const uint32_t row_count = row_begin < e.seg_cnt ? min(item_rows, e.seg_cnt - row_begin) : 0u;
+    const size_t seg = (size_t(e.tree) * 2 + e.parity) * n + e.seg_off + row_begin;
+    const uint32_t* rows = a.rows + seg;
+    // g/h in segment order (contiguous) or by row id (gathered).
+    const float2* gh_seg = a.gh_ordered ? a.gh + seg : nullptr;
+    const float2* gh_row = a.gh_ordered ? nullptr : a.gh + size_t(e.tree) * n;
+    const uint8_t* bins = a.bins + size_t(fb) * a.bins_block_stride;
     const int kg = a.trees[e.tree].kg;
     const int kh = a.trees[e.tree].kh;
 
@@ -130,9 +137,13 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
       const uint32_t r = __ldg(rows + pos);
       return r < n ? r : 0u;  // row ids are < n by construction
     };
+    auto gh_at = [&](uint32_t pos, uint32_t r) -> float2 {
+      if (pos >= row_count) return make_float2(0.f, 0.f);
+      return gh_seg ? __ldg(gh_seg + pos) : __ldg(gh_row + r);
+    };
     uint32_t r_cur = row_at(uint32_t(tid));
     uint32_t r_nxt = row_at(uint32_t(TILE + tid));
-    float2 g_cur = (uint32_t(tid) < row_count) ? __ldg(gh + r_cur) : make_float2(0.f, 0.f);
+    float2 g_cur = gh_at(uint32_t(tid), r_cur);
     for (int t = 0; t < ntiles + NSTAGE - 1; ++t) {
       if (t < ntiles) {
         const int s = t % NSTAGE;
@@ -140,11 +151,11 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
         const uint32_t r = r_cur;
         const float2 p = g_cur;
         const uint32_t r_far = row_at(pos + 2u * TILE);
-        g_cur = (pos + TILE < row_count) ? __ldg(gh + r_nxt) : make_float2(0.f, 0.f);
+        g_cur = gh_at(pos + TILE, r_nxt);
         r_cur = r_nxt;
         r_nxt = r_far;
         if (pos < row_count) {
-          const uint8_t* src = bins + size_t(r) * kBlockFeatures;
+          const uint8_t* src = bins + size_t(r) * a.bins_row_stride;
           cp_async16(stage_bins + (size_t(s) * TILE + tid) * 32, src);
           cp_async16(stage_bins + (size_t(s) * TILE + tid) * 32 + 16, src + 16);
           uint2 v;

@@ -328,9 +328,12 @@ int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t wi
     CK(cudaMemcpyAsync(d->bin_count.p, bin_count, features * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
     CK(cudaMemcpyAsync(d->has_missing.p, d->h_has_missing.data(), features, cudaMemcpyHostToDevice, b->stream));
     d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+    d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+    d->bins_fm.alloc(size_t(features) * rows);
     CK(launch_pack_bins(src.p, width, missing ? miss.as<uint8_t>() : nullptr,
                         d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb,
-                        d->bins.as<uint8_t>(), b->error.as<uint32_t>(), b->stream));
+                        d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(),
+                        d->bins_fm.as<uint8_t>(), b->error.as<uint32_t>(), b->stream));
     if (b->take_error()) throw DataError("Binned value exceeds the feature histogram range");
     *out = d.release();
   });
@@ -358,10 +361,15 @@ struct mpsb_cuda_trainer {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   std::vector<cudaEvent_t> events;  // 2 per level (histogram build begin/end)
+  unsigned long long* level_cells = nullptr;  // device: ctl->cells after each level's build
+  std::vector<double> level_ms;
+  std::vector<uint64_t> level_cells_total;
   uint32_t rounds_enqueued = 0;
+  uint32_t blocked_levels = 2;  // levels built from the column-blocked bins
   mpsb_cuda_stats stats{};
   uint64_t kernels_per_round = 0;
   uint64_t cells_base = 0, rows_base = 0;
+  unsigned long long cells_before_round = 0;
 
   template <class T>
   T* alloc(size_t count) {
@@ -393,9 +401,13 @@ struct mpsb_cuda_trainer {
       if (options & MPSB_OPT_PER_NODE) {
         k += enqueue_hist_per_node(d);
       } else {
-        CK(launch_hist_build(dev, hcfg, grid(1), s)); ++k;
+        CK(launch_hist_build(level_view(d), hcfg, grid(1), s)); ++k;
       }
-      if (record_events) CK(cudaEventRecord(events[2 * d + 1], s));
+      if (record_events) {
+        CK(cudaEventRecord(events[2 * d + 1], s));
+        CK(cudaMemcpyAsync(level_cells + d, &dev.ctl->cells, sizeof(unsigned long long),
+                           cudaMemcpyDeviceToDevice, s));
+      }
       if (d == 0) {
         CK(launch_root_stats(dev, s)); ++k;
       } else {
@@ -414,10 +426,22 @@ struct mpsb_cuda_trainer {
     return k;
   }
 
+  // Dense levels (every row of a node close to the next) read the column-blocked copy of
+  // the bins, whose 32-byte block rows are consecutive; sparse levels read the padded
+  // row-major copy, whose 128-byte row line serves all feature blocks through L2.
+  TrainerDev level_view(uint32_t d) const {
+    TrainerDev v = dev;
+    if (d < blocked_levels) {
+      v.bins = ds->bins_blocked.as<uint8_t>();
+      v.bins_row_stride = kBlockFeatures;
+      v.bins_block_stride = uint64_t(ds->n_rows) * kBlockFeatures;
+    }
+    return v;
+  }
+
   // Plain path: the host reads the level's build list and launches one histogram build
   // per node, waiting for each level (the per-node submit/wait of mps_histogram.mm:62-80).
   uint64_t enqueue_hist_per_node(uint32_t d) {
-    (void)d;
     cudaStream_t s = b->stream;
     Control c;
     CK(cudaMemcpyAsync(&c, dev.ctl, sizeof c, cudaMemcpyDeviceToHost, s));
@@ -428,7 +452,7 @@ struct mpsb_cuda_trainer {
     CK(cudaStreamSynchronize(s));
     uint64_t k = 0;
     for (uint32_t e = 0; e < c.n_build; ++e) {
-      TrainerDev one = dev;
+      TrainerDev one = level_view(d);
       one.item_begin = prefix[e] * dev.nfb;
       one.item_end = prefix[e + 1] * dev.nfb;
       CK(cudaMemsetAsync(&dev.ctl->hist_counter, 0, sizeof(uint32_t), s));
@@ -473,12 +497,21 @@ struct mpsb_cuda_trainer {
       ++stats.rounds;
       if (timing) {
         CK(cudaStreamSynchronize(b->stream));
-        for (uint32_t d = 0; d < std::max<uint32_t>(depth, 1); ++d) {
+        const uint32_t levels = std::max<uint32_t>(depth, 1);
+        std::vector<unsigned long long> after(levels);
+        CK(cudaMemcpy(after.data(), level_cells, levels * sizeof(unsigned long long),
+                      cudaMemcpyDeviceToHost));
+        level_ms.resize(levels, 0.0);
+        level_cells_total.resize(levels, 0);
+        for (uint32_t d = 0; d < levels; ++d) {
           float ms = 0.0f;
           CK(cudaEventElapsedTime(&ms, events[2 * d], events[2 * d + 1]));
           stats.hist_ms += ms;
           ++stats.hist_timed_launches;
+          level_ms[d] += ms;
+          level_cells_total[d] += after[d] - (d ? after[d - 1] : cells_before_round);
         }
+        cells_before_round = after[levels - 1];
       }
     }
   }
@@ -526,7 +559,11 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   TrainerDev& a = t->dev;
   a = TrainerDev{};
   a.bins = ds->bins.as<uint8_t>();
+  a.bins_row_stride = uint64_t(ds->nfb) * kBlockFeatures;
+  a.bins_block_stride = kBlockFeatures;
+  a.bins_fm = ds->bins_fm.as<uint8_t>();
   a.bin_count = ds->bin_count.as<uint32_t>();
+  a.sm_count = uint32_t(b->sm_count);
   a.has_missing = ds->has_missing.as<uint8_t>();
   a.n_rows = ds->n_rows;
   a.features = F;
@@ -537,18 +574,14 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.mode = (options & MPSB_OPT_FLOAT_HIST) ? kModeFloat : kModeFixed;
   a.scan_threads = 512;
   a.n_fchunks = (F + a.scan_threads / 32 - 1) / (a.scan_threads / 32);
-  // rows per histogram work item: enough items to fill the GPU, <= 65536 (packing bound)
-  {
-    const uint64_t target_items = uint64_t(b->sm_count) * 4;
-    uint64_t per = (uint64_t(n) * ds->nfb + target_items - 1) / target_items;
-    per = std::max<uint64_t>(per, 2048);
-    per = (per + 511) / 512 * 512;
-    a.item_rows = uint32_t(std::min<uint64_t>(per, kItemRowsMax));
-  }
+  // rows per histogram work item: chosen per level on the device (about four items per
+  // SM, within the 2^16-row limb bound)
+  a.item_rows = 0;
   // Tile-shape overrides (used by the tuning sweeps): threads per CTA, pipeline stages,
   // rows per work item.
   if (const char* v = std::getenv("MPSB_HIST_THREADS")) t->hcfg.threads = std::atoi(v);
   if (const char* v = std::getenv("MPSB_HIST_STAGES")) t->hcfg.stages = std::atoi(v);
+  if (const char* v = std::getenv("MPSB_BLOCKED_LEVELS")) t->blocked_levels = uint32_t(std::atoi(v));
   if (const char* v = std::getenv("MPSB_ITEM_ROWS"))
     a.item_rows = uint32_t(std::min<long>(std::max<long>(std::atol(v), 512), long(kItemRowsMax)));
   TreeParams& tp = a.params;
@@ -609,7 +642,8 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     a.group_masks = gm;
   }
   // working state
-  a.gh = t->alloc<float2>(size_t(T) * n);
+  a.gh = t->alloc<float2>(size_t(T) * 2 * n);
+  a.gh_ordered = 1;
   a.rows = t->alloc<uint32_t>(size_t(T) * 2 * n);
   a.trees = t->alloc<TreeState>(T);
   a.max_level_nodes = uint32_t(T * level_nodes);
@@ -652,6 +686,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   if (options & MPSB_OPT_TIMING) {
     t->events.resize(2 * std::max<uint32_t>(D, 1));
     for (auto& e : t->events) CK(cudaEventCreate(&e));
+    t->level_cells = t->alloc<unsigned long long>(std::max<uint32_t>(D, 1));
   }
   CK(cudaStreamSynchronize(s));
 }
@@ -717,7 +752,20 @@ int mpsb_cuda_trainer_reset_stats(mpsb_cuda_trainer* t) {
     CK(cudaMemcpy(&c, t->dev.ctl, sizeof c, cudaMemcpyDeviceToHost));
     t->cells_base = c.cells;
     t->rows_base = c.rows_built;
+    t->cells_before_round = c.cells;
     t->stats = mpsb_cuda_stats{};
+    t->level_ms.assign(t->level_ms.size(), 0.0);
+    t->level_cells_total.assign(t->level_cells_total.size(), 0);
+  });
+}
+
+int mpsb_cuda_trainer_level_stats(const mpsb_cuda_trainer* t, uint32_t n_levels, double* ms,
+                                  uint64_t* cells) {
+  return guard([&] {
+    for (uint32_t d = 0; d < n_levels; ++d) {
+      ms[d] = d < t->level_ms.size() ? t->level_ms[d] : 0.0;
+      cells[d] = d < t->level_cells_total.size() ? t->level_cells_total[d] : 0;
+    }
   });
 }
 
@@ -821,7 +869,7 @@ int mpsb_cuda_model_predict(mpsb_cuda_backend* b, const mpsb_cuda_model* m,
     cudaStream_t s = b->stream;
     CK(cudaMemcpyAsync(d_nodes.p, flat.data(), flat.size() * sizeof(mpsb_tree_node), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(d_off.p, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, s));
-    CK(launch_predict(ds->bins.as<uint8_t>(), ds->n_rows, ds->nfb, ds->has_missing.as<uint8_t>(),
+    CK(launch_predict(ds->bins_fm.as<uint8_t>(), ds->n_rows, ds->nfb, ds->has_missing.as<uint8_t>(),
                       d_nodes.as<TreeNodeOut>(), d_off.as<uint32_t>(), uint32_t(m->trees.size()),
                       m->base, m->learning_rate, d_out.as<double>(), b->error.as<uint32_t>(), s));
     CK(cudaMemcpyAsync(out, d_out.p, size_t(ds->n_rows) * sizeof(double), cudaMemcpyDeviceToHost, s));

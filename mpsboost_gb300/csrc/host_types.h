@@ -100,7 +100,7 @@ struct mpsb_cuda_backend {
 struct mpsb_cuda_dataset {
   mpsb_cuda_backend* backend = nullptr;
   uint32_t n_rows = 0, features = 0, nfb = 0;
-  mpsb::DevBuf bins, bin_count, has_missing;
+  mpsb::DevBuf bins, bins_blocked, bins_fm, bin_count, has_missing;
   std::vector<uint32_t> h_bin_count;
   std::vector<uint8_t> h_has_missing;
 };

@@ -32,6 +32,17 @@ __device__ __forceinline__ void raise(Control* ctl, uint32_t bits) { atomicOr(&c
 
 __device__ __forceinline__ uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
+// Rows per histogram work item for a level that builds `rows` rows: about four items per
+// SM, a multiple of 512, within [4096, kItemRowsMax].
+__device__ __forceinline__ uint32_t adaptive_item_rows(uint64_t rows, uint32_t nfb, uint32_t sms) {
+  const uint64_t target = uint64_t(sms ? sms : 152) * 4;
+  uint64_t per = (rows * nfb + target - 1) / target;
+  per = (per + 511) / 512 * 512;
+  if (per < 4096) per = 4096;
+  if (per > kItemRowsMax) per = kItemRowsMax;
+  return uint32_t(per);
+}
+
 // Exponent e with x < 2^e (frexp convention) of a positive finite float.
 __device__ __forceinline__ int exponent_above(float x) {
   int e;
@@ -172,7 +183,7 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
     }
     const float g32 = __double2float_rn(g), h32 = __double2float_rn(h);
     if (!isfinite(g32) || !isfinite(h32)) bad = 1;
-    a.gh[tree_off + i] = make_float2(g32, h32);
+    a.gh[size_t(t) * 2 * a.n_rows + i] = make_float2(g32, h32);  // parity 0 = row order
     a.rows[size_t(t) * 2 * a.n_rows + i] = i;
     mg = max(mg, __float_as_uint(fabsf(g32)));
     mh = max(mh, __float_as_uint(fmaxf(h32, 0.0f)));
@@ -199,7 +210,9 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
 }
 
 __global__ void round_setup_kernel(TrainerDev a) {
-  const uint32_t chunks_per_tree = ceil_div(a.n_rows, a.item_rows);
+  const uint32_t item_rows =
+      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(a.n_rows) * a.n_trees, a.nfb, a.sm_count);
+  const uint32_t chunks_per_tree = ceil_div(a.n_rows, item_rows);
   for (uint32_t base = 0; base < a.n_trees; base += blockDim.x) {
     const uint32_t t = base + threadIdx.x;
     if (t < a.n_trees) {
@@ -257,6 +270,7 @@ __global__ void round_setup_kernel(TrainerDev a) {
     a.ctl->hist_items = a.n_trees * chunks_per_tree * a.nfb;
     a.ctl->hist_counter = 0;
     a.ctl->split_items = a.n_trees * a.n_fchunks;
+    a.ctl->item_rows = item_rows;
   }
 }
 
@@ -501,7 +515,7 @@ __device__ __forceinline__ void consider(const TreeParams& p, const Stat<FIXED>&
 // One warp per (node, feature); a CTA covers one node and blockDim/32 features and
 // writes the best split of its features to partial[node][chunk].
 template <bool FIXED>
-__global__ void split_scan_kernel(TrainerDev a, int parity) {
+__global__ void __launch_bounds__(512) split_scan_kernel(TrainerDev a, int parity) {
   using V = typename Stat<FIXED>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SplitRec* warp_best = reinterpret_cast<SplitRec*>(smem_raw);
@@ -514,6 +528,7 @@ __global__ void split_scan_kernel(TrainerDev a, int parity) {
     const uint32_t i = item / n_chunks, c = item % n_chunks;
     const NodeRec node = a.nodes[parity][i];
     const double inv_g = a.trees[node.tree].inv_g, inv_h = a.trees[node.tree].inv_h;
+    const int st_kg = a.trees[node.tree].kg, st_kh = a.trees[node.tree].kh;
     const uint32_t f = c * uint32_t(nwarps) + uint32_t(warp);
     SplitRec best;
     best.valid = 0;
@@ -522,7 +537,8 @@ __global__ void split_scan_kernel(TrainerDev a, int parity) {
     best.threshold = 0;
     best.default_left = 1;
     uint32_t err = 0;
-    bool active = f < a.features;
+    // A node with fewer than 2 * min_samples_leaf rows has no admissible split.
+    bool active = f < a.features && node.count >= 2 * P.min_samples_leaf;
     if (active) {
       const uint32_t allowed = a.node_allowed[parity][i * P.path_words + (f >> 5)];
       active = (allowed >> (f & 31)) & 1u;
@@ -585,35 +601,106 @@ __global__ void split_scan_kernel(TrainerDev a, int parity) {
             P.split_strategy == 1
                 ? stable_random_threshold(P.random_seed, f, node.node_index, node.depth, nb - 1)
                 : 0xffffffffu;
+        // Exact FP32 pre-screen. Every eligible candidate's score S = gL^2/(hL+lambda) +
+        // gR^2/(hR+lambda) is computed in FP32 with relative error <= 7u (u = 2^-24, the
+        // conversions of g, h and lambda included). A candidate whose FP32 score is below
+        // M(1 - 2^-20), M the warp's best FP32 score over certainly eligible candidates, then
+        // has an exact score at least 2u*M below that candidate's, far outside the FP64
+        // evaluation's own rounding (a few 2^-53 * M, the parent score included), so its FP64
+        // gain is strictly lower and it cannot win. Only the rest -- and candidates whose
+        // min_child_weight test or score is too close to call in FP32 -- run the FP64
+        // evaluation of the reference. The score is quadratic only without reg_alpha, the
+        // admissible set monotone in it only without monotone constraints, and random
+        // thresholds leave one candidate: the screen is off for those, and where 2^-k leaves
+        // the FP32 normal range.
+        const bool screen = P.split_strategy == 0 && mono == 0 && P.reg_alpha == 0.0 &&
+                            P.reg_lambda > 0.0 &&
+                            (!FIXED || (st_kg >= -120 && st_kg <= 120 && st_kh >= -120 && st_kh <= 120));
+        const float lam32 = float(P.reg_lambda), mcw32 = float(P.min_child_weight);
+        // 2^-k exactly, built from the exponent field.
+        const float inv_g32 = FIXED && screen ? __int_as_float((127 - st_kg) << 23) : 1.0f;
+        const float inv_h32 = FIXED && screen ? __int_as_float((127 - st_kh) << 23) : 1.0f;
+        auto to32 = [&](V v, float inv32) -> float {
+          if constexpr (FIXED) return __ll2float_rn(v) * inv32;
+          else return __double2float_rn(v);
+        };
+        // 0: rejected by the FP64 test before any arithmetic (no error flag either);
+        // 1: admissible, FP32 score in *s32; 2: too close to call.
+        auto classify = [&](const Stat<FIXED>& cl, const Stat<FIXED>& cr, float* s32) -> int {
+          if (cl.count < P.min_samples_leaf || cr.count < P.min_samples_leaf) return 0;
+          if constexpr (!FIXED) {
+            if (!isfinite(cl.h) || !isfinite(cr.h) || !isfinite(cl.g) || !isfinite(cr.g)) return 2;
+          }
+          if (!(cl.h > 0) || !(cr.h > 0)) return 0;  // fixed point: image > 0 iff q > 0
+          const float lh = to32(cl.h, inv_h32), rh = to32(cr.h, inv_h32);
+          int cls = 1;
+          if (P.min_child_weight > 0.0) {
+            const float lo = mcw32 * (1.0f - 3e-6f), hi = mcw32 * (1.0f + 3e-6f);
+            if (lh < lo || rh < lo) return 0;
+            if (lh <= hi || rh <= hi) cls = 2;
+          }
+          const float lg = to32(cl.g, inv_g32), rg = to32(cr.g, inv_g32);
+          const float sc = __fdiv_rn(lg * lg, lh + lam32) + __fdiv_rn(rg * rg, rh + lam32);
+          if (!isfinite(sc)) cls = 2;
+          *s32 = sc;
+          return cls;
+        };
+        float best32 = -1.0f;
+        const Stat<FIXED> carry_in = left;
+        for (int pass = screen ? 0 : 1; pass < 2; ++pass) {
+          left = carry_in;
+          const float cut = best32 >= 1e-30f ? best32 * (1.0f - 0x1p-20f) : -1.0f;
 #pragma unroll 1
-        for (int k = 0; k < 8; ++k) {
-          const int s = lane * 8 + k;
-          if (!(hm && s == kMissingSlot)) {  // reload the slot (L1-resident)
-            Stat<FIXED> b;
-            b.count = base[s * 3 + 0];
-            if constexpr (FIXED) {
-              b.g = (long long)base[s * 3 + 1];
-              b.h = (long long)base[s * 3 + 2];
-            } else {
-              b.g = __longlong_as_double((long long)base[s * 3 + 1]);
-              b.h = __longlong_as_double((long long)base[s * 3 + 2]);
+          for (int k = 0; k < 8; ++k) {
+            const int s = lane * 8 + k;
+            bool empty_bin = false;
+            if (!(hm && s == kMissingSlot)) {  // reload the slot (L1-resident)
+              Stat<FIXED> b;
+              b.count = base[s * 3 + 0];
+              empty_bin = b.count == 0;
+              if constexpr (FIXED) {
+                b.g = (long long)base[s * 3 + 1];
+                b.h = (long long)base[s * 3 + 2];
+              } else {
+                b.g = __longlong_as_double((long long)base[s * 3 + 1]);
+                b.h = __longlong_as_double((long long)base[s * 3 + 2]);
+              }
+              left = stat_add<FIXED>(left, b);
             }
-            left = stat_add<FIXED>(left, b);
+            const uint32_t t = uint32_t(s);
+            if (t + 1 >= nb) continue;
+            const Stat<FIXED> right = stat_sub<FIXED>(nmp, left);
+            if (left.count > nmp.count) {
+              if (pass == 1) err |= kErrPrefix;
+              continue;
+            }
+            if (left.count == 0 && right.count == 0) continue;
+            if (P.split_strategy == 1 && t != rnd) continue;
+            // After an empty bin the candidate repeats threshold t-1's statistics exactly and
+            // loses the tie to it (IsBetterSplit prefers the lower threshold).
+            if (P.split_strategy == 0 && t > 0 && empty_bin) continue;
+            for (int d = 0; d < 2; ++d) {
+              const uint32_t dl = 1u - uint32_t(d);  // default_left 1, then 0
+              if (dl == 0 && miss.count == 0) break;
+              const Stat<FIXED> cl = dl ? stat_add<FIXED>(left, miss) : left;
+              const Stat<FIXED> cr = dl ? right : stat_add<FIXED>(right, miss);
+              if (pass == 0) {
+                float sc;
+                if (classify(cl, cr, &sc) == 1) best32 = fmaxf(best32, sc);
+              } else {
+                if (screen && cut > 0.0f) {
+                  float sc;
+                  const int cls = classify(cl, cr, &sc);
+                  if (cls == 0 || (cls == 1 && sc < cut)) continue;
+                }
+                consider<FIXED>(P, cl, cr, inv_g, inv_h, mono, node.lo, node.hi, f, t, dl, best, err);
+              }
+            }
           }
-          const uint32_t t = uint32_t(s);
-          if (t + 1 >= nb) continue;
-          const Stat<FIXED> right = stat_sub<FIXED>(nmp, left);
-          if (left.count > nmp.count) {
-            err |= kErrPrefix;
-            continue;
+          if (pass == 0) {
+            for (int off = 16; off > 0; off >>= 1)
+              best32 = fmaxf(best32, __shfl_xor_sync(0xffffffffu, best32, off));
           }
-          if (left.count == 0 && right.count == 0) continue;
-          if (P.split_strategy == 1 && t != rnd) continue;
-          consider<FIXED>(P, stat_add<FIXED>(left, miss), right, inv_g, inv_h, mono, node.lo,
-                          node.hi, f, t, 1u, best, err);
-          if (miss.count > 0)
-            consider<FIXED>(P, left, stat_add<FIXED>(right, miss), inv_g, inv_h, mono, node.lo,
-                            node.hi, f, t, 0u, best, err);
         }
       }
     }
@@ -698,11 +785,11 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
   for (uint32_t t = threadIdx.x; t < a.n_trees; t += blockDim.x) tree_acc[t] = 0;
   __syncthreads();
 
-  // Phase A: best split per node, valid flags, valid prefix.
-  uint32_t carry = 0;
+  // Phase A: best split per node, valid flags, valid prefix; rows the next level builds.
+  uint32_t carry = 0, built_units = 0;
   for (uint32_t base = 0; base < n; base += blockDim.x) {
     const uint32_t i = base + threadIdx.x;
-    uint32_t v[1] = {0};
+    uint32_t v[2] = {0, 0};
     uint32_t tree = 0;
     bool first = false;
     if (i < n) {
@@ -714,22 +801,26 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
         }
         a.partial[size_t(i) * a.n_fchunks] = b;
         v[0] = b.valid;
+        if (b.valid) v[1] = uint32_t(((b.lcount <= b.rcount ? b.lcount : b.rcount) + 255) / 256);
       }
       tree = a.nodes[parity][i].tree;
       first = i == 0 || a.nodes[parity][i - 1].tree != tree;
     }
-    uint32_t tot[1];
+    uint32_t tot[2];
     const uint32_t own = v[0];
-    block_scan<1>(v, tot, sh);
+    block_scan<2>(v, tot, sh);
     if (i < n) {
       a.scratch_flags[i] = own;
       a.scratch_prefix[i] = carry + v[0];
       if (first) tree_vbase[tree] = carry + v[0];
     }
     carry += tot[0];
+    built_units += tot[1];
     __syncthreads();
   }
   __syncthreads();
+  const uint32_t item_rows =
+      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(built_units) * 256, a.nfb, a.sm_count);
 
   // Phase B1: acceptance under max_leaves, accepted prefix, chunk prefixes.
   // Scanned values: 0 accepted, 1 build chunks, 2 partition chunks, 3 leaf segments,
@@ -753,7 +844,7 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
         const SplitRec& b = a.partial[size_t(i) * a.n_fchunks];
         const uint32_t built = uint32_t(b.lcount <= b.rcount ? b.lcount : b.rcount);
         if (!last) {
-          v[1] = ceil_div(built, a.item_rows);
+          v[1] = ceil_div(built, item_rows);
           v[2] = ceil_div(node.seg_cnt, kPartChunk);
         }
       }
@@ -972,6 +1063,7 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
       ctl->hist_items = carry6[1] * a.nfb;
       ctl->part_chunks = carry6[2];
       ctl->split_items = 2 * n_acc * a.n_fchunks;
+      ctl->item_rows = item_rows;
     }
     ctl->hist_counter = 0;
   }
@@ -991,8 +1083,8 @@ __device__ __forceinline__ uint32_t find_entry(const uint32_t* prefix, uint32_t 
 
 __device__ __forceinline__ bool row_goes_left(const TrainerDev& a, uint32_t row, uint32_t f,
                                               uint32_t thr, uint32_t dl) {
-  const uint8_t b =
-      a.bins[(size_t(f >> 5) * a.n_rows + row) * kBlockFeatures + (f & 31)];
+  // Feature-major copy: a node's rows are sorted, so neighbouring rows share sectors.
+  const uint8_t b = a.bins_fm[size_t(f) * a.n_rows + row];
   if (a.has_missing[f] && b == kMissingSlot) return dl != 0;
   return b <= thr;
 }
@@ -1089,8 +1181,12 @@ __global__ void __launch_bounds__(kPartThreads) partition_scatter_kernel(Trainer
       }
     }
     __syncthreads();
-    const uint32_t* src = a.rows + (size_t(pe.tree) * 2 + pe.parity) * a.n_rows + pe.seg_off + start;
-    uint32_t* dst = a.rows + (size_t(pe.tree) * 2 + (pe.parity ^ 1)) * a.n_rows + pe.seg_off;
+    const size_t src_off = (size_t(pe.tree) * 2 + pe.parity) * a.n_rows + pe.seg_off + start;
+    const size_t dst_off = (size_t(pe.tree) * 2 + (pe.parity ^ 1)) * a.n_rows + pe.seg_off;
+    const uint32_t* src = a.rows + src_off;
+    uint32_t* dst = a.rows + dst_off;
+    const float2* gh_src = a.gh_ordered ? a.gh + src_off : nullptr;
+    float2* gh_dst = a.gh_ordered ? a.gh + dst_off : nullptr;
     const uint32_t left_before_chunk = a.part_offsets[c];
     const uint32_t right_before_chunk = start - left_before_chunk;
 #pragma unroll
@@ -1104,8 +1200,12 @@ __global__ void __launch_bounds__(kPartThreads) partition_scatter_kernel(Trainer
         const bool left = (word >> lane) & 1u;
         const uint32_t r = src[p];
         const uint32_t rel = left ? left_before_chunk + lpos : pe.lcount + right_before_chunk + (p - lpos);
-        if (rel < pe.seg_cnt) dst[rel] = r;  // always true when the counts agree
-        else err = kErrPartition;
+        if (rel < pe.seg_cnt) {  // always true when the counts agree
+          dst[rel] = r;
+          if (a.gh_ordered) gh_dst[rel] = gh_src[p];
+        } else {
+          err = kErrPartition;
+        }
       }
     }
     __syncthreads();
@@ -1182,7 +1282,7 @@ __global__ void squared_error_kernel(const double* labels, const double* preds, 
 
 // RegressionModel::Predict (trainer.cpp:268-282): per row, trees in order,
 // result += lr * leaf; traversal of RegressionTree::Predict (tree.cpp:179-214).
-__global__ void predict_kernel(const uint8_t* bins, uint32_t n_rows, const uint8_t* has_missing,
+__global__ void predict_kernel(const uint8_t* bins_fm, uint32_t n_rows, const uint8_t* has_missing,
                                const TreeNodeOut* nodes, const uint32_t* tree_offsets,
                                uint32_t n_trees, double base, double lr, double* out,
                                uint32_t* error) {
@@ -1204,7 +1304,7 @@ __global__ void predict_kernel(const uint8_t* bins, uint32_t n_rows, const uint8
           break;
         }
         const uint32_t f = nd.feature_index;
-        const uint8_t b = bins[(size_t(f >> 5) * n_rows + r) * kBlockFeatures + (f & 31)];
+        const uint8_t b = bins_fm[size_t(f) * n_rows + r];
         const bool left = (has_missing[f] && b == kMissingSlot) ? nd.default_left != 0
                                                                  : b <= nd.threshold_bin;
         node = left ? nd.left_child : nd.right_child;
@@ -1215,12 +1315,14 @@ __global__ void predict_kernel(const uint8_t* bins, uint32_t n_rows, const uint8
   if (bad) atomicOr(error, kErrCapacity);
 }
 
-// Feature-major [features][rows] bins (u8 or u16) + optional missing mask ->
-// column-blocked u8 [nfb][rows][32] with missing rows at slot 255. Out-of-range bins
-// raise kErrGradient-free data errors through `error` (bit 0).
+// Feature-major [features][rows] bins (u8 or u16) + optional missing mask -> three u8
+// layouts with missing rows at 255: rows padded to nfb * 32 bytes and column blocks
+// [nfb][rows][32] (histograms of sparse and dense levels), and a feature-major copy (row
+// routing). Out-of-range bins set bit 0 of `error`.
 __global__ void pack_bins_kernel(const void* src, uint32_t width, const uint8_t* missing,
                                  const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
-                                 uint32_t nfb, uint8_t* out, uint32_t* error) {
+                                 uint32_t nfb, uint8_t* out, uint8_t* out_blocked,
+                                 uint8_t* out_fm, uint32_t* error) {
   __shared__ uint8_t tile[32][129];
   const uint32_t fb = blockIdx.y;
   uint32_t bad = 0;
@@ -1244,13 +1346,17 @@ __global__ void pack_bins_kernel(const void* src, uint32_t width, const uint8_t*
         }
       }
       tile[c][r] = v;
+      if (f < features && row < n_rows) out_fm[size_t(f) * n_rows + row] = v;
     }
     __syncthreads();
-    // store 128 rows x 32 bytes (coalesced along the block row)
+    // store 128 rows x 32 bytes: row-major rows padded to nfb * 32 bytes
     for (uint32_t k = threadIdx.x; k < 32 * 128; k += blockDim.x) {
       const uint32_t r = k / 32, c = k % 32;
       const uint32_t row = r0 + r;
-      if (row < n_rows) out[(size_t(fb) * n_rows + row) * kBlockFeatures + c] = tile[c][r];
+      if (row < n_rows) {
+        out[size_t(row) * nfb * kBlockFeatures + fb * kBlockFeatures + c] = tile[c][r];
+        out_blocked[(size_t(fb) * n_rows + row) * kBlockFeatures + c] = tile[c][r];
+      }
     }
     __syncthreads();
   }
@@ -1325,19 +1431,21 @@ cudaError_t launch_squared_error(const double* labels, const double* preds, uint
 }
 cudaError_t launch_pack_bins(const void* src, uint32_t width, const uint8_t* missing,
                              const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
-                             uint32_t nfb, uint8_t* out, uint32_t* error, cudaStream_t s) {
+                             uint32_t nfb, uint8_t* out_rows, uint8_t* out_blocked,
+                             uint8_t* out_fm, uint32_t* error, cudaStream_t s) {
   const uint32_t gx = std::min<uint32_t>((n_rows + 127) / 128, 4096u);
   pack_bins_kernel<<<dim3(gx > 0 ? gx : 1, nfb), 256, 0, s>>>(src, width, missing, bin_count,
-                                                              n_rows, features, nfb, out, error);
+                                                              n_rows, features, nfb, out_rows,
+                                                              out_blocked, out_fm, error);
   return cudaGetLastError();
 }
-cudaError_t launch_predict(const uint8_t* bins, uint32_t n_rows, uint32_t nfb,
+cudaError_t launch_predict(const uint8_t* bins_fm, uint32_t n_rows, uint32_t nfb,
                            const uint8_t* has_missing, const TreeNodeOut* nodes,
                            const uint32_t* tree_offsets, uint32_t n_trees, double base,
                            double lr, double* out, uint32_t* error, cudaStream_t s) {
   (void)nfb;
   const int grid = int(std::min<uint64_t>((n_rows + 255) / 256, 152ull * 16));
-  predict_kernel<<<grid > 0 ? grid : 1, 256, 0, s>>>(bins, n_rows, has_missing, nodes,
+  predict_kernel<<<grid > 0 ? grid : 1, 256, 0, s>>>(bins_fm, n_rows, has_missing, nodes,
                                                       tree_offsets, n_trees, base, lr, out, error);
   return cudaGetLastError();
 }

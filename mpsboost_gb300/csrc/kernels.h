@@ -11,7 +11,10 @@ namespace mpsb {
 // Device pointers and sizes of one training session, passed by value to every kernel.
 struct TrainerDev {
   // dataset
-  const uint8_t* bins;          // [nfb][n_rows][32] column-blocked u8 bins
+  const uint8_t* bins;          // u8 bins for histograms: row r, feature f at
+                                //   r * bins_row_stride + (f/32) * bins_block_stride + f%32
+  uint64_t bins_row_stride, bins_block_stride;
+  const uint8_t* bins_fm;       // [features][n_rows] feature-major u8 bins (routing rows)
   const uint32_t* bin_count;    // [features]
   const uint8_t* has_missing;   // [features]
   uint32_t n_rows, features, nfb, n_trees;
@@ -21,7 +24,9 @@ struct TrainerDev {
   uint32_t weights_per_tree;
   uint32_t objective;
   double* preds;                // [n_trees][n_rows]
-  float2* gh;                   // [n_trees][n_rows]
+  float2* gh;                   // gh_ordered: [n_trees][2][n_rows] in row-segment order
+                                // (moved along by the partition); else [n_trees][n_rows]
+  uint32_t gh_ordered;
   uint32_t* rows;               // [n_trees][2][n_rows]
   TreeState* trees;             // [n_trees]
   TreeParams params;
@@ -54,7 +59,9 @@ struct TrainerDev {
   TreeNodeOut* tree_nodes;      // [n_trees][max_tree_nodes]
   uint32_t max_tree_nodes;
   Control* ctl;
-  uint32_t item_rows;           // rows per histogram work item (<= kItemRowsMax)
+  uint32_t item_rows;           // rows per histogram work item (<= kItemRowsMax); 0: the
+                                // level's adaptive value ctl->item_rows
+  uint32_t sm_count;
   uint32_t mode;                // kModeFixed / kModeFloat
   uint32_t ovr;                 // labels are class ids; tree t fits class t (logistic)
   uint32_t scan_threads;        // block size of the split scan (multiple of 32)
@@ -95,14 +102,15 @@ cudaError_t launch_apply_leaves(const TrainerDev& a, int grid, cudaStream_t stre
 cudaError_t launch_round_end(const TrainerDev& a, cudaStream_t stream);
 cudaError_t launch_squared_error(const double* labels, const double* preds, uint64_t n,
                                  double* out_pairs, uint32_t* error, cudaStream_t stream);
-cudaError_t launch_predict(const uint8_t* bins, uint32_t n_rows, uint32_t nfb,
+cudaError_t launch_predict(const uint8_t* bins_fm, uint32_t n_rows, uint32_t nfb,
                            const uint8_t* has_missing, const TreeNodeOut* nodes,
                            const uint32_t* tree_offsets, uint32_t n_trees, double base,
                            double learning_rate, double* out, uint32_t* error,
                            cudaStream_t stream);
 cudaError_t launch_pack_bins(const void* src, uint32_t width, const uint8_t* missing,
                              const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
-                             uint32_t nfb, uint8_t* out, uint32_t* error, cudaStream_t stream);
+                             uint32_t nfb, uint8_t* out_rows, uint8_t* out_blocked,
+                             uint8_t* out_fm, uint32_t* error, cudaStream_t stream);
 // Number of kernels each launch_* helper enqueues (launch accounting).
 constexpr int kPartitionKernels = 3;
 

@@ -163,7 +163,10 @@ extern "C" int mpsb_cuda_build_histogram_noalloc(const uint8_t* bins, uint32_t d
     noalloc_setup_kernel<<<1, 1, 0, s>>>(st, build, prefix, ctl, n_rows, uint32_t(per), nfb);
     CK(cudaGetLastError());
     TrainerDev a{};
-    a.bins = bins;
+    a.bins = bins;  // column-blocked [nfb][dataset_rows][32]
+    a.bins_row_stride = kBlockFeatures;
+    a.bins_block_stride = uint64_t(dataset_rows) * kBlockFeatures;
+    a.sm_count = uint32_t(sc.sm_count);
     a.n_rows = dataset_rows;
     a.features = features;
     a.nfb = nfb;

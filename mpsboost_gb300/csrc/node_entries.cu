@@ -41,6 +41,10 @@ struct Session {
 void base_session(Session& ss, mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds) {
   TrainerDev& a = ss.a;
   a.bins = ds->bins.as<uint8_t>();
+  a.bins_row_stride = uint64_t(ds->nfb) * kBlockFeatures;
+  a.bins_block_stride = kBlockFeatures;
+  a.bins_fm = ds->bins_fm.as<uint8_t>();
+  a.sm_count = uint32_t(b->sm_count);
   a.bin_count = ds->bin_count.as<uint32_t>();
   a.has_missing = ds->has_missing.as<uint8_t>();
   a.n_rows = ds->n_rows;

@@ -18,7 +18,9 @@ constexpr uint32_t kItemRowsMax = 65536;  // rows of one histogram work item (li
 constexpr uint32_t kPartChunk = 4096;     // rows per partition chunk
 constexpr uint32_t kApplyChunk = 4096;    // rows per leaf-application chunk
 
-enum : int { kModeFixed = 0, kModeFloat = 1 };
+// kModeFixedG: fixed point, gradient limbs only (a root build whose count and hessian
+// histograms are restored from the fit's first round).
+enum : int { kModeFixed = 0, kModeFloat = 1, kModeFixedG = 2 };
 
 // Device status bits (ORed into TrainerState::error).
 enum : uint32_t {
@@ -31,6 +33,7 @@ enum : uint32_t {
   kErrCapacity = 1u << 6,        // an internal table overflowed
   kErrGradient = 1u << 7,        // invalid label / prediction / weight / gradient
   kErrPrefix = 1u << 8,          // prefix exceeded the non-missing parent (tree_split.cpp:212-214)
+  kErrRootCache = 1u << 9,       // the hessian scale of a reused root histogram changed
 };
 
 // Tree parameters resolved on the host (tree.hpp:47-72, tree_structure.cpp:54-62).

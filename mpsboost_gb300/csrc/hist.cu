@@ -13,10 +13,12 @@
 //  * A multi-stage cp.async pipeline stages each gathered row's 32-byte bin sector; the
 //    staging thread also writes the row's quantized g/h (computed once per row) next to
 //    it. Row ids are prefetched two tiles ahead and g/h one tile ahead in registers.
-//  * The CTA-private histogram lives in shared memory laid out [bin][feature] and lane l
-//    of every warp owns feature l: per row a warp does one byte load, one broadcast load
-//    of the row's values and one red.shared per accumulator; the 32 lanes hit 32
-//    different features, so their words fall in different banks for any bin values.
+//  * The CTA-private histogram lives in shared memory laid out [bin][feature]. A warp
+//    takes four staged rows at a time: each lane loads one 4-byte word (four features of
+//    one row) and the row's values, then issues four rounds of reductions in which the
+//    32 lanes touch 32 different features, so their words fall in different banks for
+//    any bin values. Per four rows: one bins wavefront, one values wavefront, and one
+//    red.shared per accumulator per feature.
 //  * Only 32-bit integer shared reductions are native on sm_103 (64-bit and FP32 ones run
 //    several times slower), so fixed mode splits each quantized value q (|q| <= 2^30) into
 //    a 16-bit unsigned low limb and a signed high limb and accumulates count, g_lo, g_hi,
@@ -58,13 +60,17 @@ struct HistSmem<kModeFixed> {  // count, g_lo, g_hi, h_lo, h_hi: five u32 words 
   static constexpr size_t kBytes = 5ull * kSlots * kBlockFeatures * sizeof(uint32_t);
 };
 template <>
+struct HistSmem<kModeFixedG> {  // g_lo, g_hi
+  static constexpr size_t kBytes = 2ull * kSlots * kBlockFeatures * sizeof(uint32_t);
+};
+template <>
 struct HistSmem<kModeFloat> {
   static constexpr size_t kBytes = 3ull * kSlots * kBlockFeatures * sizeof(uint32_t);
 };
 
 // Per staged row: 32 bin bytes (cp.async) and 8 bytes of per-row values written by the
 // staging thread: fixed mode the limbs {g_lo | h_lo << 16, g_hi | h_hi << 16} (16-bit
-// each), float mode {g, h}.
+// each), gradient-only mode {g_lo | g_hi << 16, 0}, float mode {g, h}.
 constexpr int kRowBytes = 32 + 8;
 
 template <int MODE, int THREADS, int NSTAGE>
@@ -86,8 +92,6 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
   const uint32_t n = a.n_rows;
   const uint32_t nfb = a.nfb;
   const uint32_t hist_base = static_cast<uint32_t>(__cvta_generic_to_shared(hist_smem));
-  // lane = feature of the block: its cell (bin b) lives at word b * 32 + lane
-  const uint32_t lane_base = hist_base + uint32_t(lane) * 4u;
 
   for (;;) {
     const uint32_t limit = a.item_end ? a.item_end : a.ctl->hist_items;
@@ -167,6 +171,10 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
             const uint32_t glo = uint32_t(qg) & 0xFFFFu, ghi = uint32_t(qg >> 16) & 0xFFFFu;
             const uint32_t hlo = uint32_t(qh) & 0xFFFFu, hhi = uint32_t(qh >> 16) & 0xFFFFu;
             v = make_uint2(glo | (hlo << 16), ghi | (hhi << 16));
+          } else if constexpr (MODE == kModeFixedG) {
+            // |q| <= 2^30: the low 32 bits hold q in two's complement; the reductions
+            // take its unsigned low and signed high 16 bits.
+            v = make_uint2(uint32_t(quantize_f32(p.x, kg)), 0u);
           } else {
             v = make_uint2(__float_as_uint(p.x), __float_as_uint(p.y));
           }
@@ -184,33 +192,47 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
         const uint2* sv = stage_val + s * TILE;
         const int row0 = warp * RPW;
         const int nrows = max(0, min(RPW, tile_rows - row0));
-        auto accumulate = [&](uint32_t b, uint2 q) {
-          const uint32_t addr = lane_base + b * (kBlockFeatures * 4u);
+        // A warp takes its rows four at a time: lane l reads the 4-byte word (l & 7) of row
+        // l >> 3 (four features' bins) and that row's values, so one 128-byte wavefront
+        // brings the bins of four rows and one more their values. In the i-th reduction
+        // round lane l updates byte (i + (l >> 3)) & 3 of its word: across the warp the 32
+        // features are distinct, so the 32 words fall in 32 different banks.
+        const uint32_t quad_byte = uint32_t(lane & 7) * 4u;
+        const uint32_t rot = uint32_t(lane >> 3);
+        auto accumulate = [&](uint32_t f, uint32_t b, uint2 q) {
+          const uint32_t addr = hist_base + (b * kBlockFeatures + f) * 4u;
           if constexpr (MODE == kModeFixed) {
             red_shared_u32<0>(addr, 1u);
             red_shared_u32<1u * CELLS * 4u>(addr, q.x & 0xFFFFu);
             red_shared_u32<2u * CELLS * 4u>(addr, uint32_t(int32_t(int16_t(q.y & 0xFFFFu))));
             red_shared_u32<3u * CELLS * 4u>(addr, q.x >> 16);
             red_shared_u32<4u * CELLS * 4u>(addr, q.y >> 16);
+          } else if constexpr (MODE == kModeFixedG) {
+            red_shared_u32<0>(addr, q.x & 0xFFFFu);
+            red_shared_u32<1u * CELLS * 4u>(addr, uint32_t(int32_t(q.x) >> 16));
           } else {
             red_shared_u32<0>(addr, 1u);
             red_shared_f32<CELLS * 4u>(addr, __uint_as_float(q.x));
             red_shared_f32<2u * CELLS * 4u>(addr, __uint_as_float(q.y));
           }
         };
-        int j = 0;
-        for (; j + 4 <= nrows; j += 4) {
-          uint32_t b[4];
-          uint2 q[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            b[u] = sb[(row0 + j + u) * 32 + lane];
-            q[u] = sv[row0 + j + u];
+        for (int j = 0; j < nrows; j += 4) {
+          const int r = j + int(rot);
+          const bool ok = r < nrows;
+          uint32_t w = 0;
+          uint2 q = make_uint2(0u, 0u);
+          if (ok) {
+            w = *reinterpret_cast<const uint32_t*>(sb + (row0 + r) * 32 + quad_byte);
+            q = sv[row0 + r];
           }
+          if (ok) {
 #pragma unroll
-          for (int u = 0; u < 4; ++u) accumulate(b[u], q[u]);
+            for (uint32_t i = 0; i < 4; ++i) {
+              const uint32_t sel = (i + rot) & 3u;
+              accumulate(quad_byte + sel, (w >> (8u * sel)) & 0xFFu, q);
+            }
+          }
         }
-        for (; j < nrows; ++j) accumulate(sb[(row0 + j) * 32 + lane], sv[row0 + j]);
         __syncthreads();
       }
     }
@@ -231,6 +253,10 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
         atomicAdd(dst + 0, (unsigned long long)cnt);
         atomicAdd(dst + 1, (unsigned long long)g);
         atomicAdd(dst + 2, (unsigned long long)hh);
+      } else if constexpr (MODE == kModeFixedG) {
+        const uint32_t* w = reinterpret_cast<const uint32_t*>(hist_smem);
+        const long long g = (long long)int32_t(w[CELLS + idx]) * 65536 + (long long)w[idx];
+        if (g != 0) atomicAdd(dst + 1, (unsigned long long)g);
       } else {
         const uint32_t* hc = reinterpret_cast<const uint32_t*>(hist_smem);
         const float* hgf = reinterpret_cast<const float*>(hc + CELLS);
@@ -274,7 +300,12 @@ cudaError_t launch_variant(const TrainerDev& a, int grid, cudaStream_t stream) {
 
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,
                               cudaStream_t stream) {
-  // Shared memory: 160 KB (fixed) / 96 KB (float) histogram + stages x threads x 40 B.
+  // Shared memory: 160 KB (fixed) / 64 KB (gradient only) / 96 KB (float) histogram +
+  // stages x threads x 40 B.
+  if (a.mode == kModeFixedG) {
+    if (cfg.threads == 1024) return launch_variant<kModeFixedG, 1024, 2>(a, grid, stream);
+    return launch_variant<kModeFixedG, 768, 2>(a, grid, stream);
+  }
   if (a.mode == kModeFixed) {
     if (cfg.threads == 768) return launch_variant<kModeFixed, 768, 2>(a, grid, stream);
     if (cfg.threads == 640) return launch_variant<kModeFixed, 640, 2>(a, grid, stream);

@@ -41,6 +41,7 @@ std::string describe_device_error(uint32_t bits) {
   if (bits & kErrCapacity) m += " internal capacity exceeded;";
   if (bits & kErrGradient) m += " invalid label, prediction, weight or gradient;";
   if (bits & kErrPrefix) m += " non-missing histogram prefix exceeded parent;";
+  if (bits & kErrRootCache) m += " hessian scale of the reused root histogram changed;";
   return m;
 }
 
@@ -358,8 +359,12 @@ struct mpsb_cuda_trainer {
   HistConfig hcfg;
   std::vector<std::unique_ptr<DevBuf>> bufs;
   std::vector<double> base_scores;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t graph_exec = nullptr;
+  // One graph for a full round and one for a round that reuses the roots' count and
+  // hessian histograms.
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  bool root_reuse = false;  // the hessian does not depend on the prediction
+  bool root_saved = false;  // a round has saved the roots' count/hessian histograms
   std::vector<cudaEvent_t> events;  // 2 per level (histogram build begin/end)
   unsigned long long* level_cells = nullptr;  // device: ctl->cells after each level's build
   std::vector<double> level_ms;
@@ -367,7 +372,7 @@ struct mpsb_cuda_trainer {
   uint32_t rounds_enqueued = 0;
   uint32_t blocked_levels = 2;  // levels built from the column-blocked bins
   mpsb_cuda_stats stats{};
-  uint64_t kernels_per_round = 0;
+  uint64_t kernels_per_round[2] = {0, 0};
   uint64_t cells_base = 0, rows_base = 0;
   unsigned long long cells_before_round = 0;
 
@@ -379,15 +384,18 @@ struct mpsb_cuda_trainer {
   }
 
   ~mpsb_cuda_trainer() {
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
-    if (graph) cudaGraphDestroy(graph);
+    for (int i = 0; i < 2; ++i) {
+      if (graph_exec[i]) cudaGraphExecDestroy(graph_exec[i]);
+      if (graph[i]) cudaGraphDestroy(graph[i]);
+    }
     for (cudaEvent_t e : events) cudaEventDestroy(e);
   }
 
   int grid(int per_sm) const { return b->sm_count * per_sm; }
 
-  // Enqueue one boosting round. Returns the number of kernels enqueued.
-  uint64_t enqueue_round(bool record_events) {
+  // Enqueue one boosting round. Returns the number of kernels enqueued. root_gradient_only:
+  // the roots' count and hessian histograms come from the fit's first round.
+  uint64_t enqueue_round(bool record_events, bool root_gradient_only) {
     cudaStream_t s = b->stream;
     uint64_t k = 0;
     CK(launch_round_begin(dev, s)); ++k;
@@ -401,7 +409,9 @@ struct mpsb_cuda_trainer {
       if (options & MPSB_OPT_PER_NODE) {
         k += enqueue_hist_per_node(d);
       } else {
-        CK(launch_hist_build(level_view(d), hcfg, grid(1), s)); ++k;
+        TrainerDev view = level_view(d);
+        if (d == 0 && root_gradient_only) view.mode = kModeFixedG;
+        CK(launch_hist_build(view, hcfg, grid(1), s)); ++k;
       }
       if (record_events) {
         CK(cudaEventRecord(events[2 * d + 1], s));
@@ -409,6 +419,9 @@ struct mpsb_cuda_trainer {
                            cudaMemcpyDeviceToDevice, s));
       }
       if (d == 0) {
+        if (root_reuse) {
+          CK(launch_root_cache(dev, root_gradient_only ? 0 : 1, grid(4), s)); ++k;
+        }
         CK(launch_root_stats(dev, s)); ++k;
       } else {
         CK(launch_subtract(dev, grid(8), s)); ++k;
@@ -471,27 +484,30 @@ struct mpsb_cuda_trainer {
     // Events captured into a graph cannot be timed, so timing runs launch directly.
     const bool use_graph = !(options & (MPSB_OPT_NO_GRAPH | MPSB_OPT_PER_NODE | MPSB_OPT_TIMING));
     for (uint32_t r = 0; r < rounds; ++r) {
+      const bool g_only = root_reuse && root_saved;
+      const int gi = g_only ? 1 : 0;
       if (use_graph) {
-        if (!graph_exec) {
+        if (!graph_exec[gi]) {
           CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
           uint64_t k = 0;
           try {
-            k = enqueue_round(timing);
+            k = enqueue_round(timing, g_only);
           } catch (...) {
             cudaGraph_t g = nullptr;
             cudaStreamEndCapture(b->stream, &g);
             if (g) cudaGraphDestroy(g);
             throw;
           }
-          CK(cudaStreamEndCapture(b->stream, &graph));
-          CK(cudaGraphInstantiate(&graph_exec, graph, 0));
-          kernels_per_round = k;
+          CK(cudaStreamEndCapture(b->stream, &graph[gi]));
+          CK(cudaGraphInstantiate(&graph_exec[gi], graph[gi], 0));
+          kernels_per_round[gi] = k;
         }
-        CK(cudaGraphLaunch(graph_exec, b->stream));
-        stats.kernel_launches += kernels_per_round;
+        CK(cudaGraphLaunch(graph_exec[gi], b->stream));
+        stats.kernel_launches += kernels_per_round[gi];
       } else {
-        stats.kernel_launches += enqueue_round(timing);
+        stats.kernel_launches += enqueue_round(timing, g_only);
       }
+      root_saved = root_reuse;
       stats.hist_launches += (options & MPSB_OPT_PER_NODE) ? 0 : std::max<uint32_t>(depth, 1);
       ++rounds_enqueued;
       ++stats.rounds;
@@ -584,6 +600,16 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   if (const char* v = std::getenv("MPSB_BLOCKED_LEVELS")) t->blocked_levels = uint32_t(std::atoi(v));
   if (const char* v = std::getenv("MPSB_ITEM_ROWS"))
     a.item_rows = uint32_t(std::min<long>(std::max<long>(std::atol(v), 512), long(kItemRowsMax)));
+  // Squared error and quantile have hessian = sample weight, the same in every round: the
+  // roots' count and hessian histograms are built once per fit (MPSB_ROOT_REUSE=0 builds
+  // them every round).
+  t->root_reuse = a.mode == kModeFixed && !(options & MPSB_OPT_PER_NODE) &&
+                  (p->objective == MPSB_SQUARED_ERROR || p->objective == MPSB_QUANTILE);
+  if (const char* v = std::getenv("MPSB_ROOT_REUSE")) t->root_reuse = t->root_reuse && std::atoi(v) != 0;
+  if (t->root_reuse) {
+    a.root_cache = t->alloc<unsigned long long>(size_t(T) * F * kSlots * 2);
+    a.root_cache_kh = t->alloc<int>(T);
+  }
   TreeParams& tp = a.params;
   tp.min_samples_leaf = p->min_samples_leaf;
   tp.min_child_weight = p->min_child_weight;

@@ -4,6 +4,8 @@
 //                  FP64 math rounded once to FP32 pairs, plus per-tree max|g| / max h for
 //                  the fixed-point scales.
 //   round_setup    fixed-point exponents, root node, level-0 build list.
+//   root_cache     the roots' count and hessian histograms kept from a fit's first round
+//                  (objectives whose hessian does not depend on the prediction).
 //   root_stats     root statistics from the root histogram; root leaf value
 //                  (TreeTrainingAccess::Create, tree_structure.cpp:104-116).
 //   subtract       SubtractHistograms (tree_histogram.cpp:16-66): exact int64 in fixed
@@ -284,6 +286,35 @@ __global__ void zero_build_slots_kernel(TrainerDev a) {
     const uint64_t w = idx % (words_per_slot / 2);
     reinterpret_cast<ulonglong2*>(a.hist + a.build[e].slot * words_per_slot)[w] =
         make_ulonglong2(0, 0);
+  }
+}
+
+// The root of every tree holds all rows in every round, so its count histogram never
+// changes, and when the hessian does not depend on the prediction (squared error and
+// quantile: h = weight) neither does its hessian histogram, nor the hessian scale. The
+// first round of a fit builds the roots in full and saves those two words per cell; later
+// rounds build only the gradient limbs and restore them. The hessian scale is checked.
+__global__ void root_cache_kernel(TrainerDev a, int save) {
+  const uint64_t per_tree = uint64_t(a.features) * kSlots;
+  const uint64_t total = per_tree * a.n_trees;
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < total;
+       i += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t t = uint32_t(i / per_tree);
+    const uint64_t cell = i % per_tree;
+    unsigned long long* slot = a.hist + (uint64_t(a.build[t].slot) * per_tree + cell) * 3;
+    unsigned long long* c = a.root_cache + i * 2;
+    if (save) {
+      c[0] = slot[0];
+      c[1] = slot[2];
+      if (cell == 0) a.root_cache_kh[t] = a.trees[t].kh;
+    } else {
+      if (a.root_cache_kh[t] != a.trees[t].kh) {
+        if (cell == 0) raise(a.ctl, kErrRootCache);
+        continue;
+      }
+      slot[0] = c[0];
+      slot[2] = c[1];
+    }
   }
 }
 
@@ -1383,6 +1414,10 @@ cudaError_t launch_zero_build_slots(const TrainerDev& a, int grid, cudaStream_t 
 }
 cudaError_t launch_root_stats(const TrainerDev& a, cudaStream_t s) {
   root_stats_kernel<<<1, 1024, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_root_cache(const TrainerDev& a, int save, int grid, cudaStream_t s) {
+  root_cache_kernel<<<grid, 256, 0, s>>>(a, save);
   return cudaGetLastError();
 }
 cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t s) {

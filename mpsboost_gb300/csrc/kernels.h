@@ -78,6 +78,10 @@ struct TrainerDev {
   // Histogram item range of one launch: [item_begin, item_end); item_end 0 = the whole
   // level (ctl->hist_items). Per-node launches of the plain path set a node's range.
   uint32_t item_begin, item_end;
+  // Root count/hessian histograms of the fit's first round: [n_trees][features][256]
+  // {count, qh} and the hessian scale they were built with (null: not reused).
+  unsigned long long* root_cache;
+  int* root_cache_kh;
 };
 
 struct HistConfig {
@@ -92,6 +96,9 @@ cudaError_t launch_gradients(const TrainerDev& a, int grid, cudaStream_t stream)
 cudaError_t launch_round_setup(const TrainerDev& a, cudaStream_t stream);
 cudaError_t launch_zero_build_slots(const TrainerDev& a, int grid, cudaStream_t stream);
 cudaError_t launch_root_stats(const TrainerDev& a, cudaStream_t stream);
+// save != 0: copy the roots' count and hessian words into root_cache; else restore them
+// into the roots' slots (after a gradient-only build).
+cudaError_t launch_root_cache(const TrainerDev& a, int save, int grid, cudaStream_t stream);
 cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t stream);
 cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStream_t stream);
 cudaError_t launch_finalize(const TrainerDev& a, int parity, uint32_t depth, cudaStream_t stream);

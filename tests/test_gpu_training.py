@@ -160,6 +160,22 @@ def test_paths_agree(backend):
     assert a.train_predictions.tobytes() == c.train_predictions.tobytes()
 
 
+@pytest.mark.parametrize("objective", ["squared_error", "quantile"])
+def test_root_reuse_is_exact(backend, monkeypatch, objective):
+    """Rounds that restore the roots' count/hessian histograms from the first round give
+    the same trees as rounds that build them in full."""
+    x, y, w = _data(45, 20000, 12, 0.05, 2, objective)
+    binned = mb.quantize_dense(x, 255)
+    params = dict(n_estimators=4, learning_rate=0.2, max_depth=6, min_samples_leaf=2,
+                  objective=objective)
+    a = mb.train_regressor(backend, binned, y, w, **params)
+    monkeypatch.setenv("MPSB_ROOT_REUSE", "0")
+    b = mb.train_regressor(backend, binned, y, w, **params)
+    for t1, t2 in zip(a.trees, b.trees):
+        assert t1.tobytes() == t2.tobytes()
+    assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
+
+
 def test_logistic_against_replica(backend, port):
     x, y, w = _data(41, 6000, 8, 0.1, 2, "binary_logistic")
     params = dict(n_estimators=3, learning_rate=0.2, max_depth=5, min_samples_leaf=4,

@@ -83,6 +83,8 @@ struct SplitRec {
   double lg, lh, rg, rh;
   double ll, lu, rl, ru;
 };
+static_assert(sizeof(SplitRec) % 8 == 0 && sizeof(SplitRec) / 8 <= 32,
+              "a warp copies a SplitRec one 8-byte word per lane");
 
 // Output tree node, layout of mpsb_tree_node.
 struct TreeNodeOut {
@@ -208,6 +210,71 @@ __device__ __forceinline__ uint32_t stable_random_threshold(uint32_t seed, uint3
   v *= 0x94D049BB133111EBULL;
   v ^= v >> 31;
   return (uint32_t)(v % candidates);
+}
+
+// IEEE-754 conversions on the integer pipe. sm_103 runs FP64 arithmetic and 64-bit
+// conversions on a narrow FP64 pipe; these give the round-to-nearest-even results of the
+// standard (the bit patterns of a correctly rounded conversion) with 32/64-bit integer
+// instructions only.
+
+// Round-to-nearest-even of m * 2^-s for s in [1, 63]: the shifted value, possibly carrying
+// one bit past its width.
+__device__ __forceinline__ unsigned long long rne_shift(unsigned long long m, int s) {
+  const unsigned long long q = m >> s;
+  const unsigned long long rem = m & ((1ull << s) - 1ull);
+  const unsigned long long half = 1ull << (s - 1);
+  return q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+}
+
+// (float)q, correctly rounded.
+__device__ __forceinline__ float s64_to_f32_rn(long long q) {
+  if (q == 0) return 0.0f;
+  const uint32_t sign = q < 0 ? 0x80000000u : 0u;
+  const unsigned long long a = q < 0 ? 0ull - (unsigned long long)q : (unsigned long long)q;
+  int e = 63 - __clzll((long long)a);  // position of the leading bit
+  unsigned long long m;
+  if (e <= 23) {
+    m = a << (23 - e);
+  } else {
+    m = rne_shift(a, e - 23);
+    if (m == (1ull << 24)) {
+      m >>= 1;
+      ++e;
+    }
+  }
+  return __uint_as_float(sign | (uint32_t(e + 127) << 23) | (uint32_t(m) & 0x7FFFFFu));
+}
+
+// True when the double is neither infinite nor NaN.
+__device__ __forceinline__ bool f64_finite(double x) {
+  return ((__double2hiint(x) >> 20) & 0x7FF) != 0x7FF;
+}
+
+// (float)x, correctly rounded (overflow to infinity, underflow through the subnormals).
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t sign = uint32_t(b >> 32) & 0x80000000u;
+  const int e = int((b >> 52) & 0x7FF);
+  const unsigned long long frac = b & ((1ull << 52) - 1ull);
+  if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (frac ? 0x400000u : 0u));
+  if (e == 0) return __uint_as_float(sign);  // |x| < 2^-1022: below half the least float
+  const int E = e - 1023;
+  const unsigned long long m = frac | (1ull << 52);
+  if (E > 127) return __uint_as_float(sign | 0x7F800000u);
+  if (E >= -126) {
+    unsigned long long q = rne_shift(m, 29);
+    int ee = E;
+    if (q == (1ull << 24)) {
+      q >>= 1;
+      ++ee;
+    }
+    if (ee > 127) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | (uint32_t(ee + 127) << 23) | (uint32_t(q) & 0x7FFFFFu));
+  }
+  // Subnormal result: m * 2^(E-52) in units of 2^-149 is m * 2^(E+97).
+  const int s = -E - 97;  // >= 30
+  if (s > 53) return __uint_as_float(sign);  // below a quarter of the least subnormal
+  return __uint_as_float(sign | uint32_t(rne_shift(m, s)));  // a carry gives 2^-126 exactly
 }
 
 // round_half_even(x * 2^k) for a finite float x, exactly, with integer arithmetic only.

@@ -588,7 +588,11 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.objective = p->objective;
   a.ovr = t->ovr ? 1 : 0;
   a.mode = (options & MPSB_OPT_FLOAT_HIST) ? kModeFloat : kModeFixed;
-  a.scan_threads = 512;
+  // Four features (warps) per split-scan CTA spread a shallow level's few nodes over many
+  // SMs; MPSB_SCAN_THREADS overrides (a multiple of 32, at most 512).
+  a.scan_threads = 128;
+  if (const char* v = std::getenv("MPSB_SCAN_THREADS"))
+    a.scan_threads = uint32_t(std::min(512, std::max(32, std::atoi(v) / 32 * 32)));
   a.n_fchunks = (F + a.scan_threads / 32 - 1) / (a.scan_threads / 32);
   // rows per histogram work item: chosen per level on the device (about four items per
   // SM, within the 2^16-row limb bound)

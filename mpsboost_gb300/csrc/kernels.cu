@@ -122,15 +122,16 @@ __device__ __forceinline__ double logistic_probability(double m) {  // objective
 }
 
 // Objective gradient of one row (objective.cpp:290-429). Returns false on a reference
-// TrainingError condition.
+// TrainingError condition. Finiteness tests read the exponent bits (integer pipe); the
+// FP64 pipe does only the arithmetic the reference rounds.
 __device__ __forceinline__ bool objective_pair(uint32_t objective, double y, double p,
                                                const TreeParams& prm, double* g, double* h) {
-  if (!isfinite(y) || !isfinite(p)) return false;
+  if (!f64_finite(y) || !f64_finite(p)) return false;
   switch (objective) {
     case 0:
       *g = __dadd_rn(p, -y);
       *h = 1.0;
-      return isfinite(*g);
+      return f64_finite(*g);
     case 1: {
       if (y != 0.0 && y != 1.0) return false;
       const double prob = logistic_probability(p);
@@ -165,25 +166,37 @@ __device__ __forceinline__ bool objective_pair(uint32_t objective, double y, dou
   }
 }
 
+// True for a double with the sign bit set and a non-zero magnitude (x < 0).
+__device__ __forceinline__ bool f64_negative(double x) {
+  const long long b = __double_as_longlong(x);
+  return b < 0 && (b & 0x7FFFFFFFFFFFFFFFll) != 0;
+}
+
 // grid = (x, n_trees): blockIdx.y is the tree, so a block's maxima belong to one tree.
 __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
   __shared__ uint32_t sg[8], shh[8];
   const uint32_t t = blockIdx.y;
   const size_t tree_off = size_t(t) * a.n_rows;
+  // Squared error and quantile have h = 1, so h * w = w exactly.
+  const bool unit_h = a.objective == 0 || a.objective == 2;
+  const long long class_bits = __double_as_longlong(double(t));
   uint32_t mg = 0, mh = 0, bad = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_rows; i += gridDim.x * blockDim.x) {
     double y = a.labels[i];
-    if (a.ovr) y = (y == double(t)) ? 1.0 : 0.0;
+    if (a.ovr) {  // y == t (class ids are non-negative integers; -0.0 equals class 0)
+      const long long yb = __double_as_longlong(y);
+      y = (yb == class_bits || (t == 0 && (yb << 1) == 0)) ? 1.0 : 0.0;
+    }
     const double p = a.preds[tree_off + i];
     double g = 0.0, h = 0.0;
     if (!objective_pair(a.objective, y, p, a.params, &g, &h)) bad = 1;
     if (a.weights != nullptr) {
       const double w = a.weights_per_tree ? a.weights[tree_off + i] : a.weights[i];
       g = __dmul_rn(g, w);
-      h = __dmul_rn(h, w);
-      if (!isfinite(g) || !isfinite(h) || h < 0.0) bad = 1;
+      h = unit_h ? w : __dmul_rn(h, w);
+      if (!f64_finite(g) || !f64_finite(h) || f64_negative(h)) bad = 1;
     }
-    const float g32 = __double2float_rn(g), h32 = __double2float_rn(h);
+    const float g32 = f64_to_f32_rn(g), h32 = f64_to_f32_rn(h);
     if (!isfinite(g32) || !isfinite(h32)) bad = 1;
     a.gh[size_t(t) * 2 * a.n_rows + i] = make_float2(g32, h32);  // parity 0 = row order
     a.rows[size_t(t) * 2 * a.n_rows + i] = i;
@@ -414,7 +427,7 @@ __global__ void subtract_kernel(TrainerDev a) {
 template <bool FIXED>
 struct Stat {
   using V = typename std::conditional<FIXED, long long, double>::type;
-  unsigned long long count;
+  uint32_t count;  // a node holds fewer than 2^32 rows
   V g, h;
 };
 
@@ -545,13 +558,18 @@ __device__ __forceinline__ void consider(const TreeParams& p, const Stat<FIXED>&
 
 // One warp per (node, feature); a CTA covers one node and blockDim/32 features and
 // writes the best split of its features to partial[node][chunk].
+constexpr int kScanThreadsMax = 512;
+
 template <bool FIXED>
-__global__ void __launch_bounds__(512) split_scan_kernel(TrainerDev a, int parity) {
+__global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev a, int parity) {
   using V = typename Stat<FIXED>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SplitRec* warp_best = reinterpret_cast<SplitRec*>(smem_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
+  SplitRec* warp_best = reinterpret_cast<SplitRec*>(smem_raw);
+  // FP32 screen values of each lane's 16 candidates (8 thresholds x 2 missing directions),
+  // [warp][candidate][lane].
+  float* s_scores = reinterpret_cast<float*>(smem_raw + sizeof(SplitRec) * nwarps);
   const TreeParams& P = a.params;
   const uint32_t n_chunks = a.n_fchunks;
   const uint32_t items = a.ctl->n_nodes * n_chunks;
@@ -586,7 +604,8 @@ __global__ void __launch_bounds__(512) split_scan_kernel(TrainerDev a, int parit
       for (int k = 0; k < 8; ++k) {
         const int s = lane * 8 + k;
         Stat<FIXED> b;
-        b.count = base[s * 3 + 0];
+        const unsigned long long raw_count = base[s * 3 + 0];
+        b.count = uint32_t(raw_count);  // the total below checks the full word
         if constexpr (FIXED) {
           b.g = (long long)base[s * 3 + 1];
           b.h = (long long)base[s * 3 + 2];
@@ -595,7 +614,7 @@ __global__ void __launch_bounds__(512) split_scan_kernel(TrainerDev a, int parit
           b.h = __longlong_as_double((long long)base[s * 3 + 2]);
           if (!isfinite(b.g) || !isfinite(b.h) || b.h < 0.0) err |= kErrNonFinite;
         }
-        total_count += b.count;
+        total_count += raw_count;
         if (hm && s == kMissingSlot) {
           miss = b;
         } else {
@@ -633,39 +652,49 @@ __global__ void __launch_bounds__(512) split_scan_kernel(TrainerDev a, int parit
                 ? stable_random_threshold(P.random_seed, f, node.node_index, node.depth, nb - 1)
                 : 0xffffffffu;
         // Exact FP32 pre-screen. Every eligible candidate's score S = gL^2/(hL+lambda) +
-        // gR^2/(hR+lambda) is computed in FP32 with relative error <= 7u (u = 2^-24, the
-        // conversions of g, h and lambda included). A candidate whose FP32 score is below
-        // M(1 - 2^-20), M the warp's best FP32 score over certainly eligible candidates, then
-        // has an exact score at least 2u*M below that candidate's, far outside the FP64
-        // evaluation's own rounding (a few 2^-53 * M, the parent score included), so its FP64
-        // gain is strictly lower and it cannot win. Only the rest -- and candidates whose
-        // min_child_weight test or score is too close to call in FP32 -- run the FP64
-        // evaluation of the reference. The score is quadratic only without reg_alpha, the
-        // admissible set monotone in it only without monotone constraints, and random
-        // thresholds leave one candidate: the screen is off for those, and where 2^-k leaves
-        // the FP32 normal range.
+        // gR^2/(hR+lambda) is computed in FP32 with relative error <= 13u (u = 2^-24; each
+        // int64 -> FP32 conversion below is within 3u, lambda is rounded once). A candidate
+        // whose FP32 score is below M(1 - 2^-18), M the warp's best FP32 score over certainly
+        // eligible candidates, then has an exact score at least 30u*M below that candidate's,
+        // far outside the FP64 evaluation's own rounding (a few 2^-53 * M, the parent score
+        // included), so its FP64 gain is strictly lower and it cannot win. Only the rest --
+        // and candidates whose min_child_weight test or score is too close to call in FP32
+        // -- run the FP64 evaluation of the reference. The score is quadratic only without
+        // reg_alpha, the admissible set monotone in it only without monotone constraints,
+        // and random thresholds leave one candidate: the screen is off for those, and where
+        // 2^-k leaves the FP32 normal range.
         const bool screen = P.split_strategy == 0 && mono == 0 && P.reg_alpha == 0.0 &&
                             P.reg_lambda > 0.0 &&
                             (!FIXED || (st_kg >= -120 && st_kg <= 120 && st_kh >= -120 && st_kh <= 120));
         const float lam32 = float(P.reg_lambda), mcw32 = float(P.min_child_weight);
+        const bool mcw_on = P.min_child_weight > 0.0;
         // 2^-k exactly, built from the exponent field.
         const float inv_g32 = FIXED && screen ? __int_as_float((127 - st_kg) << 23) : 1.0f;
         const float inv_h32 = FIXED && screen ? __int_as_float((127 - st_kh) << 23) : 1.0f;
+        // |v| as hi * 2^32 + lo: float(hi) and float(lo) are each within u, and the fused
+        // multiply-add rounds once more, so the result is within 3u of v (no cancellation:
+        // both parts are non-negative). 32-bit conversions stay off the FP64 pipe.
         auto to32 = [&](V v, float inv32) -> float {
-          if constexpr (FIXED) return __ll2float_rn(v) * inv32;
-          else return __double2float_rn(v);
+          if constexpr (FIXED) {
+            const unsigned long long m = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+            const float f = __fmaf_rn(__uint2float_rn(uint32_t(m >> 32)), 4294967296.0f,
+                                      __uint2float_rn(uint32_t(m)));
+            return (v < 0 ? -f : f) * inv32;
+          } else {
+            return f64_to_f32_rn(v);
+          }
         };
         // 0: rejected by the FP64 test before any arithmetic (no error flag either);
         // 1: admissible, FP32 score in *s32; 2: too close to call.
         auto classify = [&](const Stat<FIXED>& cl, const Stat<FIXED>& cr, float* s32) -> int {
           if (cl.count < P.min_samples_leaf || cr.count < P.min_samples_leaf) return 0;
           if constexpr (!FIXED) {
-            if (!isfinite(cl.h) || !isfinite(cr.h) || !isfinite(cl.g) || !isfinite(cr.g)) return 2;
+            if (!f64_finite(cl.h) || !f64_finite(cr.h) || !f64_finite(cl.g) || !f64_finite(cr.g)) return 2;
           }
           if (!(cl.h > 0) || !(cr.h > 0)) return 0;  // fixed point: image > 0 iff q > 0
           const float lh = to32(cl.h, inv_h32), rh = to32(cr.h, inv_h32);
           int cls = 1;
-          if (P.min_child_weight > 0.0) {
+          if (mcw_on) {
             const float lo = mcw32 * (1.0f - 3e-6f), hi = mcw32 * (1.0f + 3e-6f);
             if (lh < lo || rh < lo) return 0;
             if (lh <= hi || rh <= hi) cls = 2;
@@ -680,14 +709,14 @@ __global__ void __launch_bounds__(512) split_scan_kernel(TrainerDev a, int parit
         const Stat<FIXED> carry_in = left;
         for (int pass = screen ? 0 : 1; pass < 2; ++pass) {
           left = carry_in;
-          const float cut = best32 >= 1e-30f ? best32 * (1.0f - 0x1p-20f) : -1.0f;
+          const float cut = best32 >= 1e-30f ? best32 * (1.0f - 0x1p-18f) : -1.0f;
 #pragma unroll 1
           for (int k = 0; k < 8; ++k) {
             const int s = lane * 8 + k;
             bool empty_bin = false;
             if (!(hm && s == kMissingSlot)) {  // reload the slot (L1-resident)
               Stat<FIXED> b;
-              b.count = base[s * 3 + 0];
+              b.count = uint32_t(base[s * 3 + 0]);
               empty_bin = b.count == 0;
               if constexpr (FIXED) {
                 b.g = (long long)base[s * 3 + 1];
@@ -715,15 +744,15 @@ __global__ void __launch_bounds__(512) split_scan_kernel(TrainerDev a, int parit
               if (dl == 0 && miss.count == 0) break;
               const Stat<FIXED> cl = dl ? stat_add<FIXED>(left, miss) : left;
               const Stat<FIXED> cr = dl ? right : stat_add<FIXED>(right, miss);
+              float& slot_score = s_scores[(warp * 16 + k * 2 + d) * 32 + lane];
               if (pass == 0) {
-                float sc;
-                if (classify(cl, cr, &sc) == 1) best32 = fmaxf(best32, sc);
+                // The screen value: -inf rejects, +inf always evaluates.
+                float sc = 0.0f;
+                const int cls = classify(cl, cr, &sc);
+                if (cls == 1) best32 = fmaxf(best32, sc);
+                slot_score = cls == 0 ? -INFINITY : (cls == 2 ? INFINITY : sc);
               } else {
-                if (screen && cut > 0.0f) {
-                  float sc;
-                  const int cls = classify(cl, cr, &sc);
-                  if (cls == 0 || (cls == 1 && sc < cut)) continue;
-                }
+                if (screen && cut > 0.0f && slot_score < cut) continue;
                 consider<FIXED>(P, cl, cr, inv_g, inv_h, mono, node.lo, node.hi, f, t, dl, best, err);
               }
             }
@@ -816,7 +845,56 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
   for (uint32_t t = threadIdx.x; t < a.n_trees; t += blockDim.x) tree_acc[t] = 0;
   __syncthreads();
 
-  // Phase A: best split per node, valid flags, valid prefix; rows the next level builds.
+  // Phase A0: one warp per node merges the best splits of the node's feature chunks into
+  // chunk 0's record (lanes read chunks in parallel; the features of different chunks
+  // differ, so the total order of better_split has a unique winner among valid records).
+  if (depth < P.max_depth) {  // nodes at max_depth never split (tree.cpp:152-154)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t nfc = a.n_fchunks;
+    for (uint32_t i = warp; i < n; i += nw) {
+      SplitRec* rec = a.partial + size_t(i) * nfc;
+      uint32_t mine = lane < int(nfc) ? uint32_t(lane) : 0u;
+      for (uint32_t c = lane + 32; c < nfc; c += 32)
+        if (better_split(rec[c], rec[mine])) mine = c;
+      uint32_t v = rec[mine].valid, f = rec[mine].feature, thr = rec[mine].threshold;
+      uint32_t dl = rec[mine].default_left;
+      double g = rec[mine].gain;
+      for (int off = 16; off > 0; off >>= 1) {
+        const uint32_t ov = __shfl_xor_sync(0xffffffffu, v, off);
+        const double og = __shfl_xor_sync(0xffffffffu, g, off);
+        const uint32_t of = __shfl_xor_sync(0xffffffffu, f, off);
+        const uint32_t ot = __shfl_xor_sync(0xffffffffu, thr, off);
+        const uint32_t od = __shfl_xor_sync(0xffffffffu, dl, off);
+        const uint32_t om = __shfl_xor_sync(0xffffffffu, mine, off);
+        bool take;
+        if (ov != v) take = ov > v;
+        else if (!v) take = om < mine;  // all invalid: keep chunk 0's record
+        else if (og != g) take = og > g;
+        else if (of != f) take = of < f;
+        else if (ot != thr) take = ot < thr;
+        else if (od != dl) take = od > dl;
+        else take = om < mine;
+        if (take) {
+          v = ov;
+          g = og;
+          f = of;
+          thr = ot;
+          dl = od;
+          mine = om;
+        }
+      }
+      if (mine != 0) {  // copy the winner's record into chunk 0, word by word
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(rec + mine);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(rec);
+        const unsigned long long w = lane < int(sizeof(SplitRec) / 8) ? src[lane] : 0ull;
+        __syncwarp();
+        if (lane < int(sizeof(SplitRec) / 8)) dst[lane] = w;
+      }
+    }
+  }
+  __syncthreads();
+
+  // Phase A: valid flags, valid prefix; rows the next level builds.
   uint32_t carry = 0, built_units = 0;
   for (uint32_t base = 0; base < n; base += blockDim.x) {
     const uint32_t i = base + threadIdx.x;
@@ -824,13 +902,8 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
     uint32_t tree = 0;
     bool first = false;
     if (i < n) {
-      if (depth < P.max_depth) {  // nodes at max_depth never split (tree.cpp:152-154)
-        SplitRec b = a.partial[size_t(i) * a.n_fchunks];
-        for (uint32_t c = 1; c < a.n_fchunks; ++c) {
-          const SplitRec x = a.partial[size_t(i) * a.n_fchunks + c];
-          if (better_split(x, b)) b = x;
-        }
-        a.partial[size_t(i) * a.n_fchunks] = b;
+      if (depth < P.max_depth) {
+        const SplitRec& b = a.partial[size_t(i) * a.n_fchunks];
         v[0] = b.valid;
         if (b.valid) v[1] = uint32_t(((b.lcount <= b.rcount ? b.lcount : b.rcount) + 255) / 256);
       }
@@ -1259,18 +1332,21 @@ __global__ void apply_leaves_kernel(TrainerDev a) {
     const uint32_t count = min(kApplyChunk, ls.seg_cnt - start);
     const uint32_t* rows = a.rows + (size_t(ls.tree) * 2 + ls.parity) * a.n_rows + ls.seg_off + start;
     double* pred = a.preds + size_t(ls.tree) * a.n_rows;
+    // lr * leaf is the same product for every row of a leaf.
+    const double step = __dmul_rn(lr, ls.value);
+    const double step_l = ls.split ? __dmul_rn(lr, ls.left_value) : step;
+    const double step_r = ls.split ? __dmul_rn(lr, ls.right_value) : step;
     for (uint32_t p = threadIdx.x; p < count; p += blockDim.x) {
       const uint32_t r = rows[p];
       if (r >= a.n_rows) {
         err = kErrCapacity;
         continue;
       }
-      double v = ls.value;
+      double v = step;
       if (ls.split)
-        v = row_goes_left(a, r, ls.feature, ls.threshold, ls.default_left) ? ls.left_value
-                                                                           : ls.right_value;
-      const double out = __dadd_rn(pred[r], __dmul_rn(lr, v));
-      if (!isfinite(out)) err = kErrNonFinite;
+        v = row_goes_left(a, r, ls.feature, ls.threshold, ls.default_left) ? step_l : step_r;
+      const double out = __dadd_rn(pred[r], v);
+      if (!f64_finite(out)) err = kErrNonFinite;
       pred[r] = out;
     }
   }
@@ -1426,7 +1502,8 @@ cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t s) {
 }
 cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStream_t s) {
   const int threads = int(a.scan_threads);
-  const size_t smem = sizeof(SplitRec) * (threads / 32);
+  if (threads < 32 || threads > kScanThreadsMax || threads % 32) return cudaErrorInvalidValue;
+  const size_t smem = (sizeof(SplitRec) + 16 * 32 * sizeof(float)) * (threads / 32);
   if (a.mode == kModeFixed) split_scan_kernel<true><<<grid, threads, smem, s>>>(a, parity);
   else split_scan_kernel<false><<<grid, threads, smem, s>>>(a, parity);
   return cudaGetLastError();

@@ -182,3 +182,20 @@ def test_node_entry_errors(backend):
     wide = mb.quantize_dense(np.linspace(0, 1, 1000, dtype=np.float32)[:, None], 300)
     with pytest.raises(mb.UnsupportedError, match="256"):
         backend.dataset(wide)
+
+
+def test_integer_pipe_conversions_match_hardware(tmp_path):
+    """The integer-pipe int64->float and double->float conversions used by the gradient
+    and split-scan kernels equal the hardware's correctly rounded conversions bit for bit
+    (2^26 seeded inputs per family, ties, overflow and subnormal edges)."""
+    import os
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = tmp_path / "conversions_check"
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    "-I", os.path.join(root, "mpsboost_gb300", "csrc"), "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "native", "conversions_check.cu"), "-o", str(exe)],
+                   check=True)
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, run.stdout + run.stderr

@@ -75,14 +75,12 @@ constexpr int kRowBytes = 32 + 8;
 
 template <int MODE, int THREADS, int NSTAGE>
 __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
-  constexpr int TILE = THREADS;
   constexpr int WARPS = THREADS / 32;
-  constexpr int RPW = TILE / WARPS;  // rows per warp per tile (32)
   constexpr int CELLS = kSlots * kBlockFeatures;
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned char* hist_smem = smem;
-  uint8_t* stage_bins = smem + HistSmem<MODE>::kBytes;               // [NSTAGE][TILE][32]
-  uint2* stage_val = reinterpret_cast<uint2*>(stage_bins + size_t(NSTAGE) * TILE * 32);  // [NSTAGE][TILE]
+  uint8_t* stage_bins = smem + HistSmem<MODE>::kBytes;  // [WARPS][NSTAGE][32 rows][32]
+  uint2* stage_val = reinterpret_cast<uint2*>(stage_bins + size_t(NSTAGE) * THREADS * 32);  // [WARPS][NSTAGE][32]
 
   __shared__ uint32_t s_item, s_entry;
 
@@ -134,8 +132,17 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
     }
     __syncthreads();
 
-    const int ntiles = int((row_count + TILE - 1) / TILE);
+    // Each warp runs its own two-stage pipeline over 32-row tiles (tiles warp, warp +
+    // WARPS, ...): lane l stages row l of a tile (cp.async of its 32-byte bin block, the
+    // quantized values by a shared store) while the warp reduces the previous tile. Only
+    // __syncwarp orders a warp's stages, so warps drift freely and keep the shared-memory
+    // reduction pipe busy; the CTA meets only at item boundaries.
+    const uint32_t ntiles = (row_count + 31u) / 32u;
+    const uint32_t my_tiles = uint32_t(warp) < ntiles ? (ntiles - uint32_t(warp) + WARPS - 1) / WARPS : 0u;
+    uint8_t* wbins = stage_bins + size_t(warp) * NSTAGE * 32 * 32;        // [NSTAGE][32][32]
+    uint2* wval = stage_val + size_t(warp) * NSTAGE * 32;                  // [NSTAGE][32]
     // Register pipeline: row ids two tiles ahead, g/h one tile ahead.
+    auto pos_of = [&](uint32_t k) -> uint32_t { return (uint32_t(warp) + k * WARPS) * 32u + uint32_t(lane); };
     auto row_at = [&](uint32_t pos) -> uint32_t {
       if (pos >= row_count) return 0u;
       const uint32_t r = __ldg(rows + pos);
@@ -145,23 +152,48 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
       if (pos >= row_count) return make_float2(0.f, 0.f);
       return gh_seg ? __ldg(gh_seg + pos) : __ldg(gh_row + r);
     };
-    uint32_t r_cur = row_at(uint32_t(tid));
-    uint32_t r_nxt = row_at(uint32_t(TILE + tid));
-    float2 g_cur = gh_at(uint32_t(tid), r_cur);
-    for (int t = 0; t < ntiles + NSTAGE - 1; ++t) {
-      if (t < ntiles) {
-        const int s = t % NSTAGE;
-        const uint32_t pos = uint32_t(t) * TILE + tid;
+    uint32_t r_cur = my_tiles > 0 ? row_at(pos_of(0)) : 0u;
+    uint32_t r_nxt = my_tiles > 1 ? row_at(pos_of(1)) : 0u;
+    float2 g_cur = my_tiles > 0 ? gh_at(pos_of(0), r_cur) : make_float2(0.f, 0.f);
+    const uint32_t quad_byte = uint32_t(lane & 7) * 4u;
+    const uint32_t rot = uint32_t(lane >> 3);
+    // A warp takes a tile's rows four at a time: lane l reads the 4-byte word (l & 7) of
+    // row l >> 3 (four features' bins) and that row's values, so one 128-byte wavefront
+    // brings the bins of four rows and one more their values. In the i-th reduction round
+    // lane l updates byte (i + (l >> 3)) & 3 of its word: across the warp the 32 features
+    // are distinct, so the 32 words fall in 32 different banks.
+    auto accumulate = [&](uint32_t f, uint32_t b, uint2 q) {
+      const uint32_t addr = hist_base + (b * kBlockFeatures + f) * 4u;
+      if constexpr (MODE == kModeFixed) {
+        red_shared_u32<0>(addr, 1u);
+        red_shared_u32<1u * CELLS * 4u>(addr, q.x & 0xFFFFu);
+        red_shared_u32<2u * CELLS * 4u>(addr, uint32_t(int32_t(int16_t(q.y & 0xFFFFu))));
+        red_shared_u32<3u * CELLS * 4u>(addr, q.x >> 16);
+        red_shared_u32<4u * CELLS * 4u>(addr, q.y >> 16);
+      } else if constexpr (MODE == kModeFixedG) {
+        red_shared_u32<0>(addr, q.x & 0xFFFFu);
+        red_shared_u32<1u * CELLS * 4u>(addr, uint32_t(int32_t(q.x) >> 16));
+      } else {
+        red_shared_u32<0>(addr, 1u);
+        red_shared_f32<CELLS * 4u>(addr, __uint_as_float(q.x));
+        red_shared_f32<2u * CELLS * 4u>(addr, __uint_as_float(q.y));
+      }
+    };
+    for (uint32_t k = 0; k < my_tiles + 1; ++k) {
+      if (k < my_tiles) {
+        const int st = int(k % NSTAGE);
+        const uint32_t pos = pos_of(k);
         const uint32_t r = r_cur;
         const float2 p = g_cur;
-        const uint32_t r_far = row_at(pos + 2u * TILE);
-        g_cur = gh_at(pos + TILE, r_nxt);
+        const uint32_t r_far = k + 2 < my_tiles ? row_at(pos_of(k + 2)) : 0u;
+        g_cur = k + 1 < my_tiles ? gh_at(pos_of(k + 1), r_nxt) : make_float2(0.f, 0.f);
         r_cur = r_nxt;
         r_nxt = r_far;
         if (pos < row_count) {
           const uint8_t* src = bins + size_t(r) * a.bins_row_stride;
-          cp_async16(stage_bins + (size_t(s) * TILE + tid) * 32, src);
-          cp_async16(stage_bins + (size_t(s) * TILE + tid) * 32 + 16, src + 16);
+          uint8_t* dst = wbins + (size_t(st) * 32 + lane) * 32;
+          cp_async16(dst, src);
+          cp_async16(dst + 16, src + 16);
           uint2 v;
           if constexpr (MODE == kModeFixed) {
             // |q| <= 2^30: low limb = q & 0xFFFF (unsigned), high limb = q >> 16 (signed,
@@ -178,54 +210,24 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
           } else {
             v = make_uint2(__float_as_uint(p.x), __float_as_uint(p.y));
           }
-          stage_val[s * TILE + tid] = v;
+          wval[st * 32 + lane] = v;
         }
       }
       cp_async_commit();
-      if (t >= NSTAGE - 1) {
-        cp_async_wait<NSTAGE - 1>();
-        __syncthreads();
-        const int ct = t - (NSTAGE - 1);
-        const int s = ct % NSTAGE;
-        const int tile_rows = min(TILE, int(row_count) - ct * TILE);
-        const uint8_t* sb = stage_bins + size_t(s) * TILE * 32;
-        const uint2* sv = stage_val + s * TILE;
-        const int row0 = warp * RPW;
-        const int nrows = max(0, min(RPW, tile_rows - row0));
-        // A warp takes its rows four at a time: lane l reads the 4-byte word (l & 7) of row
-        // l >> 3 (four features' bins) and that row's values, so one 128-byte wavefront
-        // brings the bins of four rows and one more their values. In the i-th reduction
-        // round lane l updates byte (i + (l >> 3)) & 3 of its word: across the warp the 32
-        // features are distinct, so the 32 words fall in 32 different banks.
-        const uint32_t quad_byte = uint32_t(lane & 7) * 4u;
-        const uint32_t rot = uint32_t(lane >> 3);
-        auto accumulate = [&](uint32_t f, uint32_t b, uint2 q) {
-          const uint32_t addr = hist_base + (b * kBlockFeatures + f) * 4u;
-          if constexpr (MODE == kModeFixed) {
-            red_shared_u32<0>(addr, 1u);
-            red_shared_u32<1u * CELLS * 4u>(addr, q.x & 0xFFFFu);
-            red_shared_u32<2u * CELLS * 4u>(addr, uint32_t(int32_t(int16_t(q.y & 0xFFFFu))));
-            red_shared_u32<3u * CELLS * 4u>(addr, q.x >> 16);
-            red_shared_u32<4u * CELLS * 4u>(addr, q.y >> 16);
-          } else if constexpr (MODE == kModeFixedG) {
-            red_shared_u32<0>(addr, q.x & 0xFFFFu);
-            red_shared_u32<1u * CELLS * 4u>(addr, uint32_t(int32_t(q.x) >> 16));
-          } else {
-            red_shared_u32<0>(addr, 1u);
-            red_shared_f32<CELLS * 4u>(addr, __uint_as_float(q.x));
-            red_shared_f32<2u * CELLS * 4u>(addr, __uint_as_float(q.y));
-          }
-        };
+      if (k >= 1) {
+        cp_async_wait<1>();
+        __syncwarp();
+        const uint32_t ct = k - 1;
+        const int st = int(ct % NSTAGE);
+        const uint32_t tile_pos = (uint32_t(warp) + ct * WARPS) * 32u;
+        const int nrows = int(min(32u, row_count - tile_pos));
+        const uint8_t* sb = wbins + size_t(st) * 32 * 32;
+        const uint2* sv = wval + st * 32;
         for (int j = 0; j < nrows; j += 4) {
           const int r = j + int(rot);
-          const bool ok = r < nrows;
-          uint32_t w = 0;
-          uint2 q = make_uint2(0u, 0u);
-          if (ok) {
-            w = *reinterpret_cast<const uint32_t*>(sb + (row0 + r) * 32 + quad_byte);
-            q = sv[row0 + r];
-          }
-          if (ok) {
+          if (r < nrows) {
+            const uint32_t w = *reinterpret_cast<const uint32_t*>(sb + r * 32 + quad_byte);
+            const uint2 q = sv[r];
 #pragma unroll
             for (uint32_t i = 0; i < 4; ++i) {
               const uint32_t sel = (i + rot) & 3u;
@@ -233,9 +235,11 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
             }
           }
         }
-        __syncthreads();
+        __syncwarp();
       }
     }
+    cp_async_wait<0>();
+    __syncthreads();
 
     // Flush non-empty cells into the node's slot.
     unsigned long long* dst_base =
@@ -303,7 +307,7 @@ cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int gr
   // Shared memory: 160 KB (fixed) / 64 KB (gradient only) / 96 KB (float) histogram +
   // stages x threads x 40 B.
   if (a.mode == kModeFixedG) {
-    if (cfg.threads == 1024) return launch_variant<kModeFixedG, 1024, 2>(a, grid, stream);
+    if (cfg.root_threads == 1024) return launch_variant<kModeFixedG, 1024, 2>(a, grid, stream);
     return launch_variant<kModeFixedG, 768, 2>(a, grid, stream);
   }
   if (a.mode == kModeFixed) {

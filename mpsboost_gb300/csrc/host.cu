@@ -601,7 +601,9 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   // rows per work item.
   if (const char* v = std::getenv("MPSB_HIST_THREADS")) t->hcfg.threads = std::atoi(v);
   if (const char* v = std::getenv("MPSB_HIST_STAGES")) t->hcfg.stages = std::atoi(v);
+  if (const char* v = std::getenv("MPSB_ROOT_THREADS")) t->hcfg.root_threads = std::atoi(v);
   if (const char* v = std::getenv("MPSB_BLOCKED_LEVELS")) t->blocked_levels = uint32_t(std::atoi(v));
+  if (const char* v = std::getenv("MPSB_ITEMS_PER_SM")) a.items_per_sm = uint32_t(std::max(1, std::atoi(v)));
   if (const char* v = std::getenv("MPSB_ITEM_ROWS"))
     a.item_rows = uint32_t(std::min<long>(std::max<long>(std::atol(v), 512), long(kItemRowsMax)));
   // Squared error and quantile have hessian = sample weight, the same in every round: the

@@ -34,10 +34,11 @@ __device__ __forceinline__ void raise(Control* ctl, uint32_t bits) { atomicOr(&c
 
 __device__ __forceinline__ uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
-// Rows per histogram work item for a level that builds `rows` rows: about four items per
-// SM, a multiple of 512, within [4096, kItemRowsMax].
-__device__ __forceinline__ uint32_t adaptive_item_rows(uint64_t rows, uint32_t nfb, uint32_t sms) {
-  const uint64_t target = uint64_t(sms ? sms : 152) * 4;
+// Rows per histogram work item for a level that builds `rows` rows: about per_sm (default
+// four) items per SM, a multiple of 512, within [4096, kItemRowsMax].
+__device__ __forceinline__ uint32_t adaptive_item_rows(uint64_t rows, uint32_t nfb, uint32_t sms,
+                                                      uint32_t per_sm) {
+  const uint64_t target = uint64_t(sms ? sms : 152) * (per_sm ? per_sm : 4);
   uint64_t per = (rows * nfb + target - 1) / target;
   per = (per + 511) / 512 * 512;
   if (per < 4096) per = 4096;
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
 
 __global__ void round_setup_kernel(TrainerDev a) {
   const uint32_t item_rows =
-      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(a.n_rows) * a.n_trees, a.nfb, a.sm_count);
+      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(a.n_rows) * a.n_trees, a.nfb, a.sm_count, a.items_per_sm);
   const uint32_t chunks_per_tree = ceil_div(a.n_rows, item_rows);
   for (uint32_t base = 0; base < a.n_trees; base += blockDim.x) {
     const uint32_t t = base + threadIdx.x;
@@ -924,7 +925,7 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
   }
   __syncthreads();
   const uint32_t item_rows =
-      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(built_units) * 256, a.nfb, a.sm_count);
+      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(built_units) * 256, a.nfb, a.sm_count, a.items_per_sm);
 
   // Phase B1: acceptance under max_leaves, accepted prefix, chunk prefixes.
   // Scanned values: 0 accepted, 1 build chunks, 2 partition chunks, 3 leaf segments,

@@ -62,6 +62,7 @@ struct TrainerDev {
   uint32_t item_rows;           // rows per histogram work item (<= kItemRowsMax); 0: the
                                 // level's adaptive value ctl->item_rows
   uint32_t sm_count;
+  uint32_t items_per_sm;        // histogram work items per SM of the adaptive item size (0: 4)
   uint32_t mode;                // kModeFixed / kModeFloat
   uint32_t ovr;                 // labels are class ids; tree t fits class t (logistic)
   uint32_t scan_threads;        // block size of the split scan (multiple of 32)
@@ -85,8 +86,9 @@ struct TrainerDev {
 };
 
 struct HistConfig {
-  int threads = 768;
+  int threads = 768;        // fixed and float builds
   int stages = 2;
+  int root_threads = 1024;  // gradient-only root builds (64 KB histogram)
 };
 
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,

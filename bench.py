@@ -38,6 +38,10 @@ SEED = 20260719 + 2
 PARAMS = dict(max_depth=DEPTH, learning_rate=LR, min_samples_leaf=20, min_child_weight=1.0,
               reg_lambda=1.0, max_bins=BINS)
 METRIC = "trees/s @10Mx128x255bins d8 (fixed-point batched)"
+# DRAM bytes per histogram launch on this workload: one ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum over the 24 histogram launches of three
+# steady-state rounds (610.6 MB read + 6.9 MB written per launch on average).
+HIST_TRAFFIC_BYTES_PER_LAUNCH = 617.5e6
 CONFIG = {
     "workload": "regression 10,000,000 rows x 128 features (64 normal, 32 lognormal, 32 int[0,1000)), "
                 "255 bins, depth 8, lr 0.05, weighted squared error",
@@ -271,7 +275,8 @@ def run_ours(args, rank, world):
         "gpu_launches": int(st["kernel_launches"]),
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "frac": achieved / peak, "traffic": HIST_TRAFFIC_BYTES_PER_LAUNCH,
+                     "traffic_unit": "bytes per launch (ncu)", "peak_kind": peak_kind,
                      "kernel": "hist_build_kernel<fixed>",
                      "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
                      "cells_per_s": ts["hist_cells"] / (ts["hist_ms"] / 1e3), "levels": levels},

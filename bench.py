@@ -331,6 +331,44 @@ def run_e2e(mb, backend, binned, y, w, trees):
             "note": "one fit of K trees: dataset upload, training, model readback"}
 
 
+def run_forest(args, rank, world):
+    """Random-forest regression: 1,000,000 rows x 100 N(0,1) features, Friedman-1 target on
+    x0..x4 + N(0,1); 256 trees, per-tree Poisson(1) row weights, 10 = sqrt(100) features per
+    tree, depth 12, min_samples_leaf 20; every tree of a batch built in the same launches.
+    A step is one forest of ``--forest-trees`` trees."""
+    import mpsboost_gb300 as mb
+
+    n, f, trees = 1_000_000, 100, args.forest_trees
+    rng = np.random.default_rng(20260719 + 5)
+    x = rng.standard_normal((n, f), dtype=np.float32)
+    u = (x[:, :5] - x[:, :5].min(0)) / (x[:, :5].max(0) - x[:, :5].min(0))  # to [0, 1]
+    y = (10 * np.sin(np.pi * u[:, 0] * u[:, 1]) + 20 * (u[:, 2] - 0.5) ** 2 + 10 * u[:, 3] + 5 * u[:, 4]
+         + rng.normal(size=n))
+    counts = rng.poisson(1.0, size=(trees, n)).astype(np.uint8)
+    subsets = [rng.choice(f, size=10, replace=False) for _ in range(trees)]
+    binned = mb.quantize_dense(x, 255)
+    backend = mb.CudaBackend(int(os.environ.get("LOCAL_RANK", "0")))
+    params = dict(max_depth=12, min_samples_leaf=20, max_bins=255)
+    for _ in range(args.warmup):
+        mb.train_forest(backend, binned, y, row_counts=counts[: min(trees, 16)],
+                        feature_subsets=subsets[: min(trees, 16)], **params)
+    times, nodes = [], 0
+    for _ in range(args.steps):
+        barrier(world)
+        t0 = time.perf_counter()
+        models = mb.train_forest(backend, binned, y, row_counts=counts, feature_subsets=subsets, **params)
+        times.append(time.perf_counter() - t0)
+        nodes = sum(len(m.trees[0]) for m in models)
+    dt = reduce_max(statistics.median(times), world)
+    if rank == 0:
+        print(json.dumps({"metric": "forest trees/s @1Mx100 d12 sqrt-features Poisson(1)",
+                          "value": world * trees / dt, "unit": "trees/s", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "seconds_per_forest": dt,
+                          "trees": trees, "nodes": nodes, "dtype": "int64", "data": "synthetic",
+                          "note": "host-timed fit of the whole forest (sample expansion, upload, "
+                                  "training, model readback), binned data resident"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -342,6 +380,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--rows", type=int, default=ROWS,
                     help="rows of the synthetic workload (profiling runs use fewer)")
+    ap.add_argument("--workload", choices=["regression", "forest"], default="regression",
+                    help="forest: the 256-tree random-forest configuration instead of the default")
+    ap.add_argument("--forest-trees", type=int, default=256)
     ap.add_argument("--only-train", action="store_true",
                     help="time the training rounds only (for launch lists and ncu captures)")
     args = ap.parse_args()
@@ -350,6 +391,8 @@ def main():
     rank, world = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "forest":
+        run_forest(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:

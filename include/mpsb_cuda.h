@@ -34,6 +34,10 @@
  *                                      (src/python/binding_model.cpp:34-45)
  *   mpsb_cuda_train_ovr                the one-vs-rest fit of
  *                                      src/mpsboost/estimators/multiclass.py:113-160
+ *   mpsb_cuda_train_forest             the per-tree fits of _ForestMixin.fit
+ *                                      (src/mpsboost/estimators/forest.py:101-183,
+ *                                      forest_sampling.py:42-63): one single-round tree
+ *                                      per row sample and feature subset
  *   mpsb_cuda_model_create             RegressionModel::Restore (trainer.hpp:271-279)
  *   mpsb_cuda_model_predict            RegressionModel::Predict (trainer.hpp:266-269)
  *   mpsb_cuda_trainer_*                the same training loop as a session with
@@ -271,6 +275,23 @@ int mpsb_cuda_train_ovr(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dat
                         const double* labels, const double* weights, uint64_t n,
                         uint32_t n_classes, const mpsb_train_params* params,
                         uint32_t options, mpsb_cuda_model** out);
+/* n_trees independent single-round trees (a random forest / extra-trees ensemble), the
+   frontier of every tree of a batch built in the same launches. Tree t trains on the
+   multiset of rows given by row_counts[t * n + r] (how many times row r is drawn: 0 for
+   rows outside the bootstrap sample) and on the features
+   features[feature_offsets[t] .. feature_offsets[t + 1]); the result equals the
+   reference's fit on matrix[rows][:, sorted(features)] with this dataset's bins (ties
+   between features resolve by feature index). seeds[t] (or params->random_seed when
+   seeds is NULL) seeds random thresholds; a feature's rank in the tree's ascending
+   subset enters the threshold hash. params->n_estimators is ignored; interaction
+   constraints are unsupported. out receives n_trees models of one tree each, without
+   training predictions. */
+int mpsb_cuda_train_forest(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                           const double* labels, const double* weights, uint64_t n,
+                           const mpsb_train_params* params, uint32_t n_trees,
+                           const uint8_t* row_counts, const uint32_t* feature_offsets,
+                           const uint32_t* features, const uint32_t* seeds, uint32_t options,
+                           mpsb_cuda_model** out);
 /* A model from host trees (e.g. one loaded from a file): base_score + learning_rate *
    sum of trees, node_counts[n_trees], nodes concatenated tree by tree. */
 int mpsb_cuda_model_create(double base_score, double learning_rate, uint32_t n_trees,

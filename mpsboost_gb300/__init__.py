@@ -14,8 +14,10 @@ from .backend import (
     CudaBackend,
     RegressionModel,
     Trainer,
+    forest_samples,
     make_params,
     quantize_dense,
+    train_forest,
     train_ovr,
     train_regressor,
 )
@@ -29,6 +31,8 @@ __all__ = [
     "RegressionModel",
     "Trainer",
     "TrainingError",
+    "forest_samples",
+    "train_forest",
     "UnsupportedError",
     "make_params",
     "quantize_dense",

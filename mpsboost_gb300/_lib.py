@@ -141,6 +141,8 @@ SIGNATURES = {
     "mpsb_cuda_build_histogram_noalloc": (_I32, [_VP, _U32, _U32, _VP, _U32, _VP, _VP, _VP]),
     "mpsb_cuda_train_regressor": (_I32, [_VP, _VP, _VP, _VP, _U64, C.POINTER(TrainParams), _U32, C.POINTER(_VP)]),
     "mpsb_cuda_train_ovr": (_I32, [_VP, _VP, _VP, _VP, _U64, _U32, C.POINTER(TrainParams), _U32, _VP]),
+    "mpsb_cuda_train_forest": (_I32, [_VP, _VP, _VP, _VP, _U64, C.POINTER(TrainParams), _U32, _VP, _VP,
+                                      _VP, _VP, _U32, _VP]),
     "mpsb_cuda_model_create": (_I32, [_F64, _F64, _U32, _VP, _VP, C.POINTER(_VP)]),
     "mpsb_cuda_model_tree_count": (_U32, [_VP]),
     "mpsb_cuda_model_base_score": (_F64, [_VP]),

@@ -482,6 +482,75 @@ def train_ovr(backend: CudaBackend, dataset: BinnedDataset, labels, n_classes: i
     return _train(backend, dataset, labels, weights, options, int(n_classes), **params)
 
 
+def forest_samples(n_rows: int, n_features: int, n_trees: int, *, random_state=None,
+                   bootstrap: bool = True, sample_fraction: float = 1.0,
+                   max_features: float = 1.0):
+    """Per-tree row multiplicities, feature subsets and seeds drawn as the reference's
+    forest draws them (forest.py:120-127, forest_sampling.py:94-116, randomization.py:43-84):
+    a generator seeded with random_state gives each tree a row seed and a feature seed;
+    rows are ceil(n * sample_fraction) draws with replacement (bootstrap) or without, the
+    features ceil(F * max_features) distinct draws; the feature seed also seeds the tree's
+    random thresholds. Returns (row_counts uint8 [n_trees, n_rows], subsets, seeds)."""
+
+    from math import ceil
+
+    gen = np.random.default_rng(random_state)
+    jobs = [(int(gen.integers(0, np.iinfo(np.int32).max)), int(gen.integers(0, np.iinfo(np.int32).max)))
+            for _ in range(n_trees)]
+    counts = np.zeros((n_trees, n_rows), np.uint8)
+    subsets, seeds = [], []
+    n_draw = max(1, int(ceil(n_rows * float(sample_fraction))))
+    n_feat = max(1, int(ceil(n_features * float(max_features))))
+    for t, (row_seed, feature_seed) in enumerate(jobs):
+        if bootstrap:
+            rows = np.random.default_rng(row_seed).integers(0, n_rows, size=n_draw, dtype=np.int64)
+        else:
+            rows = np.random.default_rng(row_seed).choice(n_rows, size=n_draw, replace=False)
+        c = np.bincount(rows, minlength=n_rows)
+        if c.max() > 255:
+            raise ValueError("a row is drawn more than 255 times")
+        counts[t] = c.astype(np.uint8)
+        subsets.append(np.random.default_rng(feature_seed).choice(n_features, size=n_feat, replace=False))
+        seeds.append(feature_seed)
+    return counts, subsets, np.asarray(seeds, np.uint32)
+
+
+def train_forest(backend: CudaBackend, dataset: BinnedDataset, labels, weights=None, *,
+                 row_counts, feature_subsets, seeds=None, hist_mode: str = "fixed",
+                 **params) -> list[RegressionModel]:
+    """Independent single-round trees, one per (row multiset, feature subset), every tree's
+    frontier of a batch built in the same launches (the fits of _ForestMixin.fit,
+    forest.py:101-183). Returns one single-tree model per tree; a forest predicts the mean
+    of their predictions."""
+
+    dev = backend.dataset(dataset)
+    y = np.ascontiguousarray(labels, dtype=np.float64)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    counts = np.ascontiguousarray(row_counts, dtype=np.uint8)
+    n_trees = counts.shape[0]
+    if counts.shape != (n_trees, y.size) or len(feature_subsets) != n_trees:
+        raise ValueError("row_counts must be [n_trees, n_rows] with one feature subset per tree")
+    offsets = np.zeros(n_trees + 1, np.uint32)
+    offsets[1:] = np.cumsum([len(f) for f in feature_subsets])
+    feats = np.ascontiguousarray(np.concatenate([np.asarray(f, np.uint32) for f in feature_subsets]))
+    sd = None if seeds is None else np.ascontiguousarray(seeds, dtype=np.uint32)
+    params.setdefault("max_bins", dataset.max_bins)
+    params.setdefault("learning_rate", 1.0)
+    params["n_estimators"] = 1
+    p, keep = make_params(**params)
+    lib = _lib.load()
+    handles = (C.c_void_p * n_trees)()
+    check(lib.mpsb_cuda_train_forest(backend.handle, dev.handle, ptr(y), ptr(w), y.size, C.byref(p),
+                                     n_trees, ptr(counts), ptr(offsets), ptr(feats), ptr(sd),
+                                     _options(hist_mode, True, False), handles))
+    del keep
+    models = []
+    for h in list(handles):
+        models.append(RegressionModel._from_handle(h))
+        lib.mpsb_cuda_model_destroy(h)
+    return models
+
+
 def _options(hist_mode: str, batched: bool, graph: bool) -> int:
     opts = 0
     if hist_mode == "float":

@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
     const uint32_t item_rows = a.item_rows ? a.item_rows : a.ctl->item_rows;
     const uint32_t row_begin = (chunk - a.build_prefix[s_entry]) * item_rows;
     const uint32_t row_count = row_begin < e.seg_cnt ? min(item_rows, e.seg_cnt - row_begin) : 0u;
-    const size_t seg = (size_t(e.tree) * 2 + e.parity) * n + e.seg_off + row_begin;
+    const size_t seg = (size_t(e.tree) * 2 + e.parity) * a.seg_stride + e.seg_off + row_begin;
     const uint32_t* rows = a.rows + seg;
     // g/h in segment order (contiguous) or by row id (gathered).
     const float2* gh_seg = a.gh_ordered ? a.gh + seg : nullptr;
@@ -133,8 +133,9 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
     __syncthreads();
 
     // Each warp runs its own two-stage pipeline over 32-row tiles (tiles warp, warp +
-    // WARPS, ...): lane l stages row l of a tile (cp.async of its 32-byte bin block, the
-    // quantized values by a shared store) while the warp reduces the previous tile. Only
+    // WARPS, ...): lane l stages row l's quantized values by a shared store, and lanes 2j,
+    // 2j+1 copy the two 16-byte halves of a row's 32-byte bin block with cp.async, while
+    // the warp reduces the previous tile. Only
     // __syncwarp orders a warp's stages, so warps drift freely and keep the shared-memory
     // reduction pipe busy; the CTA meets only at item boundaries.
     const uint32_t ntiles = (row_count + 31u) / 32u;
@@ -189,11 +190,18 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
         g_cur = k + 1 < my_tiles ? gh_at(pos_of(k + 1), r_nxt) : make_float2(0.f, 0.f);
         r_cur = r_nxt;
         r_nxt = r_far;
+        // Two lanes per row: each copy instruction touches 16 rows' lines instead of 32.
+        const uint32_t valid = min(32u, row_count - (uint32_t(warp) + k * WARPS) * 32u);
+#pragma unroll
+        for (uint32_t i = 0; i < 2; ++i) {
+          const uint32_t row_in_tile = 16u * i + uint32_t(lane >> 1);
+          const uint32_t rr = __shfl_sync(0xffffffffu, r, int(row_in_tile));
+          const uint32_t half = uint32_t(lane & 1) * 16u;
+          if (row_in_tile < valid)
+            cp_async16(wbins + (size_t(st) * 32 + row_in_tile) * 32 + half,
+                       bins + size_t(rr) * a.bins_row_stride + half);
+        }
         if (pos < row_count) {
-          const uint8_t* src = bins + size_t(r) * a.bins_row_stride;
-          uint8_t* dst = wbins + (size_t(st) * 32 + lane) * 32;
-          cp_async16(dst, src);
-          cp_async16(dst + 16, src + 16);
           uint2 v;
           if constexpr (MODE == kModeFixed) {
             // |q| <= 2^30: low limb = q & 0xFFFF (unsigned), high limb = q >> 16 (signed,

@@ -399,7 +399,7 @@ struct mpsb_cuda_trainer {
     cudaStream_t s = b->stream;
     uint64_t k = 0;
     CK(launch_round_begin(dev, s)); ++k;
-    CK(launch_gradients(dev, std::max(1, std::min(grid(4), int((dev.n_rows + 255) / 256))), s)); ++k;
+    CK(launch_gradients(dev, std::max(1, std::min(grid(4), int((dev.seg_stride + 255) / 256))), s)); ++k;
     CK(launch_round_setup(dev, s)); ++k;
     const uint32_t levels = std::max<uint32_t>(depth, 1);
     for (uint32_t d = 0; d < levels; ++d) {
@@ -545,9 +545,23 @@ struct mpsb_cuda_trainer {
 
 namespace {
 
+// A batch of forest trees: per tree its sample (a multiset of rows, ascending), feature
+// subset (as a mask and ranks), random-threshold seed and base score.
+struct ForestSpec {
+  uint32_t n_trees = 0;
+  uint32_t cap = 0;                  // largest sample
+  std::vector<uint32_t> sample;      // [n_trees][cap]
+  std::vector<uint32_t> count;       // [n_trees]
+  std::vector<uint32_t> masks;       // [n_trees][path_words]
+  std::vector<uint32_t> ranks;       // [n_trees][features]
+  std::vector<uint32_t> seeds;       // [n_trees] or empty
+  std::vector<double> base_scores;   // [n_trees]
+};
+
 void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
                    const double* labels, const double* weights, uint64_t n,
-                   const mpsb_train_params* p, uint32_t options, uint32_t n_classes) {
+                   const mpsb_train_params* p, uint32_t options, uint32_t n_classes,
+                   const ForestSpec* forest = nullptr) {
   if (!b || !ds || !labels || !p) throw TrainingError("null argument");
   validate_training_params(*p);
   validate_tree_params(*p, ds->features);
@@ -560,7 +574,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   t->options = options;
   t->depth = p->max_depth;
   t->ovr = n_classes > 0;
-  t->n_trees = t->ovr ? n_classes : 1;
+  t->n_trees = forest ? forest->n_trees : (t->ovr ? n_classes : 1);
   if (t->ovr && p->objective != MPSB_BINARY_LOGISTIC)
     throw TrainingError("one-vs-rest training uses the binary_logistic objective");
   const uint32_t T = t->n_trees;
@@ -568,7 +582,8 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   const uint32_t D = p->max_depth;
   if (D > 24) throw UnsupportedError("max_depth above 24 is not supported by the CUDA backend");
   const uint64_t max_leaves_eff = effective_max_leaves(*p);
-  const uint64_t by_rows = std::max<uint64_t>(1, (n + p->min_samples_leaf - 1) / p->min_samples_leaf);
+  const uint64_t seg_rows = forest ? forest->cap : n;  // positions per tree
+  const uint64_t by_rows = std::max<uint64_t>(1, (seg_rows + p->min_samples_leaf - 1) / p->min_samples_leaf);
   const uint64_t leaves = std::min<uint64_t>({uint64_t(1) << std::min<uint32_t>(D, 30), max_leaves_eff, by_rows});
   const uint64_t level_nodes = std::max<uint64_t>(1, std::min<uint64_t>(D ? (uint64_t(1) << (D - 1)) : 1, leaves));
   const uint64_t tree_nodes = 2 * leaves + 1;
@@ -582,6 +597,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.sm_count = uint32_t(b->sm_count);
   a.has_missing = ds->has_missing.as<uint8_t>();
   a.n_rows = ds->n_rows;
+  a.seg_stride = uint32_t(seg_rows);
   a.features = F;
   a.nfb = ds->nfb;
   a.n_trees = T;
@@ -609,7 +625,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   // Squared error and quantile have hessian = sample weight, the same in every round: the
   // roots' count and hessian histograms are built once per fit (MPSB_ROOT_REUSE=0 builds
   // them every round).
-  t->root_reuse = a.mode == kModeFixed && !(options & MPSB_OPT_PER_NODE) &&
+  t->root_reuse = !forest && a.mode == kModeFixed && !(options & MPSB_OPT_PER_NODE) &&
                   (p->objective == MPSB_SQUARED_ERROR || p->objective == MPSB_QUANTILE);
   if (const char* v = std::getenv("MPSB_ROOT_REUSE")) t->root_reuse = t->root_reuse && std::atoi(v) != 0;
   if (t->root_reuse) {
@@ -651,7 +667,8 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   std::vector<double> init(static_cast<size_t>(n));
   a.preds = t->alloc<double>(size_t(T) * n);
   for (uint32_t k = 0; k < T; ++k) {
-    t->base_scores[k] = base_score(*p, labels, weights, n, t->ovr ? int64_t(k) : -1);
+    t->base_scores[k] = forest ? forest->base_scores[k]
+                               : base_score(*p, labels, weights, n, t->ovr ? int64_t(k) : -1);
     std::fill(init.begin(), init.end(), t->base_scores[k]);
     CK(cudaMemcpyAsync(a.preds + size_t(k) * n, init.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
@@ -673,10 +690,32 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     CK(cudaStreamSynchronize(s));
     a.group_masks = gm;
   }
+  if (forest) {
+    const size_t cells = size_t(T) * forest->cap;
+    uint32_t* d_sample = t->alloc<uint32_t>(cells);
+    CK(cudaMemcpyAsync(d_sample, forest->sample.data(), cells * 4, cudaMemcpyHostToDevice, s));
+    uint32_t* d_count = t->alloc<uint32_t>(T);
+    CK(cudaMemcpyAsync(d_count, forest->count.data(), size_t(T) * 4, cudaMemcpyHostToDevice, s));
+    uint32_t* d_masks = t->alloc<uint32_t>(size_t(T) * W);
+    CK(cudaMemcpyAsync(d_masks, forest->masks.data(), size_t(T) * W * 4, cudaMemcpyHostToDevice, s));
+    uint32_t* d_ranks = t->alloc<uint32_t>(size_t(T) * F);
+    CK(cudaMemcpyAsync(d_ranks, forest->ranks.data(), size_t(T) * F * 4, cudaMemcpyHostToDevice, s));
+    a.sample_rows = d_sample;
+    a.sample_count = d_count;
+    a.tree_feature_masks = d_masks;
+    a.feature_rank = d_ranks;
+    if (!forest->seeds.empty()) {
+      uint32_t* d_seeds = t->alloc<uint32_t>(T);
+      CK(cudaMemcpyAsync(d_seeds, forest->seeds.data(), size_t(T) * 4, cudaMemcpyHostToDevice, s));
+      a.tree_seeds = d_seeds;
+    }
+    a.skip_apply = 1;
+    CK(cudaStreamSynchronize(s));
+  }
   // working state
-  a.gh = t->alloc<float2>(size_t(T) * 2 * n);
+  a.gh = t->alloc<float2>(size_t(T) * 2 * seg_rows);
   a.gh_ordered = 1;
-  a.rows = t->alloc<uint32_t>(size_t(T) * 2 * n);
+  a.rows = t->alloc<uint32_t>(size_t(T) * 2 * seg_rows);
   a.trees = t->alloc<TreeState>(T);
   a.max_level_nodes = uint32_t(T * level_nodes);
   a.n_slots = a.max_level_nodes;
@@ -694,7 +733,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.sub = t->alloc<SubEntry>(a.max_level_nodes);
   a.part = t->alloc<PartEntry>(a.max_level_nodes);
   a.part_prefix = t->alloc<uint32_t>(a.max_level_nodes + 1);
-  a.max_part_chunks = uint32_t(T * ((n + kPartChunk - 1) / kPartChunk + level_nodes + 1));
+  a.max_part_chunks = uint32_t(T * ((seg_rows + kPartChunk - 1) / kPartChunk + level_nodes + 1));
   a.part_counts = t->alloc<uint32_t>(a.max_part_chunks);
   a.part_offsets = t->alloc<uint32_t>(a.max_part_chunks);
   a.part_flags = t->alloc<uint32_t>(size_t(a.max_part_chunks) * (kPartChunk / 32));
@@ -723,7 +762,8 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   CK(cudaStreamSynchronize(s));
 }
 
-mpsb_cuda_model* export_model(mpsb_cuda_trainer* t, uint32_t tree_index) {
+mpsb_cuda_model* export_model(mpsb_cuda_trainer* t, uint32_t tree_index,
+                              bool with_predictions = true) {
   const TrainerDev& a = t->dev;
   uint32_t rounds = 0;
   CK(cudaMemcpy(&rounds, a.round_counter, sizeof rounds, cudaMemcpyDeviceToHost));
@@ -742,9 +782,11 @@ mpsb_cuda_model* export_model(mpsb_cuda_trainer* t, uint32_t tree_index) {
                   a.model_nodes + (size_t(r) * a.n_trees + tree_index) * a.max_tree_nodes,
                   size_t(c) * sizeof(mpsb_tree_node), cudaMemcpyDeviceToHost));
   }
-  m->train_predictions.resize(a.n_rows);
-  CK(cudaMemcpy(m->train_predictions.data(), a.preds + size_t(tree_index) * a.n_rows,
-                size_t(a.n_rows) * sizeof(double), cudaMemcpyDeviceToHost));
+  if (with_predictions) {
+    m->train_predictions.resize(a.n_rows);
+    CK(cudaMemcpy(m->train_predictions.data(), a.preds + size_t(tree_index) * a.n_rows,
+                  size_t(a.n_rows) * sizeof(double), cudaMemcpyDeviceToHost));
+  }
   return m.release();
 }
 
@@ -842,6 +884,100 @@ int mpsb_cuda_train_ovr(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
   });
 }
 
+int mpsb_cuda_train_forest(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
+                           const double* labels, const double* weights, uint64_t n,
+                           const mpsb_train_params* p, uint32_t n_trees,
+                           const uint8_t* row_counts, const uint32_t* feature_offsets,
+                           const uint32_t* features, const uint32_t* seeds, uint32_t options,
+                           mpsb_cuda_model** out) {
+  return guard([&] {
+    if (!b || !ds || !labels || !p || !row_counts || !feature_offsets || !features || !out)
+      throw TrainingError("null argument");
+    if (n_trees == 0) throw TrainingError("n_estimators must be at least 1");
+    if (n != ds->n_rows) throw TrainingError("Training data, labels, or max_bins contract does not match");
+    if (p->n_interaction_groups)
+      throw UnsupportedError("forest training on the CUDA backend takes no interaction constraints");
+    validate_training_params(*p);
+    validate_tree_params(*p, ds->features);
+    validate_weights(weights, n);
+    const uint32_t F = ds->features, W = (F + 31) / 32;
+    // Trees per trainer: the histogram slots of a tree's widest level dominate its device
+    // memory, so batch as many trees as fit in half of the free memory.
+    mpsb_train_params tp = *p;
+    tp.n_estimators = 1;
+    uint64_t cap_all = 1;
+    for (uint32_t t = 0; t < n_trees; ++t) {
+      uint64_t c = 0;
+      for (uint64_t r = 0; r < n; ++r) c += row_counts[size_t(t) * n + r];
+      if (c == 0) throw TrainingError("a forest tree's row sample must not be empty");
+      if (c >= 0x80000000ull) throw UnsupportedError("a forest tree's row sample exceeds 2^31 rows");
+      cap_all = std::max(cap_all, c);
+      const uint32_t f0 = feature_offsets[t], f1 = feature_offsets[t + 1];
+      if (f1 <= f0) throw TrainingError("a forest tree's feature subset must not be empty");
+      std::vector<uint8_t> seen(F, 0);
+      for (uint32_t i = f0; i < f1; ++i) {
+        if (features[i] >= F) throw TrainingError("forest feature index out of range");
+        if (seen[features[i]]++) throw TrainingError("forest feature subsets must not repeat a feature");
+      }
+    }
+    const uint64_t leaves = std::min<uint64_t>(
+        {uint64_t(1) << std::min<uint32_t>(p->max_depth, 30), std::max<uint64_t>(effective_max_leaves(*p), 2),
+         std::max<uint64_t>(1, (cap_all + p->min_samples_leaf - 1) / p->min_samples_leaf)});
+    const uint64_t per_tree = leaves * uint64_t(F) * kSlots * 24 + cap_all * (2 * 12 + 8) + n * 8 +
+                              uint64_t(2 * leaves + 1) * 64 * 8;
+    size_t free_b = 0, total_b = 0;
+    b->activate();
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    uint64_t batch = std::max<uint64_t>(1, (free_b / 2) / std::max<uint64_t>(per_tree, 1));
+    if (const char* v = std::getenv("MPSB_FOREST_BATCH")) batch = std::max(1, std::atoi(v));
+    batch = std::min<uint64_t>(batch, n_trees);
+    for (uint32_t t0 = 0; t0 < n_trees; t0 += uint32_t(batch)) {
+      const uint32_t B = std::min<uint32_t>(uint32_t(batch), n_trees - t0);
+      ForestSpec fs;
+      fs.n_trees = B;
+      fs.count.resize(B);
+      for (uint32_t k = 0; k < B; ++k) {
+        uint64_t c = 0;
+        for (uint64_t r = 0; r < n; ++r) c += row_counts[size_t(t0 + k) * n + r];
+        fs.count[k] = uint32_t(c);
+        fs.cap = std::max<uint32_t>(fs.cap, uint32_t(c));
+      }
+      fs.sample.assign(size_t(B) * fs.cap, 0);
+      fs.masks.assign(size_t(B) * W, 0);
+      fs.ranks.assign(size_t(B) * F, 0);
+      fs.base_scores.resize(B);
+      if (seeds) fs.seeds.assign(seeds + t0, seeds + t0 + B);
+      std::vector<double> ys, ws;
+      for (uint32_t k = 0; k < B; ++k) {
+        const uint8_t* m = row_counts + size_t(t0 + k) * n;
+        uint32_t* dst = fs.sample.data() + size_t(k) * fs.cap;
+        ys.clear();
+        ws.clear();
+        uint32_t pos = 0;
+        for (uint64_t r = 0; r < n; ++r)
+          for (uint32_t c = 0; c < m[r]; ++c) {
+            dst[pos++] = uint32_t(r);
+            ys.push_back(labels[r]);
+            if (weights) ws.push_back(weights[r]);
+          }
+        // The reference fits the tree on its sample: base score over the sample's rows.
+        fs.base_scores[k] = base_score(tp, ys.data(), weights ? ws.data() : nullptr, ys.size(), -1);
+        std::vector<uint32_t> sub(features + feature_offsets[t0 + k], features + feature_offsets[t0 + k + 1]);
+        std::sort(sub.begin(), sub.end());
+        for (uint32_t i = 0; i < sub.size(); ++i) {
+          fs.masks[size_t(k) * W + sub[i] / 32] |= 1u << (sub[i] % 32);
+          fs.ranks[size_t(k) * F + sub[i]] = i;  // position in the tree's ascending subset
+        }
+      }
+      std::unique_ptr<mpsb_cuda_trainer> t(new mpsb_cuda_trainer);
+      setup_trainer(t.get(), b, ds, labels, weights, n, &tp, options | MPSB_OPT_NO_GRAPH, 0, &fs);
+      t->run(1);
+      t->synchronize();
+      for (uint32_t k = 0; k < B; ++k) out[t0 + k] = export_model(t.get(), k, false);
+    }
+  });
+}
+
 int mpsb_cuda_model_create(double base, double lr, uint32_t n_trees, const uint32_t* counts,
                            const mpsb_tree_node* nodes, mpsb_cuda_model** out) {
   return guard([&] {
@@ -876,6 +1012,8 @@ int mpsb_cuda_model_tree_nodes(const mpsb_cuda_model* m, uint32_t t, mpsb_tree_n
 }
 int mpsb_cuda_model_train_predictions(const mpsb_cuda_model* m, double* out) {
   return guard([&] {
+    if (m->train_predictions.empty())
+      throw TrainingError("this model holds no training predictions (forest tree or loaded model)");
     std::memcpy(out, m->train_predictions.data(), m->train_predictions.size() * sizeof(double));
   });
 }

@@ -35,10 +35,10 @@ __device__ __forceinline__ void raise(Control* ctl, uint32_t bits) { atomicOr(&c
 __device__ __forceinline__ uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
 // Rows per histogram work item for a level that builds `rows` rows: about per_sm (default
-// four) items per SM, a multiple of 512, within [4096, kItemRowsMax].
+// three) items per SM, a multiple of 512, within [4096, kItemRowsMax].
 __device__ __forceinline__ uint32_t adaptive_item_rows(uint64_t rows, uint32_t nfb, uint32_t sms,
                                                       uint32_t per_sm) {
-  const uint64_t target = uint64_t(sms ? sms : 152) * (per_sm ? per_sm : 4);
+  const uint64_t target = uint64_t(sms ? sms : 152) * (per_sm ? per_sm : 3);
   uint64_t per = (rows * nfb + target - 1) / target;
   per = (per + 511) / 512 * 512;
   if (per < 4096) per = 4096;
@@ -182,15 +182,24 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
   const bool unit_h = a.objective == 0 || a.objective == 2;
   const long long class_bits = __double_as_longlong(double(t));
   uint32_t mg = 0, mh = 0, bad = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_rows; i += gridDim.x * blockDim.x) {
+  // Position p of the tree's root segment holds row i: the identity for boosting, the
+  // tree's sample for a forest.
+  const uint32_t count = a.sample_rows ? a.sample_count[t] : a.n_rows;
+  const size_t pos_off = size_t(t) * 2 * a.seg_stride;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x) {
+    const uint32_t i = a.sample_rows ? a.sample_rows[size_t(t) * a.seg_stride + p] : p;
+    if (i >= a.n_rows) {
+      bad = 1;
+      continue;
+    }
     double y = a.labels[i];
     if (a.ovr) {  // y == t (class ids are non-negative integers; -0.0 equals class 0)
       const long long yb = __double_as_longlong(y);
       y = (yb == class_bits || (t == 0 && (yb << 1) == 0)) ? 1.0 : 0.0;
     }
-    const double p = a.preds[tree_off + i];
+    const double pred = a.preds[tree_off + i];
     double g = 0.0, h = 0.0;
-    if (!objective_pair(a.objective, y, p, a.params, &g, &h)) bad = 1;
+    if (!objective_pair(a.objective, y, pred, a.params, &g, &h)) bad = 1;
     if (a.weights != nullptr) {
       const double w = a.weights_per_tree ? a.weights[tree_off + i] : a.weights[i];
       g = __dmul_rn(g, w);
@@ -199,8 +208,8 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
     }
     const float g32 = f64_to_f32_rn(g), h32 = f64_to_f32_rn(h);
     if (!isfinite(g32) || !isfinite(h32)) bad = 1;
-    a.gh[size_t(t) * 2 * a.n_rows + i] = make_float2(g32, h32);  // parity 0 = row order
-    a.rows[size_t(t) * 2 * a.n_rows + i] = i;
+    a.gh[pos_off + p] = make_float2(g32, h32);  // parity 0 = the root segment's order
+    a.rows[pos_off + p] = i;
     mg = max(mg, __float_as_uint(fabsf(g32)));
     mh = max(mh, __float_as_uint(fmaxf(h32, 0.0f)));
   }
@@ -225,10 +234,32 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
   if (bad) raise(a.ctl, kErrGradient);
 }
 
+__device__ __forceinline__ uint32_t root_rows(const TrainerDev& a, uint32_t t) {
+  return a.sample_rows ? a.sample_count[t] : a.n_rows;
+}
+
 __global__ void round_setup_kernel(TrainerDev a) {
-  const uint32_t item_rows =
-      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(a.n_rows) * a.n_trees, a.nfb, a.sm_count, a.items_per_sm);
-  const uint32_t chunks_per_tree = ceil_div(a.n_rows, item_rows);
+  if (threadIdx.x == 0) {  // trees are few: serial prefix of the roots' work items
+    uint64_t total = 0;
+    for (uint32_t t = 0; t < a.n_trees; ++t) total += root_rows(a, t);
+    const uint32_t item_rows =
+        a.item_rows ? a.item_rows : adaptive_item_rows(total, a.nfb, a.sm_count, a.items_per_sm);
+    uint32_t acc = 0;
+    for (uint32_t t = 0; t < a.n_trees; ++t) {
+      a.build_prefix[t] = acc;
+      acc += ceil_div(root_rows(a, t), item_rows);
+    }
+    a.build_prefix[a.n_trees] = acc;
+    a.ctl->free_top = a.n_slots - a.n_trees;
+    a.ctl->n_nodes = a.n_trees;
+    a.ctl->n_build = a.n_trees;
+    a.ctl->n_sub = 0;
+    a.ctl->n_part = 0;
+    a.ctl->hist_items = acc * a.nfb;
+    a.ctl->hist_counter = 0;
+    a.ctl->split_items = a.n_trees * a.n_fchunks;
+    a.ctl->item_rows = item_rows;
+  }
   for (uint32_t base = 0; base < a.n_trees; base += blockDim.x) {
     const uint32_t t = base + threadIdx.x;
     if (t < a.n_trees) {
@@ -240,9 +271,10 @@ __global__ void round_setup_kernel(TrainerDev a) {
       s.inv_g = ldexp(1.0, -s.kg);
       s.inv_h = ldexp(1.0, -s.kh);
       const uint32_t slot = a.free_stack[a.n_slots - 1 - t];
+      const uint32_t cnt = root_rows(a, t);
       NodeRec r;
       r.seg_off = 0;
-      r.seg_cnt = a.n_rows;
+      r.seg_cnt = cnt;
       r.node_index = 0;
       r.slot = slot;
       r.count = 0;
@@ -269,24 +301,11 @@ __global__ void round_setup_kernel(TrainerDev a) {
       e.tree = t;
       e.parity = 0;
       e.seg_off = 0;
-      e.seg_cnt = a.n_rows;
+      e.seg_cnt = cnt;
       e.slot = slot;
       e.pad = 0;
       a.build[t] = e;
-      a.build_prefix[t] = t * chunks_per_tree;
     }
-  }
-  if (threadIdx.x == 0) {
-    a.build_prefix[a.n_trees] = a.n_trees * chunks_per_tree;
-    a.ctl->free_top = a.n_slots - a.n_trees;
-    a.ctl->n_nodes = a.n_trees;
-    a.ctl->n_build = a.n_trees;
-    a.ctl->n_sub = 0;
-    a.ctl->n_part = 0;
-    a.ctl->hist_items = a.n_trees * chunks_per_tree * a.nfb;
-    a.ctl->hist_counter = 0;
-    a.ctl->split_items = a.n_trees * a.n_fchunks;
-    a.ctl->item_rows = item_rows;
   }
 }
 
@@ -650,7 +669,10 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
         const int8_t mono = P.has_monotonic ? a.monotonic[f] : 0;
         const uint32_t rnd =
             P.split_strategy == 1
-                ? stable_random_threshold(P.random_seed, f, node.node_index, node.depth, nb - 1)
+                ? stable_random_threshold(
+                      a.tree_seeds ? a.tree_seeds[node.tree] : P.random_seed,
+                      a.feature_rank ? a.feature_rank[size_t(node.tree) * a.features + f] : f,
+                      node.node_index, node.depth, nb - 1)
                 : 0xffffffffu;
         // Exact FP32 pre-screen. Every eligible candidate's score S = gL^2/(hL+lambda) +
         // gR^2/(hR+lambda) is computed in FP32 with relative error <= 13u (u = 2^-24; each
@@ -1206,7 +1228,7 @@ __global__ void __launch_bounds__(kPartThreads) partition_count_kernel(TrainerDe
     const uint32_t lc = c - a.part_prefix[e];
     const uint32_t start = lc * kPartChunk;
     const uint32_t count = min(kPartChunk, pe.seg_cnt - start);
-    const uint32_t* rows = a.rows + (size_t(pe.tree) * 2 + pe.parity) * a.n_rows + pe.seg_off + start;
+    const uint32_t* rows = a.rows + (size_t(pe.tree) * 2 + pe.parity) * a.seg_stride + pe.seg_off + start;
     uint32_t mine = 0;
 #pragma unroll
     for (int k = 0; k < kPartPerThread; ++k) {
@@ -1286,8 +1308,8 @@ __global__ void __launch_bounds__(kPartThreads) partition_scatter_kernel(Trainer
       }
     }
     __syncthreads();
-    const size_t src_off = (size_t(pe.tree) * 2 + pe.parity) * a.n_rows + pe.seg_off + start;
-    const size_t dst_off = (size_t(pe.tree) * 2 + (pe.parity ^ 1)) * a.n_rows + pe.seg_off;
+    const size_t src_off = (size_t(pe.tree) * 2 + pe.parity) * a.seg_stride + pe.seg_off + start;
+    const size_t dst_off = (size_t(pe.tree) * 2 + (pe.parity ^ 1)) * a.seg_stride + pe.seg_off;
     const uint32_t* src = a.rows + src_off;
     uint32_t* dst = a.rows + dst_off;
     const float2* gh_src = a.gh_ordered ? a.gh + src_off : nullptr;
@@ -1322,6 +1344,7 @@ __global__ void __launch_bounds__(kPartThreads) partition_scatter_kernel(Trainer
 // Leaf application and round end
 // ------------------------------------------------------------------------------------
 __global__ void apply_leaves_kernel(TrainerDev a) {
+  if (a.skip_apply) return;  // forest trees: no training predictions
   const double lr = a.params.learning_rate;
   uint32_t err = 0;
   const uint32_t n_seg = a.ctl->n_leafseg;
@@ -1331,7 +1354,7 @@ __global__ void apply_leaves_kernel(TrainerDev a) {
     const LeafSeg ls = a.leafseg[s];
     const uint32_t start = (c - a.leaf_prefix[s]) * kApplyChunk;
     const uint32_t count = min(kApplyChunk, ls.seg_cnt - start);
-    const uint32_t* rows = a.rows + (size_t(ls.tree) * 2 + ls.parity) * a.n_rows + ls.seg_off + start;
+    const uint32_t* rows = a.rows + (size_t(ls.tree) * 2 + ls.parity) * a.seg_stride + ls.seg_off + start;
     double* pred = a.preds + size_t(ls.tree) * a.n_rows;
     // lr * leaf is the same product for every row of a leaf.
     const double step = __dmul_rn(lr, ls.value);

@@ -24,10 +24,20 @@ struct TrainerDev {
   uint32_t weights_per_tree;
   uint32_t objective;
   double* preds;                // [n_trees][n_rows]
-  float2* gh;                   // gh_ordered: [n_trees][2][n_rows] in row-segment order
+  float2* gh;                   // gh_ordered: [n_trees][2][seg_stride] in row-segment order
                                 // (moved along by the partition); else [n_trees][n_rows]
   uint32_t gh_ordered;
-  uint32_t* rows;               // [n_trees][2][n_rows]
+  uint32_t* rows;               // [n_trees][2][seg_stride] row ids of the level's segments
+  uint32_t seg_stride;          // positions per (tree, parity) of rows / gh: n_rows, or the
+                                // largest sample of a forest (a row appears once per draw)
+  // Forest samples (null for boosting): per tree the multiset of rows it trains on,
+  // [n_trees][seg_stride] in ascending row order, and its size; the feature rank of each
+  // feature in the tree's subset (random thresholds hash the rank) and per-tree seeds.
+  const uint32_t* sample_rows;
+  const uint32_t* sample_count;   // [n_trees]
+  const uint32_t* feature_rank;   // [n_trees][features] or null (rank = feature)
+  const uint32_t* tree_seeds;     // [n_trees] or null (params.random_seed)
+  uint32_t skip_apply;            // 1: no prediction update (forest trees are single-round)
   TreeState* trees;             // [n_trees]
   TreeParams params;
   const int8_t* monotonic;      // [features] or null
@@ -62,7 +72,7 @@ struct TrainerDev {
   uint32_t item_rows;           // rows per histogram work item (<= kItemRowsMax); 0: the
                                 // level's adaptive value ctl->item_rows
   uint32_t sm_count;
-  uint32_t items_per_sm;        // histogram work items per SM of the adaptive item size (0: 4)
+  uint32_t items_per_sm;        // histogram work items per SM of the adaptive item size (0: 3)
   uint32_t mode;                // kModeFixed / kModeFloat
   uint32_t ovr;                 // labels are class ids; tree t fits class t (logistic)
   uint32_t scan_threads;        // block size of the split scan (multiple of 32)

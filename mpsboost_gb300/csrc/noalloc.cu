@@ -168,6 +168,7 @@ extern "C" int mpsb_cuda_build_histogram_noalloc(const uint8_t* bins, uint32_t d
     a.bins_block_stride = uint64_t(dataset_rows) * kBlockFeatures;
     a.sm_count = uint32_t(sc.sm_count);
     a.n_rows = dataset_rows;
+    a.seg_stride = dataset_rows;  // one segment (tree 0, parity 0) at offset 0
     a.features = features;
     a.nfb = nfb;
     a.n_trees = 1;

@@ -48,6 +48,7 @@ void base_session(Session& ss, mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds
   a.bin_count = ds->bin_count.as<uint32_t>();
   a.has_missing = ds->has_missing.as<uint8_t>();
   a.n_rows = ds->n_rows;
+  a.seg_stride = ds->n_rows;  // the partition entry writes parity 1 at this offset
   a.features = ds->features;
   a.nfb = ds->nfb;
   a.n_trees = 1;

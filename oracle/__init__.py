@@ -329,6 +329,17 @@ class Oracle:
         )
         return self._wrap_dataset(out.value)
 
+    def dataset_subset(self, dataset: Dataset, rows, features) -> Dataset:
+        """matrix[rows][:, features] with the source's bins (a forest tree's sample)."""
+
+        self._port_only()
+        r = np.ascontiguousarray(rows, dtype=np.uint64)
+        f = np.ascontiguousarray(features, dtype=np.uint32)
+        out = C.c_void_p()
+        self._check(self.lib.orc_dataset_subset(C.c_void_p(dataset.handle), _ptr(r), C.c_uint64(r.size),
+                                                _ptr(f), C.c_uint32(f.size), C.byref(out)))
+        return self._wrap_dataset(out.value)
+
     # -- objectives / histograms -------------------------------------------------------
     def gradients(self, objective, labels, predictions, alpha=0.5, variance_power=1.5) -> np.ndarray:
         y = np.ascontiguousarray(labels, dtype=np.float64)

@@ -258,6 +258,45 @@ int orc_transform_dense(const void* schema_dataset, const void* data, int scalar
   return ORC_OK;
 }
 
+int orc_dataset_subset(const void* src, const uint64_t* rows, uint64_t n_rows,
+                       const uint32_t* features, uint32_t n_features, void** out) {
+  const dataset_t* s = (const dataset_t*)src;
+  if (n_rows == 0 || n_features == 0) return fail(ORC_DATA_ERROR, "empty subset");
+  for (uint64_t i = 0; i < n_rows; ++i)
+    if (rows[i] >= s->rows) return fail(ORC_DATA_ERROR, "subset row out of range");
+  uint64_t total = 0;
+  for (uint32_t j = 0; j < n_features; ++j) {
+    if (features[j] >= s->features) return fail(ORC_DATA_ERROR, "subset feature out of range");
+    total += s->boundary_count[features[j]];
+  }
+  dataset_t* d = alloc_dataset(n_rows, n_features);
+  if (!d) return fail(ORC_OTHER_ERROR, "out of host memory");
+  d->max_bins = s->max_bins;
+  d->n_boundaries = total;
+  d->boundaries = (float*)malloc((total > 0 ? total : 1) * sizeof(float));
+  if (!d->boundaries) { orc_dataset_free(d); return fail(ORC_OTHER_ERROR, "out of host memory"); }
+  uint64_t off = 0;
+  for (uint32_t j = 0; j < n_features; ++j) {
+    const uint32_t f = features[j];
+    d->boundary_offset[j] = off;
+    d->boundary_count[j] = s->boundary_count[f];
+    d->bin_count[j] = s->bin_count[f];
+    memcpy(d->boundaries + off, s->boundaries + s->boundary_offset[f],
+           s->boundary_count[f] * sizeof(float));
+    off += s->boundary_count[f];
+    uint64_t missing = 0;
+    for (uint64_t i = 0; i < n_rows; ++i) {
+      const uint64_t si = (uint64_t)f * s->rows + rows[i], di = (uint64_t)j * n_rows + i;
+      d->bins[di] = s->bins[si];
+      d->missing[di] = s->missing[si];
+      missing += s->missing[si];
+    }
+    d->missing_count[j] = missing;
+  }
+  *out = d;
+  return ORC_OK;
+}
+
 int orc_dataset_info(const void* p, uint64_t* rows, uint32_t* features, uint32_t* max_bins,
                      uint64_t* boundary_total) {
   const dataset_t* d = (const dataset_t*)p;

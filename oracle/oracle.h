@@ -171,6 +171,12 @@ int orc_scan_splits(const void* dataset, const double* pairs, uint64_t n,
 int orc_partition_rows(const void* dataset, const uint64_t* rows, uint64_t n_rows,
                        uint32_t feature, uint32_t threshold_bin, int default_left,
                        uint64_t* left_out, uint64_t* right_out, uint64_t* n_left);
+/* The materialized sample of a forest tree, matrix[rows][:, features] with the source's
+   bins and boundaries (rows may repeat; features in the given order). Missing counts are
+   recomputed for the sample. The schema of _ForestMixin's per-tree fit
+   (forest_sampling.py:56-60) when the sample keeps the full data's bin boundaries. */
+int orc_dataset_subset(const void* dataset, const uint64_t* rows, uint64_t n_rows,
+                       const uint32_t* features, uint32_t n_features, void** out);
 /* Weighted FP64 gradients of one boosting round rounded to FP32, the input of the
    fixed-point replica (trainer.cpp:178-216 followed by a round-to-nearest cast). */
 int orc_weighted_pairs32(uint32_t objective, double alpha, double variance_power,

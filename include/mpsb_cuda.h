@@ -14,6 +14,10 @@
  *   mpsb_cuda_backend_info             QueryBackendInfo (backend.hpp:197-200)
  *   mpsb_quantize_dense                QuantizeDense (binned_dataset.hpp:137-138)
  *   mpsb_transform_dense               TransformDense (binned_dataset.hpp:140-144)
+ *   mpsb_cuda_dataset_quantize         QuantizeDense (binned_dataset.hpp:137-138) on the
+ *                                      device, the binned matrix left resident
+ *   mpsb_cuda_dataset_transform        TransformDense (binned_dataset.hpp:140-144) on
+ *                                      the device with a quantized dataset's schema
  *   mpsb_cuda_dataset_create           the per-node NewBuffer(dataset.bin_data())
  *                                      upload of src/mps/mps_histogram.mm:149, made
  *                                      once per dataset and kept resident
@@ -262,6 +266,32 @@ int mpsb_cuda_build_histogram_noalloc(const uint8_t* bins, uint32_t dataset_rows
                                       uint32_t features, const uint32_t* rows,
                                       uint32_t n_rows, const float* pairs,
                                       mpsb_histogram_bin* out, void* stream);
+
+/* ---- quantile binning on the device ------------------------------------------- */
+/* QuantizeDense on the GPU: the matrix (scalar_type 1 = float32, 2 = float64; element
+   (r, f) at byte offset r * row_stride + f * col_stride) is uploaded, binned with the
+   reference's quantile rule and kept resident as a training dataset. NaN is missing, Inf
+   and float64 values outside the float32 range are DataErrors. max_bins <= 256 (255 when a
+   feature has missing values). Bins and boundaries equal mpsb_quantize_dense's, except
+   that a boundary at zero may carry either sign (the two zeros compare equal). */
+int mpsb_cuda_dataset_quantize(mpsb_cuda_backend* backend, const void* data, int scalar_type,
+                               uint64_t rows, uint32_t features, uint64_t row_stride,
+                               uint64_t col_stride, uint32_t max_bins, mpsb_cuda_dataset** out);
+/* TransformDense on the GPU with the boundaries of a device-quantized dataset. */
+int mpsb_cuda_dataset_transform(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* schema,
+                                const void* data, int scalar_type, uint64_t rows,
+                                uint32_t features, uint64_t row_stride, uint64_t col_stride,
+                                mpsb_cuda_dataset** out);
+/* The schema of a device-quantized dataset: boundary_total() floats, and per feature the
+   offset and count of its boundaries, its bin count and missing count. Any output may be
+   NULL. */
+uint64_t mpsb_cuda_dataset_boundary_total(const mpsb_cuda_dataset* dataset);
+int mpsb_cuda_dataset_schema(const mpsb_cuda_dataset* dataset, float* boundaries,
+                             uint64_t* boundary_offset, uint32_t* boundary_count,
+                             uint32_t* bin_count, uint64_t* missing_count);
+/* The binned matrix, feature-major u8 [features][rows] (missing rows as bin 0), and the
+   missing flags (may be NULL), as mpsb_quantize_dense lays them out. */
+int mpsb_cuda_dataset_export(const mpsb_cuda_dataset* dataset, uint8_t* bins, uint8_t* missing);
 
 /* ---- training ------------------------------------------------------------------ */
 /* weights may be NULL (unit weights). options: MPSB_OPT_* bits. */

@@ -12,11 +12,13 @@ from .backend import (
     DEFAULT_PARAMS,
     BinnedDataset,
     CudaBackend,
+    DeviceBinnedDataset,
     RegressionModel,
     Trainer,
     forest_samples,
     make_params,
     quantize_dense,
+    quantize_device,
     train_forest,
     train_ovr,
     train_regressor,
@@ -28,6 +30,7 @@ __all__ = [
     "CudaBackend",
     "DataError",
     "DEFAULT_PARAMS",
+    "DeviceBinnedDataset",
     "RegressionModel",
     "Trainer",
     "TrainingError",
@@ -36,6 +39,7 @@ __all__ = [
     "UnsupportedError",
     "make_params",
     "quantize_dense",
+    "quantize_device",
     "train_ovr",
     "train_regressor",
 ]

@@ -140,6 +140,11 @@ SIGNATURES = {
     "mpsb_cuda_partition_rows": (_I32, [_VP, _VP, _VP, _U64, _U32, _U32, _I32, _VP, _VP, C.POINTER(_U64)]),
     "mpsb_cuda_build_histogram_noalloc": (_I32, [_VP, _U32, _U32, _VP, _U32, _VP, _VP, _VP]),
     "mpsb_cuda_train_regressor": (_I32, [_VP, _VP, _VP, _VP, _U64, C.POINTER(TrainParams), _U32, C.POINTER(_VP)]),
+    "mpsb_cuda_dataset_quantize": (_I32, [_VP, _VP, C.c_int, _U64, _U32, _U64, _U64, _U32, C.POINTER(_VP)]),
+    "mpsb_cuda_dataset_transform": (_I32, [_VP, _VP, _VP, C.c_int, _U64, _U32, _U64, _U64, C.POINTER(_VP)]),
+    "mpsb_cuda_dataset_boundary_total": (_U64, [_VP]),
+    "mpsb_cuda_dataset_schema": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "mpsb_cuda_dataset_export": (_I32, [_VP, _VP, _VP]),
     "mpsb_cuda_train_ovr": (_I32, [_VP, _VP, _VP, _VP, _U64, _U32, C.POINTER(TrainParams), _U32, _VP]),
     "mpsb_cuda_train_forest": (_I32, [_VP, _VP, _VP, _VP, _U64, C.POINTER(TrainParams), _U32, _VP, _VP,
                                       _VP, _VP, _U32, _VP]),

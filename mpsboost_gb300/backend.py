@@ -214,6 +214,16 @@ def quantize_dense(matrix, max_bins: int = 256, n_threads: int = 0) -> BinnedDat
 class DeviceDataset:
     """A binned dataset resident in HBM (column-blocked u8, missing at slot 255)."""
 
+    @classmethod
+    def _adopt(cls, backend: "CudaBackend", handle, rows: int, features: int) -> "DeviceDataset":
+        self = cls.__new__(cls)
+        self.backend = backend
+        self.binned = None
+        self.rows = rows
+        self.features = features
+        self.handle = handle
+        return self
+
     def __init__(self, backend: "CudaBackend", binned: BinnedDataset):
         lib = _lib.load()
         self.backend = backend
@@ -242,6 +252,65 @@ class DeviceDataset:
             self.close()
         except Exception:
             pass
+
+
+class DeviceBinnedDataset:
+    """A matrix quantile-binned on the GPU and kept there (QuantizeDense on the device).
+
+    Usable wherever a ``BinnedDataset`` is (training, prediction) on the backend that
+    binned it; ``to_host()`` returns the same bins and schema as ``quantize_dense``."""
+
+    def __init__(self, backend: "CudaBackend", handle, rows: int, features: int, max_bins: int):
+        self.backend = backend
+        self.rows = rows
+        self.features = features
+        self.max_bins = max_bins
+        self._dev = DeviceDataset._adopt(backend, handle, rows, features)
+        lib = _lib.load()
+        total = int(lib.mpsb_cuda_dataset_boundary_total(handle))
+        self.boundaries_flat = np.empty(max(total, 1), np.float32)
+        self.boundary_offsets = np.empty(features, np.uint64)
+        self.boundary_counts = np.empty(features, np.uint32)
+        self.bin_counts = np.empty(features, np.uint32)
+        self.missing_counts = np.empty(features, np.uint64)
+        check(lib.mpsb_cuda_dataset_schema(handle, ptr(self.boundaries_flat), ptr(self.boundary_offsets),
+                                           ptr(self.boundary_counts), ptr(self.bin_counts),
+                                           ptr(self.missing_counts)))
+        self.boundaries_flat = self.boundaries_flat[:total]
+
+    def to_host(self) -> BinnedDataset:
+        lib = _lib.load()
+        bins = np.empty((self.features, self.rows), np.uint8)
+        missing = np.empty((self.features, self.rows), np.uint8)
+        check(lib.mpsb_cuda_dataset_export(self._dev.handle, ptr(bins), ptr(missing)))
+        return BinnedDataset(self.rows, self.features, self.max_bins, bins, missing.astype(bool),
+                             self.boundaries_flat.copy(), self.boundary_offsets.copy(),
+                             self.boundary_counts.copy(), self.bin_counts.copy(), self.missing_counts.copy())
+
+    def transform(self, matrix) -> "DeviceBinnedDataset":
+        """Bin new data on the device with this schema (TransformDense)."""
+
+        x, st, rs, cs = _as_matrix(matrix)
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.mpsb_cuda_dataset_transform(self.backend.handle, self._dev.handle, ptr(x), st,
+                                              x.shape[0], x.shape[1], rs, cs, C.byref(h)))
+        return DeviceBinnedDataset(self.backend, h, x.shape[0], x.shape[1], self.max_bins)
+
+    def close(self) -> None:
+        self._dev.close()
+
+
+def quantize_device(backend: "CudaBackend", matrix, max_bins: int = 256) -> DeviceBinnedDataset:
+    """Quantile-bin a float32/float64 matrix on the GPU (QuantizeDense,
+    binned_dataset.cpp:126-188) and keep the bins resident for training."""
+
+    x, st, rs, cs = _as_matrix(matrix)
+    lib = _lib.load()
+    h = C.c_void_p()
+    check(lib.mpsb_cuda_dataset_quantize(backend.handle, ptr(x), st, x.shape[0], x.shape[1], rs, cs,
+                                         max_bins, C.byref(h)))
+    return DeviceBinnedDataset(backend, h, x.shape[0], x.shape[1], max_bins)
 
 
 class CudaBackend:
@@ -283,7 +352,11 @@ class CudaBackend:
             pass
 
     # -- datasets ------------------------------------------------------------------------
-    def dataset(self, binned: BinnedDataset) -> DeviceDataset:
+    def dataset(self, binned) -> DeviceDataset:
+        if isinstance(binned, DeviceBinnedDataset):
+            if binned.backend is not self:
+                raise ValueError("a device-binned dataset trains on the backend that binned it")
+            return binned._dev
         key = id(self)
         dev = binned._device.get(key)
         if dev is None:

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmpsb_cuda.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["hist.cu", "kernels.cu", "host.cu", "node_entries.cu", "noalloc.cu", "quantize.cpp"]
+SOURCES = ["hist.cu", "kernels.cu", "host.cu", "node_entries.cu", "noalloc.cu", "binning.cu",
+           "quantize.cpp"]
 
 
 def _nvcc() -> str:

@@ -103,6 +103,13 @@ struct mpsb_cuda_dataset {
   mpsb::DevBuf bins, bins_blocked, bins_fm, bin_count, has_missing;
   std::vector<uint32_t> h_bin_count;
   std::vector<uint8_t> h_has_missing;
+  // Quantization schema (datasets binned on the device): boundaries per feature.
+  bool has_schema = false;
+  uint32_t max_bins = 0;
+  std::vector<float> boundaries;
+  std::vector<uint64_t> boundary_offset;
+  std::vector<uint32_t> boundary_count;
+  std::vector<uint64_t> missing_count;
 };
 
 struct mpsb_cuda_model {

@@ -43,6 +43,10 @@
  *                                      forest_sampling.py:42-63): one single-round tree
  *                                      per row sample and feature subset
  *   mpsb_cuda_model_create             RegressionModel::Restore (trainer.hpp:271-279)
+ *   mpsb_cuda_model_serialize /        SerializeModel / DeserializeModel, SaveModelFile /
+ *   _deserialize / _save / _load       LoadModelFile (trainer.hpp:152-160): the native
+ *                                      model format 1.4 (src/io/model_format.cpp,
+ *                                      model_payload.cpp), byte for byte
  *   mpsb_cuda_model_predict            RegressionModel::Predict (trainer.hpp:266-269)
  *   mpsb_cuda_trainer_*                the same training loop as a session with
  *                                      device-resident inputs (benchmarks, timing)
@@ -292,6 +296,35 @@ int mpsb_cuda_dataset_schema(const mpsb_cuda_dataset* dataset, float* boundaries
 /* The binned matrix, feature-major u8 [features][rows] (missing rows as bin 0), and the
    missing flags (may be NULL), as mpsb_quantize_dense lays them out. */
 int mpsb_cuda_dataset_export(const mpsb_cuda_dataset* dataset, uint8_t* bins, uint8_t* missing);
+
+/* ---- model files ----------------------------------------------------------------- */
+/* The reference's native model format (magic MPSBMOD, version 1.4, FNV-1a checksum),
+   byte for byte: models written here load in the reference and the reference's load
+   here (minor versions 0-4 are read). A model needs its training data's quantization
+   schema: models trained on a device-quantized dataset carry it; otherwise attach it
+   with mpsb_cuda_model_set_schema (the arrays of mpsb_quantize_dense). Objective
+   metadata comes from training (or mpsb_cuda_model_set_objective). Reading applies the
+   reference's validation; violations are TrainingErrors (DataError for the schema). */
+int mpsb_cuda_model_set_schema(mpsb_cuda_model* model, uint32_t features, uint32_t max_bins,
+                               const float* boundaries, uint64_t n_boundaries,
+                               const uint64_t* boundary_offset, const uint32_t* boundary_count,
+                               const uint32_t* bin_count, const uint64_t* missing_count);
+int mpsb_cuda_model_set_objective(mpsb_cuda_model* model, uint32_t objective, double alpha,
+                                  double variance_power);
+int mpsb_cuda_model_get_objective(const mpsb_cuda_model* model, uint32_t* objective,
+                                  double* alpha, double* variance_power);
+/* Sizes first (array outputs NULL), then the arrays. */
+int mpsb_cuda_model_get_schema(const mpsb_cuda_model* model, uint32_t* features,
+                               uint32_t* max_bins, uint64_t* n_boundaries, float* boundaries,
+                               uint64_t* boundary_offset, uint32_t* boundary_count,
+                               uint32_t* bin_count, uint64_t* missing_count);
+/* *size receives the file size; out (capacity bytes) receives the bytes when not NULL. */
+int mpsb_cuda_model_serialize(const mpsb_cuda_model* model, uint8_t* out, uint64_t capacity,
+                              uint64_t* size);
+int mpsb_cuda_model_deserialize(const uint8_t* data, uint64_t size, mpsb_cuda_model** out);
+/* Atomic save (temporary file in the same directory, fsync, rename) and load. */
+int mpsb_cuda_model_save(const mpsb_cuda_model* model, const char* path);
+int mpsb_cuda_model_load(const char* path, mpsb_cuda_model** out);
 
 /* ---- training ------------------------------------------------------------------ */
 /* weights may be NULL (unit weights). options: MPSB_OPT_* bits. */

@@ -466,6 +466,20 @@ class CudaBackend:
 # --------------------------------------------------------------------------------------
 # Models and training
 # --------------------------------------------------------------------------------------
+_OBJECTIVE_CODES = {"squared_error": 0, "binary_logistic": 1, "quantile": 2, "poisson": 3, "tweedie": 4}
+
+
+def _schema_of(dataset) -> dict:
+    """The quantization schema a model file stores (QuantizationSchema)."""
+
+    return dict(features=int(dataset.features), max_bins=int(dataset.max_bins),
+                boundaries=np.ascontiguousarray(dataset.boundaries_flat, np.float32),
+                boundary_offsets=np.ascontiguousarray(dataset.boundary_offsets, np.uint64),
+                boundary_counts=np.ascontiguousarray(dataset.boundary_counts, np.uint32),
+                bin_counts=np.ascontiguousarray(dataset.bin_counts, np.uint32),
+                missing_counts=np.ascontiguousarray(dataset.missing_counts, np.uint64))
+
+
 @dataclass
 class RegressionModel:
     """base_score + learning_rate * sum of flat trees (RegressionModel, trainer.hpp:37-76)."""
@@ -474,6 +488,10 @@ class RegressionModel:
     learning_rate: float
     trees: list
     train_predictions: np.ndarray | None = None
+    objective: int = 0
+    objective_alpha: float = 0.5
+    tweedie_variance_power: float = 1.5
+    schema: dict | None = None
 
     @classmethod
     def _from_handle(cls, handle) -> "RegressionModel":
@@ -484,7 +502,68 @@ class RegressionModel:
             check(lib.mpsb_cuda_model_tree_nodes(handle, t, ptr(nodes)))
             trees.append(nodes)
         model = cls(lib.mpsb_cuda_model_base_score(handle), lib.mpsb_cuda_model_learning_rate(handle), trees)
+        obj, alpha, power = C.c_uint32(), C.c_double(), C.c_double()
+        check(lib.mpsb_cuda_model_get_objective(handle, C.byref(obj), C.byref(alpha), C.byref(power)))
+        model.objective, model.objective_alpha, model.tweedie_variance_power = obj.value, alpha.value, power.value
+        feats, bins, nb = C.c_uint32(), C.c_uint32(), C.c_uint64()
+        if lib.mpsb_cuda_model_get_schema(handle, C.byref(feats), C.byref(bins), C.byref(nb),
+                                          None, None, None, None, None) == 0:
+            f = feats.value
+            sc = dict(features=f, max_bins=bins.value, boundaries=np.empty(nb.value, np.float32),
+                      boundary_offsets=np.empty(f, np.uint64), boundary_counts=np.empty(f, np.uint32),
+                      bin_counts=np.empty(f, np.uint32), missing_counts=np.empty(f, np.uint64))
+            check(lib.mpsb_cuda_model_get_schema(handle, None, None, None, ptr(sc["boundaries"]),
+                                                 ptr(sc["boundary_offsets"]), ptr(sc["boundary_counts"]),
+                                                 ptr(sc["bin_counts"]), ptr(sc["missing_counts"])))
+            model.schema = sc
         return model
+
+    # -- the native model file (SerializeModel / DeserializeModel, trainer.hpp:152-160) --
+    def to_bytes(self, dataset=None) -> bytes:
+        """Model file bytes (format 1.4). ``dataset``: the training data whose schema the
+        file stores, when the model does not carry one."""
+
+        lib = _lib.load()
+        h = self._handle(lib, dataset)
+        try:
+            size = C.c_uint64()
+            check(lib.mpsb_cuda_model_serialize(h, None, 0, C.byref(size)))
+            out = np.empty(size.value, np.uint8)
+            check(lib.mpsb_cuda_model_serialize(h, ptr(out), out.size, C.byref(size)))
+        finally:
+            lib.mpsb_cuda_model_destroy(h)
+        return out.tobytes()
+
+    @classmethod
+    def from_bytes(cls, data: bytes) -> "RegressionModel":
+        lib = _lib.load()
+        buf = np.frombuffer(bytes(data), np.uint8)
+        h = C.c_void_p()
+        check(lib.mpsb_cuda_model_deserialize(ptr(buf) if buf.size else None, buf.size, C.byref(h)))
+        try:
+            return cls._from_handle(h)
+        finally:
+            lib.mpsb_cuda_model_destroy(h)
+
+    def save(self, path: str, dataset=None) -> None:
+        """Atomic save (SaveModelFile): temporary file, fsync, rename."""
+
+        lib = _lib.load()
+        h = self._handle(lib, dataset)
+        try:
+            check(lib.mpsb_cuda_model_save(h, os.fsencode(path)))
+        finally:
+            lib.mpsb_cuda_model_destroy(h)
+
+    @classmethod
+    def load(cls, path: str) -> "RegressionModel":
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.mpsb_cuda_model_load(os.fsencode(path), C.byref(h)))
+        try:
+            return cls._from_handle(h)
+        finally:
+            lib.mpsb_cuda_model_destroy(h)
 
     def predict(self, backend: CudaBackend, dataset: BinnedDataset) -> np.ndarray:
         """Device batch prediction over a binned dataset with the training schema."""
@@ -499,13 +578,25 @@ class RegressionModel:
             lib.mpsb_cuda_model_destroy(handle)
         return out
 
-    def _handle(self, lib):
+    def _handle(self, lib, dataset=None):
         counts = np.asarray([len(t) for t in self.trees], np.uint32)
         nodes = np.concatenate(self.trees) if self.trees else np.empty(0, NODE_DTYPE)
         nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
         h = C.c_void_p()
         check(lib.mpsb_cuda_model_create(self.base_score, self.learning_rate, len(self.trees),
                                          ptr(counts), ptr(nodes), C.byref(h)))
+        try:
+            check(lib.mpsb_cuda_model_set_objective(h, int(self.objective), float(self.objective_alpha),
+                                                    float(self.tweedie_variance_power)))
+            sc = _schema_of(dataset) if dataset is not None else self.schema
+            if sc is not None:
+                check(lib.mpsb_cuda_model_set_schema(
+                    h, sc["features"], sc["max_bins"], ptr(sc["boundaries"]), sc["boundaries"].size,
+                    ptr(sc["boundary_offsets"]), ptr(sc["boundary_counts"]), ptr(sc["bin_counts"]),
+                    ptr(sc["missing_counts"])))
+        except Exception:
+            lib.mpsb_cuda_model_destroy(h)
+            raise
         return h
 
 
@@ -533,6 +624,8 @@ def _train(backend, dataset, labels, weights, options, n_classes, **params):
         m.train_predictions = np.empty(dataset.rows, np.float64)
         check(lib.mpsb_cuda_model_train_predictions(h, ptr(m.train_predictions)))
         lib.mpsb_cuda_model_destroy(h)
+        if m.schema is None:
+            m.schema = _schema_of(dataset)
         models.append(m)
     return models
 
@@ -619,8 +712,11 @@ def train_forest(backend: CudaBackend, dataset: BinnedDataset, labels, weights=N
     del keep
     models = []
     for h in list(handles):
-        models.append(RegressionModel._from_handle(h))
+        m = RegressionModel._from_handle(h)
         lib.mpsb_cuda_model_destroy(h)
+        if m.schema is None:
+            m.schema = _schema_of(dataset)
+        models.append(m)
     return models
 
 

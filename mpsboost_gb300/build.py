@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmpsb_cuda.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["hist.cu", "kernels.cu", "host.cu", "node_entries.cu", "noalloc.cu", "binning.cu",
-           "quantize.cpp"]
+           "quantize.cpp", "model_io.cu"]
 
 
 def _nvcc() -> str:

@@ -80,9 +80,15 @@ __global__ void keys_kernel(const uint8_t* data, int scalar_type, uint64_t rs, u
   if (threadIdx.y == 0) miss[threadIdx.x] = 0;
   const uint32_t r0 = blockIdx.x * 32, f0 = blockIdx.y * 32;
   uint32_t err = 0;
+  // Lanes walk the matrix's contiguous direction: features for row-major input, rows for
+  // column-major input (the tile is indexed [row][feature] either way).
+  const bool row_major = cs < rs;
   for (uint32_t i = threadIdx.y; i < 32; i += blockDim.y) {
-    const uint32_t r = r0 + i, f = f0 + threadIdx.x;
-    tile[i][threadIdx.x] = (r < n && f < features) ? load_value(data, scalar_type, rs, cs, r, f, &err) : 0.0f;
+    const uint32_t r = row_major ? r0 + i : r0 + threadIdx.x;
+    const uint32_t f = row_major ? f0 + threadIdx.x : f0 + i;
+    const float v = (r < n && f < features) ? load_value(data, scalar_type, rs, cs, r, f, &err) : 0.0f;
+    if (row_major) tile[i][threadIdx.x] = v;
+    else tile[threadIdx.x][i] = v;
   }
   __syncthreads();
   for (uint32_t i = threadIdx.y; i < 32; i += blockDim.y) {

@@ -773,6 +773,20 @@ mpsb_cuda_model* export_model(mpsb_cuda_trainer* t, uint32_t tree_index,
   std::unique_ptr<mpsb_cuda_model> m(new mpsb_cuda_model);
   m->base = t->base_scores[tree_index];
   m->learning_rate = t->params.learning_rate;
+  m->objective = t->params.objective;
+  m->objective_alpha = t->params.objective_alpha;
+  m->tweedie_variance_power = t->params.tweedie_variance_power;
+  const mpsb_cuda_dataset* ds = t->ds;
+  if (ds->has_schema) {  // a device-quantized dataset carries the file's schema
+    m->has_schema = true;
+    m->features = ds->features;
+    m->max_bins = ds->max_bins;
+    m->boundaries = ds->boundaries;
+    m->boundary_offset = ds->boundary_offset;
+    m->boundary_count = ds->boundary_count;
+    m->bin_count = ds->h_bin_count;
+    m->missing_count = ds->missing_count;
+  }
   m->n_trees = rounds;
   m->trees.resize(rounds);
   for (uint32_t r = 0; r < rounds; ++r) {

@@ -117,5 +117,13 @@ struct mpsb_cuda_model {
   double base = 0.0, learning_rate = 0.1;
   std::vector<std::vector<mpsb_tree_node>> trees;
   std::vector<double> train_predictions;
+  // Objective metadata and the training data's quantization schema (the model file's).
+  uint32_t objective = 0;
+  double objective_alpha = 0.5, tweedie_variance_power = 1.5;
+  bool has_schema = false;
+  uint32_t features = 0, max_bins = 0;
+  std::vector<float> boundaries;
+  std::vector<uint64_t> boundary_offset, missing_count;
+  std::vector<uint32_t> boundary_count, bin_count;
 };
 

@@ -416,6 +416,35 @@ class Oracle:
             trees.append(nodes)
         return Model(self._fn("model_base_score")(out), trees, out.value, self)
 
+    # -- the reference's model file codec (reference only) --------------------------------
+    def model_to_bytes(self, model: Model) -> bytes:
+        """SerializeModel of a model trained by the compiled reference."""
+
+        if self.kind != "reference":
+            raise ValueError("only available with the compiled reference")
+        size = C.c_uint64()
+        self._check(self.lib.ref_model_serialize(C.c_void_p(model.handle), None, C.c_uint64(0), C.byref(size)))
+        out = np.empty(size.value, np.uint8)
+        self._check(self.lib.ref_model_serialize(C.c_void_p(model.handle), _ptr(out), C.c_uint64(out.size),
+                                                 C.byref(size)))
+        return out.tobytes()
+
+    def model_from_bytes(self, data: bytes) -> Model:
+        """DeserializeModel of the reference."""
+
+        if self.kind != "reference":
+            raise ValueError("only available with the compiled reference")
+        buf = np.frombuffer(bytes(data), np.uint8).copy()
+        out = C.c_void_p()
+        self._check(self.lib.ref_model_deserialize(_ptr(buf), C.c_uint64(buf.size), C.byref(out)))
+        count = self._fn("model_tree_count")(out)
+        trees = []
+        for t in range(count):
+            nodes = np.empty(self._fn("model_tree_node_count")(out, C.c_uint32(t)), NODE_DTYPE)
+            self._check(self._fn("model_tree_nodes")(out, C.c_uint32(t), _ptr(nodes)))
+            trees.append(nodes)
+        return Model(self._fn("model_base_score")(out), trees, out.value, self)
+
     # -- port-only hooks ---------------------------------------------------------------
     def _port_only(self):
         if self.kind != "port":

@@ -134,6 +134,11 @@ typedef struct {
 ORC_DECLARE_API(orc_)
 ORC_DECLARE_API(ref_)
 
+/* ---- ref_* only: the reference's model file codec (SerializeModel / DeserializeModel,
+   trainer.hpp:152-153), used to pin the library's model files ---- */
+int ref_model_serialize(const void* model, uint8_t* out, uint64_t capacity, uint64_t* size);
+int ref_model_deserialize(const uint8_t* data, uint64_t size, void** model_out);
+
 /* ---- orc_* only: the fixed-point replica and finer-grained hooks ---- */
 
 /* Power-of-two scale exponents of one round: q_g = rne(g * 2^kg), q_h = rne(h * 2^kh). */

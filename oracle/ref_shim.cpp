@@ -10,6 +10,7 @@
 //   TrainSingleRegressionTree             tree.hpp:104-108
 //   TrainRegressionModel                  trainer.hpp:133-139
 //   RegressionTree/RegressionModel::Predict
+//   SerializeModel / DeserializeModel     trainer.hpp:152-153
 #include <cstring>
 #include <exception>
 #include <string>
@@ -303,5 +304,20 @@ int ref_model_predict(const void* model, const void* dataset, double* out) {
 }
 
 void ref_model_free(void* model) { delete static_cast<RegressionModel*>(model); }
+
+int ref_model_serialize(const void* model, std::uint8_t* out, std::uint64_t capacity,
+                        std::uint64_t* size) {
+  return Guard([&] {
+    const std::vector<std::uint8_t> bytes = SerializeModel(*static_cast<const RegressionModel*>(model));
+    *size = bytes.size();
+    if (out != nullptr && capacity >= bytes.size()) std::memcpy(out, bytes.data(), bytes.size());
+  });
+}
+
+int ref_model_deserialize(const std::uint8_t* data, std::uint64_t size, void** model_out) {
+  return Guard([&] {
+    *model_out = new RegressionModel(DeserializeModel(std::vector<std::uint8_t>(data, data + size)));
+  });
+}
 
 }  // extern "C"

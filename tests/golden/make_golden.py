@@ -4,7 +4,9 @@ Run where the reference sources exist (``python tests/golden/make_golden.py``): 
 ``oracle/_ref/libmpsb_ref.so`` from those sources (oracle/Makefile) and records, for small
 seeded inputs stored verbatim in the file, the reference's quantization, histograms,
 single trees, boosted models and predictions. ``tests/test_golden.py`` replays every case
-against the plain-C oracle, so the oracle stays pinned where the reference is absent.
+against the plain-C oracle, so the oracle stays pinned where the reference is absent;
+each case also keeps the reference's model file bytes (SerializeModel), which
+``tests/test_model_io.py`` reads and rewrites.
 """
 
 from __future__ import annotations
@@ -97,6 +99,7 @@ def main():
                 base_score=float(model.base_score).hex(),
                 trees=[nodes_json(t) for t in model.trees],
                 pred=[float(v).hex() for v in model.predict(ds)],
+                model_file=ref.model_to_bytes(model).hex(),
             )
         )
     out = os.path.join(HERE, "reference_cases.json")

@@ -107,3 +107,21 @@ def test_quantize_at_scale(backend):
     x[:, 32:] = np.exp(x[:, 32:])
     x[rng.random(x.shape) < 0.02] = np.nan
     _same(mb.quantize_device(backend, x, 255), mb.quantize_dense(x, 255))
+
+
+def test_model_files_of_gpu_models(backend, tmp_path):
+    """GPU-trained models write the native model file with their training schema and
+    read back to the same predictions (device-quantized data carries the schema)."""
+    x = _matrix(16, 8_000, 9)
+    rng = np.random.default_rng(17)
+    y = np.nan_to_num(x[:, 0]) + rng.normal(size=x.shape[0]) * 0.1
+    params = dict(n_estimators=2, learning_rate=0.3, max_depth=4)
+    host = mb.quantize_dense(x, 64)
+    dev = mb.quantize_device(backend, x, 64)
+    a = mb.train_regressor(backend, host, y, **params)
+    b = mb.train_regressor(backend, dev, y, **params)
+    assert a.to_bytes() == b.to_bytes()  # same trees, same schema
+    path = tmp_path / "gpu.mpsb"
+    b.save(str(path))
+    c = mb.RegressionModel.load(str(path))
+    assert np.array_equal(c.predict(backend, host), a.train_predictions)

@@ -38,6 +38,9 @@
  *                                      (src/python/binding_model.cpp:34-45)
  *   mpsb_cuda_train_ovr                the one-vs-rest fit of
  *                                      src/mpsboost/estimators/multiclass.py:113-160
+ *   mpsb_cuda_train_softmax            TrainMulticlassSoftmaxModel (trainer.hpp:141-147)
+ *   mpsb_cuda_model_predict_margins    MulticlassModel::PredictMargins
+ *                                      (multiclass_trainer.cpp:212-235)
  *   mpsb_cuda_train_forest             the per-tree fits of _ForestMixin.fit
  *                                      (src/mpsboost/estimators/forest.py:101-183,
  *                                      forest_sampling.py:42-63): one single-round tree
@@ -297,11 +300,26 @@ int mpsb_cuda_dataset_schema(const mpsb_cuda_dataset* dataset, float* boundaries
    missing flags (may be NULL), as mpsb_quantize_dense lays them out. */
 int mpsb_cuda_dataset_export(const mpsb_cuda_dataset* dataset, uint8_t* bins, uint8_t* missing);
 
+/* Softmax models: class count (0 for a regression model), base scores, margins
+   [rows][class_count] of a binned dataset, and creation from host trees ordered
+   (round, class). */
+uint32_t mpsb_cuda_model_class_count(const mpsb_cuda_model* model);
+int mpsb_cuda_model_class_base_scores(const mpsb_cuda_model* model, double* out);
+int mpsb_cuda_model_predict_margins(mpsb_cuda_backend* backend, const mpsb_cuda_model* model,
+                                    const mpsb_cuda_dataset* dataset, double* out);
+int mpsb_cuda_model_class_labels(const mpsb_cuda_model* model, double* out);
+/* class_labels may be NULL (0..class_count-1); otherwise strictly increasing. */
+int mpsb_cuda_model_create_softmax(uint32_t class_count, double learning_rate,
+                                   const double* base_scores, const double* class_labels,
+                                   uint32_t n_trees, const uint32_t* node_counts,
+                                   const mpsb_tree_node* nodes, mpsb_cuda_model** out);
+
 /* ---- model files ----------------------------------------------------------------- */
 /* The reference's native model format (magic MPSBMOD, version 1.4, FNV-1a checksum),
    byte for byte: models written here load in the reference and the reference's load
    here (minor versions 0-4 are read). A model needs its training data's quantization
-   schema: models trained on a device-quantized dataset carry it; otherwise attach it
+   schema (softmax models are written as the multiclass kind):
+   models trained on a device-quantized dataset carry it; otherwise attach it
    with mpsb_cuda_model_set_schema (the arrays of mpsb_quantize_dense). Objective
    metadata comes from training (or mpsb_cuda_model_set_objective). Reading applies the
    reference's validation; violations are TrainingErrors (DataError for the schema). */
@@ -321,10 +339,13 @@ int mpsb_cuda_model_get_schema(const mpsb_cuda_model* model, uint32_t* features,
 /* *size receives the file size; out (capacity bytes) receives the bytes when not NULL. */
 int mpsb_cuda_model_serialize(const mpsb_cuda_model* model, uint8_t* out, uint64_t capacity,
                               uint64_t* size);
-int mpsb_cuda_model_deserialize(const uint8_t* data, uint64_t size, mpsb_cuda_model** out);
+/* kind: 0 = DeserializeModel (regression files only), 1 = DeserializeMulticlassModel
+   (multiclass files only), -1 = either. */
+int mpsb_cuda_model_deserialize(const uint8_t* data, uint64_t size, int kind,
+                                mpsb_cuda_model** out);
 /* Atomic save (temporary file in the same directory, fsync, rename) and load. */
 int mpsb_cuda_model_save(const mpsb_cuda_model* model, const char* path);
-int mpsb_cuda_model_load(const char* path, mpsb_cuda_model** out);
+int mpsb_cuda_model_load(const char* path, int kind, mpsb_cuda_model** out);
 
 /* ---- training ------------------------------------------------------------------ */
 /* weights may be NULL (unit weights). options: MPSB_OPT_* bits. */
@@ -338,6 +359,15 @@ int mpsb_cuda_train_ovr(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dat
                         const double* labels, const double* weights, uint64_t n,
                         uint32_t n_classes, const mpsb_train_params* params,
                         uint32_t options, mpsb_cuda_model** out);
+/* Native softmax boosting: per round one tree per class, in class order, each fitted to
+   the softmax gradients of the current margins (which include the earlier classes' trees
+   of the round). labels are class ids 0..class_count-1. The model holds class_count base
+   scores (log class priors), the trees ordered (round, class) and, as its training
+   predictions, the margins [n][class_count]. */
+int mpsb_cuda_train_softmax(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                            const double* labels, const double* weights, uint64_t n,
+                            const mpsb_train_params* params, uint32_t class_count,
+                            uint32_t options, mpsb_cuda_model** out);
 /* n_trees independent single-round trees (a random forest / extra-trees ensemble), the
    frontier of every tree of a batch built in the same launches. Tree t trains on the
    multiset of rows given by row_counts[t * n + r] (how many times row r is drawn: 0 for

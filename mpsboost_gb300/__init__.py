@@ -13,6 +13,7 @@ from .backend import (
     BinnedDataset,
     CudaBackend,
     DeviceBinnedDataset,
+    MulticlassModel,
     RegressionModel,
     Trainer,
     forest_samples,
@@ -22,6 +23,7 @@ from .backend import (
     train_forest,
     train_ovr,
     train_regressor,
+    train_softmax,
 )
 
 __all__ = [
@@ -31,6 +33,7 @@ __all__ = [
     "DataError",
     "DEFAULT_PARAMS",
     "DeviceBinnedDataset",
+    "MulticlassModel",
     "RegressionModel",
     "Trainer",
     "TrainingError",
@@ -42,4 +45,5 @@ __all__ = [
     "quantize_device",
     "train_ovr",
     "train_regressor",
+    "train_softmax",
 ]

@@ -150,9 +150,15 @@ SIGNATURES = {
     "mpsb_cuda_model_get_objective": (_I32, [_VP, _VP, _VP, _VP]),
     "mpsb_cuda_model_get_schema": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "mpsb_cuda_model_serialize": (_I32, [_VP, _VP, _U64, _VP]),
-    "mpsb_cuda_model_deserialize": (_I32, [_VP, _U64, C.POINTER(_VP)]),
+    "mpsb_cuda_model_deserialize": (_I32, [_VP, _U64, C.c_int, C.POINTER(_VP)]),
     "mpsb_cuda_model_save": (_I32, [_VP, C.c_char_p]),
-    "mpsb_cuda_model_load": (_I32, [C.c_char_p, C.POINTER(_VP)]),
+    "mpsb_cuda_model_load": (_I32, [C.c_char_p, C.c_int, C.POINTER(_VP)]),
+    "mpsb_cuda_train_softmax": (_I32, [_VP, _VP, _VP, _VP, _U64, C.POINTER(TrainParams), _U32, _U32, C.POINTER(_VP)]),
+    "mpsb_cuda_model_class_count": (_U32, [_VP]),
+    "mpsb_cuda_model_class_base_scores": (_I32, [_VP, _VP]),
+    "mpsb_cuda_model_predict_margins": (_I32, [_VP, _VP, _VP, _VP]),
+    "mpsb_cuda_model_class_labels": (_I32, [_VP, _VP]),
+    "mpsb_cuda_model_create_softmax": (_I32, [_U32, _F64, _VP, _VP, _U32, _VP, _VP, C.POINTER(_VP)]),
     "mpsb_cuda_train_ovr": (_I32, [_VP, _VP, _VP, _VP, _U64, _U32, C.POINTER(TrainParams), _U32, _VP]),
     "mpsb_cuda_train_forest": (_I32, [_VP, _VP, _VP, _VP, _U64, C.POINTER(TrainParams), _U32, _VP, _VP,
                                       _VP, _VP, _U32, _VP]),

@@ -539,7 +539,7 @@ class RegressionModel:
         lib = _lib.load()
         buf = np.frombuffer(bytes(data), np.uint8)
         h = C.c_void_p()
-        check(lib.mpsb_cuda_model_deserialize(ptr(buf) if buf.size else None, buf.size, C.byref(h)))
+        check(lib.mpsb_cuda_model_deserialize(ptr(buf) if buf.size else None, buf.size, 0, C.byref(h)))
         try:
             return cls._from_handle(h)
         finally:
@@ -559,7 +559,7 @@ class RegressionModel:
     def load(cls, path: str) -> "RegressionModel":
         lib = _lib.load()
         h = C.c_void_p()
-        check(lib.mpsb_cuda_model_load(os.fsencode(path), C.byref(h)))
+        check(lib.mpsb_cuda_model_load(os.fsencode(path), 0, C.byref(h)))
         try:
             return cls._from_handle(h)
         finally:
@@ -598,6 +598,121 @@ class RegressionModel:
             lib.mpsb_cuda_model_destroy(h)
             raise
         return h
+
+
+@dataclass
+class MulticlassModel:
+    """Native softmax model (MulticlassModel, trainer.hpp:87-131): per-class base scores
+    and trees ordered (round, class); margins[row, k] = base_k + lr * sum of class k's
+    trees."""
+
+    base_scores: np.ndarray
+    learning_rate: float
+    trees: list
+    train_margins: np.ndarray | None = None
+    schema: dict | None = None
+    class_labels: np.ndarray | None = None  # None: 0..K-1
+
+    @property
+    def class_count(self) -> int:
+        return int(self.base_scores.size)
+
+    @classmethod
+    def _from_handle(cls, handle) -> "MulticlassModel":
+        lib = _lib.load()
+        reg = RegressionModel._from_handle(handle)
+        base = np.empty(lib.mpsb_cuda_model_class_count(handle), np.float64)
+        check(lib.mpsb_cuda_model_class_base_scores(handle, ptr(base)))
+        labels = np.empty(base.size, np.float64)
+        check(lib.mpsb_cuda_model_class_labels(handle, ptr(labels)))
+        return cls(base, reg.learning_rate, reg.trees, schema=reg.schema, class_labels=labels)
+
+    def _handle(self, lib, dataset=None):
+        counts = np.asarray([len(t) for t in self.trees], np.uint32)
+        nodes = np.ascontiguousarray(np.concatenate(self.trees), dtype=NODE_DTYPE)
+        base = np.ascontiguousarray(self.base_scores, np.float64)
+        labels = None if self.class_labels is None else np.ascontiguousarray(self.class_labels, np.float64)
+        h = C.c_void_p()
+        check(lib.mpsb_cuda_model_create_softmax(base.size, self.learning_rate, ptr(base), ptr(labels),
+                                                 len(self.trees), ptr(counts), ptr(nodes), C.byref(h)))
+        try:
+            sc = _schema_of(dataset) if dataset is not None else self.schema
+            if sc is not None:
+                check(lib.mpsb_cuda_model_set_schema(
+                    h, sc["features"], sc["max_bins"], ptr(sc["boundaries"]), sc["boundaries"].size,
+                    ptr(sc["boundary_offsets"]), ptr(sc["boundary_counts"]), ptr(sc["bin_counts"]),
+                    ptr(sc["missing_counts"])))
+        except Exception:
+            lib.mpsb_cuda_model_destroy(h)
+            raise
+        return h
+
+    def predict_margins(self, backend: CudaBackend, dataset) -> np.ndarray:
+        """[rows, classes] margins on the device (MulticlassModel::PredictMargins)."""
+
+        lib = _lib.load()
+        dev = backend.dataset(dataset)
+        h = self._handle(lib)
+        out = np.empty((dataset.rows, self.class_count), np.float64)
+        try:
+            check(lib.mpsb_cuda_model_predict_margins(backend.handle, h, dev.handle, ptr(out)))
+        finally:
+            lib.mpsb_cuda_model_destroy(h)
+        return out
+
+    def predict_proba(self, backend: CudaBackend, dataset) -> np.ndarray:
+        m = self.predict_margins(backend, dataset)
+        e = np.exp(m - m.max(axis=1, keepdims=True))
+        return e / e.sum(axis=1, keepdims=True)
+
+    def to_bytes(self, dataset=None) -> bytes:
+        lib = _lib.load()
+        h = self._handle(lib, dataset)
+        try:
+            size = C.c_uint64()
+            check(lib.mpsb_cuda_model_serialize(h, None, 0, C.byref(size)))
+            out = np.empty(size.value, np.uint8)
+            check(lib.mpsb_cuda_model_serialize(h, ptr(out), out.size, C.byref(size)))
+        finally:
+            lib.mpsb_cuda_model_destroy(h)
+        return out.tobytes()
+
+    @classmethod
+    def from_bytes(cls, data: bytes) -> "MulticlassModel":
+        lib = _lib.load()
+        buf = np.frombuffer(bytes(data), np.uint8)
+        h = C.c_void_p()
+        check(lib.mpsb_cuda_model_deserialize(ptr(buf) if buf.size else None, buf.size, 1, C.byref(h)))
+        try:
+            return cls._from_handle(h)
+        finally:
+            lib.mpsb_cuda_model_destroy(h)
+
+
+def train_softmax(backend: CudaBackend, dataset, labels, n_classes: int, weights=None, *,
+                  hist_mode: str = "fixed", graph: bool = True, **params) -> MulticlassModel:
+    """Native softmax boosting (TrainMulticlassSoftmaxModel, multiclass_trainer.cpp:104-149):
+    each round fits one tree per class in class order on the device."""
+
+    dev = backend.dataset(dataset)
+    y = np.ascontiguousarray(labels, dtype=np.float64)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    params.setdefault("max_bins", dataset.max_bins)
+    p, keep = make_params(**params)
+    lib = _lib.load()
+    h = C.c_void_p()
+    check(lib.mpsb_cuda_train_softmax(backend.handle, dev.handle, ptr(y), ptr(w), y.size, C.byref(p),
+                                      int(n_classes), _options(hist_mode, True, graph), C.byref(h)))
+    del keep
+    try:
+        m = MulticlassModel._from_handle(h)
+        m.train_margins = np.empty((y.size, int(n_classes)), np.float64)
+        check(lib.mpsb_cuda_model_train_predictions(h, ptr(m.train_margins)))
+    finally:
+        lib.mpsb_cuda_model_destroy(h)
+    if m.schema is None:
+        m.schema = _schema_of(dataset)
+    return m
 
 
 def _train(backend, dataset, labels, weights, options, n_classes, **params):

@@ -364,6 +364,7 @@ struct mpsb_cuda_trainer {
   cudaGraph_t graph[2] = {nullptr, nullptr};
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
   bool root_reuse = false;  // the hessian does not depend on the prediction
+  uint32_t softmax_classes = 0;  // native softmax: one tree per class per round
   bool root_saved = false;  // a round has saved the roots' count/hessian histograms
   std::vector<cudaEvent_t> events;  // 2 per level (histogram build begin/end)
   unsigned long long* level_cells = nullptr;  // device: ctl->cells after each level's build
@@ -561,7 +562,7 @@ struct ForestSpec {
 void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
                    const double* labels, const double* weights, uint64_t n,
                    const mpsb_train_params* p, uint32_t options, uint32_t n_classes,
-                   const ForestSpec* forest = nullptr) {
+                   const ForestSpec* forest = nullptr, uint32_t softmax_classes = 0) {
   if (!b || !ds || !labels || !p) throw TrainingError("null argument");
   validate_training_params(*p);
   validate_tree_params(*p, ds->features);
@@ -603,6 +604,8 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.n_trees = T;
   a.objective = p->objective;
   a.ovr = t->ovr ? 1 : 0;
+  a.n_classes = softmax_classes;
+  t->softmax_classes = softmax_classes;
   a.mode = (options & MPSB_OPT_FLOAT_HIST) ? kModeFloat : kModeFixed;
   // Four features (warps) per split-scan CTA spread a shallow level's few nodes over many
   // SMs; MPSB_SCAN_THREADS overrides (a multiple of 32, at most 512).
@@ -625,7 +628,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   // Squared error and quantile have hessian = sample weight, the same in every round: the
   // roots' count and hessian histograms are built once per fit (MPSB_ROOT_REUSE=0 builds
   // them every round).
-  t->root_reuse = !forest && a.mode == kModeFixed && !(options & MPSB_OPT_PER_NODE) &&
+  t->root_reuse = !forest && !softmax_classes && a.mode == kModeFixed && !(options & MPSB_OPT_PER_NODE) &&
                   (p->objective == MPSB_SQUARED_ERROR || p->objective == MPSB_QUANTILE);
   if (const char* v = std::getenv("MPSB_ROOT_REUSE")) t->root_reuse = t->root_reuse && std::atoi(v) != 0;
   if (t->root_reuse) {
@@ -663,10 +666,37 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     CK(cudaMemcpyAsync(d_w, weights, n * sizeof(double), cudaMemcpyHostToDevice, s));
     a.weights = d_w;
   }
-  t->base_scores.resize(T);
+  if (softmax_classes) {
+    // Margins [K][n] from the class priors (WeightedClassBaseScores,
+    // multiclass_trainer.cpp:39-67); labels must be class ids (22-37).
+    const uint32_t K = softmax_classes;
+    const double total = validate_weights(weights, n);
+    std::vector<double> cw(K, 0.0);
+    for (uint64_t i = 0; i < n; ++i) {
+      const double y = labels[i];
+      if (!std::isfinite(y)) throw TrainingError("softmax labels must be finite");
+      if (std::floor(y) != y || y < 0.0 || y >= double(K))
+        throw TrainingError("softmax labels must be encoded class ids");
+      cw[uint32_t(y)] += weights ? weights[i] : 1.0;
+      if (!std::isfinite(cw[uint32_t(y)])) throw TrainingError("softmax class prior overflowed");
+    }
+    t->base_scores.resize(K);
+    for (uint32_t k = 0; k < K; ++k) {
+      t->base_scores[k] = std::log(std::max(1e-15, cw[k] / total));
+      if (!std::isfinite(t->base_scores[k])) throw TrainingError("softmax base score is not finite");
+    }
+    std::vector<double> init(static_cast<size_t>(n));
+    a.preds = t->alloc<double>(size_t(K) * n);
+    for (uint32_t k = 0; k < K; ++k) {
+      std::fill(init.begin(), init.end(), t->base_scores[k]);
+      CK(cudaMemcpyAsync(a.preds + size_t(k) * n, init.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+      CK(cudaStreamSynchronize(s));
+    }
+  }
+  if (!softmax_classes) t->base_scores.resize(T);
   std::vector<double> init(static_cast<size_t>(n));
-  a.preds = t->alloc<double>(size_t(T) * n);
-  for (uint32_t k = 0; k < T; ++k) {
+  if (!softmax_classes) a.preds = t->alloc<double>(size_t(T) * n);
+  for (uint32_t k = 0; k < T && !softmax_classes; ++k) {
     t->base_scores[k] = forest ? forest->base_scores[k]
                                : base_score(*p, labels, weights, n, t->ovr ? int64_t(k) : -1);
     std::fill(init.begin(), init.end(), t->base_scores[k]);
@@ -748,7 +778,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.scratch_prefix = t->alloc<uint32_t>(a.max_level_nodes);
   a.scratch_aux = t->alloc<uint32_t>(a.max_level_nodes);
   a.tree_scratch = t->alloc<uint32_t>(size_t(T) * 4);
-  a.max_rounds = p->n_estimators;
+  a.max_rounds = p->n_estimators * (softmax_classes ? softmax_classes : 1);
   a.model_nodes = t->alloc<TreeNodeOut>(size_t(a.max_rounds) * T * tree_nodes);
   a.model_counts = t->alloc<uint32_t>(size_t(a.max_rounds) * T);
   a.round_counter = t->alloc<uint32_t>(1);
@@ -802,6 +832,26 @@ mpsb_cuda_model* export_model(mpsb_cuda_trainer* t, uint32_t tree_index,
                   size_t(a.n_rows) * sizeof(double), cudaMemcpyDeviceToHost));
   }
   return m.release();
+}
+
+// A softmax model: K base scores, the trees of every (round, class) in that order, and
+// the training margins [rows][K].
+mpsb_cuda_model* export_softmax(mpsb_cuda_trainer* t) {
+  mpsb_cuda_model* m = export_model(t, 0, false);
+  const uint32_t K = t->softmax_classes;
+  const TrainerDev& a = t->dev;
+  m->class_count = K;
+  m->base_scores = t->base_scores;
+  m->base = 0.0;
+  m->class_labels.resize(K);
+  for (uint32_t k = 0; k < K; ++k) m->class_labels[k] = double(k);
+  std::vector<double> margins(size_t(K) * a.n_rows);
+  CK(cudaMemcpy(margins.data(), a.preds, margins.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  m->train_predictions.resize(margins.size());
+  for (uint32_t k = 0; k < K; ++k)
+    for (uint32_t r = 0; r < a.n_rows; ++r)
+      m->train_predictions[size_t(r) * K + k] = margins[size_t(k) * a.n_rows + r];
+  return m;
 }
 
 static_assert(sizeof(mpsb_tree_node) == sizeof(TreeNodeOut), "tree node layout");
@@ -895,6 +945,21 @@ int mpsb_cuda_train_ovr(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
     t->run(p->n_estimators);
     t->synchronize();
     for (uint32_t k = 0; k < n_classes; ++k) out[k] = export_model(t.get(), k);
+  });
+}
+
+int mpsb_cuda_train_softmax(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
+                            const double* labels, const double* weights, uint64_t n,
+                            const mpsb_train_params* p, uint32_t class_count, uint32_t options,
+                            mpsb_cuda_model** out) {
+  return guard([&] {
+    if (!out) throw TrainingError("null argument");
+    if (class_count < 2) throw TrainingError("softmax class_count must be at least two");
+    std::unique_ptr<mpsb_cuda_trainer> t(new mpsb_cuda_trainer);
+    setup_trainer(t.get(), b, ds, labels, weights, n, p, options, 0, nullptr, class_count);
+    t->run(p->n_estimators * class_count);
+    t->synchronize();
+    *out = export_softmax(t.get());
   });
 }
 
@@ -1032,32 +1097,113 @@ int mpsb_cuda_model_train_predictions(const mpsb_cuda_model* m, double* out) {
   });
 }
 
+}  // extern "C"
+
+namespace {
+
+// base + lr * sum of the given trees' leaves for every row, on the device.
+void predict_trees(mpsb_cuda_backend* b, const std::vector<const std::vector<mpsb_tree_node>*>& trees,
+                   double base, double lr, const mpsb_cuda_dataset* ds, double* out) {
+  std::vector<uint32_t> offsets(trees.size() + 1, 0);
+  for (size_t t = 0; t < trees.size(); ++t) {
+    offsets[t + 1] = offsets[t] + uint32_t(trees[t]->size());
+    for (const mpsb_tree_node& nd : *trees[t])
+      if (!(nd.flags & 1u) && nd.feature_index >= ds->features)
+        throw TrainingError("Prediction feature count does not match the tree model");
+  }
+  std::vector<mpsb_tree_node> flat(offsets.back() ? offsets.back() : 1);
+  for (size_t t = 0; t < trees.size(); ++t)
+    std::copy(trees[t]->begin(), trees[t]->end(), flat.begin() + offsets[t]);
+  DevBuf d_nodes, d_off, d_out;
+  d_nodes.alloc(flat.size() * sizeof(mpsb_tree_node));
+  d_off.alloc(offsets.size() * sizeof(uint32_t));
+  d_out.alloc(size_t(ds->n_rows) * sizeof(double));
+  cudaStream_t s = b->stream;
+  CK(cudaMemcpyAsync(d_nodes.p, flat.data(), flat.size() * sizeof(mpsb_tree_node), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_off.p, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, s));
+  CK(launch_predict(ds->bins_fm.as<uint8_t>(), ds->n_rows, ds->nfb, ds->has_missing.as<uint8_t>(),
+                    d_nodes.as<TreeNodeOut>(), d_off.as<uint32_t>(), uint32_t(trees.size()), base, lr,
+                    d_out.as<double>(), b->error.as<uint32_t>(), s));
+  CK(cudaMemcpyAsync(out, d_out.p, size_t(ds->n_rows) * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (b->take_error()) throw TrainingError("Tree node index is out of bounds or the structure contains a cycle");
+}
+
+}  // namespace
+
+extern "C" {
+
 int mpsb_cuda_model_predict(mpsb_cuda_backend* b, const mpsb_cuda_model* m,
                             const mpsb_cuda_dataset* ds, double* out) {
   return guard([&] {
+    if (m->class_count) throw TrainingError("a softmax model predicts margins (mpsb_cuda_model_predict_margins)");
     b->activate();
-    std::vector<uint32_t> offsets(m->trees.size() + 1, 0);
-    for (size_t t = 0; t < m->trees.size(); ++t) {
-      offsets[t + 1] = offsets[t] + uint32_t(m->trees[t].size());
-      for (const mpsb_tree_node& nd : m->trees[t])
-        if (!(nd.flags & 1u) && nd.feature_index >= ds->features)
-          throw TrainingError("Prediction feature count does not match the tree model");
+    std::vector<const std::vector<mpsb_tree_node>*> trees;
+    for (const auto& t : m->trees) trees.push_back(&t);
+    predict_trees(b, trees, m->base, m->learning_rate, ds, out);
+  });
+}
+
+int mpsb_cuda_model_predict_margins(mpsb_cuda_backend* b, const mpsb_cuda_model* m,
+                                    const mpsb_cuda_dataset* ds, double* out) {
+  return guard([&] {
+    if (!m->class_count) throw TrainingError("not a softmax model");
+    b->activate();
+    const uint32_t K = m->class_count;
+    std::vector<double> col(ds->n_rows);
+    for (uint32_t k = 0; k < K; ++k) {  // class k owns trees k, k + K, ... (PredictMargins)
+      std::vector<const std::vector<mpsb_tree_node>*> trees;
+      for (size_t t = k; t < m->trees.size(); t += K) trees.push_back(&m->trees[t]);
+      predict_trees(b, trees, m->base_scores[k], m->learning_rate, ds, col.data());
+      for (uint32_t r = 0; r < ds->n_rows; ++r) out[size_t(r) * K + k] = col[r];
     }
-    std::vector<mpsb_tree_node> flat(offsets.back() ? offsets.back() : 1);
-    for (size_t t = 0; t < m->trees.size(); ++t)
-      std::copy(m->trees[t].begin(), m->trees[t].end(), flat.begin() + offsets[t]);
-    DevBuf d_nodes, d_off, d_out;
-    d_nodes.alloc(flat.size() * sizeof(mpsb_tree_node));
-    d_off.alloc(offsets.size() * sizeof(uint32_t));
-    d_out.alloc(size_t(ds->n_rows) * sizeof(double));
-    cudaStream_t s = b->stream;
-    CK(cudaMemcpyAsync(d_nodes.p, flat.data(), flat.size() * sizeof(mpsb_tree_node), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(d_off.p, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, s));
-    CK(launch_predict(ds->bins_fm.as<uint8_t>(), ds->n_rows, ds->nfb, ds->has_missing.as<uint8_t>(),
-                      d_nodes.as<TreeNodeOut>(), d_off.as<uint32_t>(), uint32_t(m->trees.size()),
-                      m->base, m->learning_rate, d_out.as<double>(), b->error.as<uint32_t>(), s));
-    CK(cudaMemcpyAsync(out, d_out.p, size_t(ds->n_rows) * sizeof(double), cudaMemcpyDeviceToHost, s));
-    if (b->take_error()) throw TrainingError("Tree node index is out of bounds or the structure contains a cycle");
+  });
+}
+
+uint32_t mpsb_cuda_model_class_count(const mpsb_cuda_model* m) { return m->class_count; }
+
+int mpsb_cuda_model_class_base_scores(const mpsb_cuda_model* m, double* out) {
+  return guard([&] {
+    if (!m->class_count) throw TrainingError("not a softmax model");
+    std::copy(m->base_scores.begin(), m->base_scores.end(), out);
+  });
+}
+
+int mpsb_cuda_model_class_labels(const mpsb_cuda_model* m, double* out) {
+  return guard([&] {
+    if (!m->class_count) throw TrainingError("not a softmax model");
+    std::copy(m->class_labels.begin(), m->class_labels.end(), out);
+  });
+}
+
+int mpsb_cuda_model_create_softmax(uint32_t class_count, double lr, const double* base_scores,
+                                   const double* class_labels, uint32_t n_trees,
+                                   const uint32_t* counts, const mpsb_tree_node* nodes,
+                                   mpsb_cuda_model** out) {
+  return guard([&] {
+    if (class_count < 2 || n_trees == 0 || n_trees % class_count != 0 || !std::isfinite(lr) ||
+        lr <= 0.0 || lr > 1.0)
+      throw TrainingError("softmax model metadata is invalid");
+    std::unique_ptr<mpsb_cuda_model> m(new mpsb_cuda_model);
+    m->class_count = class_count;
+    m->learning_rate = lr;
+    m->base_scores.assign(base_scores, base_scores + class_count);
+    for (double v : m->base_scores)
+      if (!std::isfinite(v)) throw TrainingError("softmax model class metadata is not finite");
+    m->class_labels.resize(class_count);
+    for (uint32_t k = 0; k < class_count; ++k) {
+      m->class_labels[k] = class_labels ? class_labels[k] : double(k);
+      if (!std::isfinite(m->class_labels[k])) throw TrainingError("softmax model class metadata is not finite");
+      if (k > 0 && !(m->class_labels[k - 1] < m->class_labels[k]))
+        throw TrainingError("softmax model class labels must be strictly increasing");
+    }
+    m->n_trees = n_trees;
+    m->trees.resize(n_trees);
+    size_t off = 0;
+    for (uint32_t t = 0; t < n_trees; ++t) {
+      m->trees[t].assign(nodes + off, nodes + off + counts[t]);
+      off += counts[t];
+    }
+    *out = m.release();
   });
 }
 

@@ -117,6 +117,10 @@ struct mpsb_cuda_model {
   double base = 0.0, learning_rate = 0.1;
   std::vector<std::vector<mpsb_tree_node>> trees;
   std::vector<double> train_predictions;
+  // Native softmax models: class count (0 for regression), per-class base scores and
+  // class labels; trees are ordered (round, class).
+  uint32_t class_count = 0;
+  std::vector<double> base_scores, class_labels;
   // Objective metadata and the training data's quantization schema (the model file's).
   uint32_t objective = 0;
   double objective_alpha = 0.5, tweedie_variance_power = 1.5;

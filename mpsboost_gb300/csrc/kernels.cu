@@ -167,6 +167,32 @@ __device__ __forceinline__ bool objective_pair(uint32_t objective, double y, dou
   }
 }
 
+// ComputeMulticlassSoftmaxGradients for one row (objective.cpp:130-152, 242-287): the
+// class probability from the row's K margins (exp of each margin minus the maximum,
+// normalized by their sum in class order), g = p - [label == target], h = p (1 - p).
+__device__ __forceinline__ bool softmax_pair(const TrainerDev& a, double label, uint32_t row,
+                                             uint32_t target, double* g, double* h) {
+  const uint32_t K = a.n_classes;
+  if (!f64_finite(label) || floor(label) != label || label < 0.0 || label >= double(K)) return false;
+  double maximum = -INFINITY;
+  for (uint32_t k = 0; k < K; ++k) {
+    const double m = a.preds[size_t(k) * a.n_rows + row];
+    if (!f64_finite(m)) return false;
+    maximum = fmax(maximum, m);
+  }
+  double normalizer = 0.0, target_exp = 0.0;
+  for (uint32_t k = 0; k < K; ++k) {
+    const double e = exp(__dadd_rn(a.preds[size_t(k) * a.n_rows + row], -maximum));
+    normalizer = __dadd_rn(normalizer, e);
+    if (k == target) target_exp = e;
+  }
+  if (!f64_finite(normalizer) || normalizer <= 0.0) return false;
+  const double p = __ddiv_rn(target_exp, normalizer);
+  *g = __dadd_rn(p, uint32_t(label) == target ? -1.0 : 0.0);
+  *h = __dmul_rn(p, __dadd_rn(1.0, -p));
+  return f64_finite(*g) && f64_finite(*h) && *h >= 0.0;
+}
+
 // True for a double with the sign bit set and a non-zero magnitude (x < 0).
 __device__ __forceinline__ bool f64_negative(double x) {
   const long long b = __double_as_longlong(x);
@@ -179,7 +205,7 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
   const uint32_t t = blockIdx.y;
   const size_t tree_off = size_t(t) * a.n_rows;
   // Squared error and quantile have h = 1, so h * w = w exactly.
-  const bool unit_h = a.objective == 0 || a.objective == 2;
+  const bool unit_h = !a.n_classes && (a.objective == 0 || a.objective == 2);
   const long long class_bits = __double_as_longlong(double(t));
   uint32_t mg = 0, mh = 0, bad = 0;
   // Position p of the tree's root segment holds row i: the identity for boosting, the
@@ -197,9 +223,13 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
       const long long yb = __double_as_longlong(y);
       y = (yb == class_bits || (t == 0 && (yb << 1) == 0)) ? 1.0 : 0.0;
     }
-    const double pred = a.preds[tree_off + i];
     double g = 0.0, h = 0.0;
-    if (!objective_pair(a.objective, y, pred, a.params, &g, &h)) bad = 1;
+    if (a.n_classes) {
+      if (!softmax_pair(a, y, i, *a.round_counter % a.n_classes, &g, &h)) bad = 1;
+    } else {
+      const double pred = a.preds[tree_off + i];
+      if (!objective_pair(a.objective, y, pred, a.params, &g, &h)) bad = 1;
+    }
     if (a.weights != nullptr) {
       const double w = a.weights_per_tree ? a.weights[tree_off + i] : a.weights[i];
       g = __dmul_rn(g, w);
@@ -1355,7 +1385,9 @@ __global__ void apply_leaves_kernel(TrainerDev a) {
     const uint32_t start = (c - a.leaf_prefix[s]) * kApplyChunk;
     const uint32_t count = min(kApplyChunk, ls.seg_cnt - start);
     const uint32_t* rows = a.rows + (size_t(ls.tree) * 2 + ls.parity) * a.seg_stride + ls.seg_off + start;
-    double* pred = a.preds + size_t(ls.tree) * a.n_rows;
+    // Softmax trees update the margins of the current round's class.
+    const size_t pred_row = a.n_classes ? *a.round_counter % a.n_classes : ls.tree;
+    double* pred = a.preds + pred_row * a.n_rows;
     // lr * leaf is the same product for every row of a leaf.
     const double step = __dmul_rn(lr, ls.value);
     const double step_l = ls.split ? __dmul_rn(lr, ls.left_value) : step;

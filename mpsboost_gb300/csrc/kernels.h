@@ -75,6 +75,9 @@ struct TrainerDev {
   uint32_t items_per_sm;        // histogram work items per SM of the adaptive item size (0: 3)
   uint32_t mode;                // kModeFixed / kModeFloat
   uint32_t ovr;                 // labels are class ids; tree t fits class t (logistic)
+  uint32_t n_classes;           // native softmax: K classes, one tree per class in turn;
+                                // preds holds the margins [K][n_rows] and the round
+                                // counter modulo K is the class of the current tree
   uint32_t scan_threads;        // block size of the split scan (multiple of 32)
   // finalize scratch
   uint32_t* scratch_flags;      // [max_level_nodes]

@@ -36,6 +36,7 @@ namespace {
 constexpr uint8_t kMagic[8] = {'M', 'P', 'S', 'B', 'M', 'O', 'D', 0};
 constexpr uint16_t kMajor = 1, kMinor = 4;
 constexpr uint32_t kRegressionKind = 0;
+constexpr uint32_t kMulticlassKind = 1;
 constexpr size_t kHeaderBytes = 32;
 
 uint64_t fnv1a64(const uint8_t* p, size_t n) {
@@ -149,7 +150,24 @@ void validate_tree(const std::vector<mpsb_tree_node>& nodes, const mpsb_cuda_mod
   }
 }
 
+// MulticlassModel::Restore (multiclass_trainer.cpp:151-194).
+void validate_softmax(const mpsb_cuda_model& m) {
+  const uint32_t K = m.class_count;
+  if (K < 2 || m.base_scores.size() != K || m.class_labels.size() != K || m.trees.empty() ||
+      m.trees.size() % K != 0 || !std::isfinite(m.learning_rate) || m.learning_rate <= 0.0 ||
+      m.learning_rate > 1.0)
+    throw TrainingError("softmax model metadata is invalid");
+  for (uint32_t k = 0; k < K; ++k) {
+    if (!std::isfinite(m.base_scores[k]) || !std::isfinite(m.class_labels[k]))
+      throw TrainingError("softmax model class metadata is not finite");
+    if (k > 0 && !(m.class_labels[k - 1] < m.class_labels[k]))
+      throw TrainingError("softmax model class labels must be strictly increasing");
+  }
+  for (const auto& t : m.trees) validate_tree(t, m);
+}
+
 void validate_model(const mpsb_cuda_model& m) {
+  if (m.class_count) return validate_softmax(m);
   if (!std::isfinite(m.base) || !std::isfinite(m.learning_rate) || m.learning_rate <= 0.0 ||
       m.learning_rate > 1.0 || m.trees.empty())
     throw TrainingError("Model base score, learning rate, or tree count is invalid");
@@ -162,17 +180,7 @@ void validate_model(const mpsb_cuda_model& m) {
   for (const auto& t : m.trees) validate_tree(t, m);
 }
 
-std::vector<uint8_t> serialize(const mpsb_cuda_model& m) {
-  if (!m.has_schema) throw TrainingError("the model holds no quantization schema; attach the training data's");
-  validate_model(m);
-  Writer w;
-  w.u(m.features);
-  w.u(m.max_bins);
-  w.f64(m.base);
-  w.f64(m.learning_rate);
-  w.u(m.objective);
-  w.f64(m.objective_alpha);
-  w.f64(m.tweedie_variance_power);
+void write_schema_tail(Writer& w, const mpsb_cuda_model& m) {  // boundary count .. boundaries
   w.u(uint64_t(m.boundaries.size()));
   for (uint32_t f = 0; f < m.features; ++f) {
     w.u(m.boundary_offset[f]);
@@ -181,6 +189,30 @@ std::vector<uint8_t> serialize(const mpsb_cuda_model& m) {
     w.u(m.missing_count[f]);
   }
   for (float b : m.boundaries) w.f32(b);
+}
+
+std::vector<uint8_t> serialize(const mpsb_cuda_model& m) {
+  if (!m.has_schema) throw TrainingError("the model holds no quantization schema; attach the training data's");
+  validate_model(m);
+  Writer w;
+  if (m.class_count) {  // BuildPayload(MulticlassModel), model_payload.cpp
+    w.u(m.class_count);
+    w.f64(m.learning_rate);
+    for (double v : m.base_scores) w.f64(v);
+    for (double v : m.class_labels) w.f64(v);
+    w.u(m.features);
+    w.u(m.max_bins);
+    write_schema_tail(w, m);
+  } else {
+    w.u(m.features);
+    w.u(m.max_bins);
+    w.f64(m.base);
+    w.f64(m.learning_rate);
+    w.u(m.objective);
+    w.f64(m.objective_alpha);
+    w.f64(m.tweedie_variance_power);
+    write_schema_tail(w, m);
+  }
   w.u(uint32_t(m.trees.size()));
   for (const auto& t : m.trees) {
     w.u(uint32_t(t.size()));
@@ -200,14 +232,15 @@ std::vector<uint8_t> serialize(const mpsb_cuda_model& m) {
   for (uint8_t c : kMagic) h.u(c);
   h.u(kMajor);
   h.u(kMinor);
-  h.u(kRegressionKind);
+  h.u(m.class_count ? kMulticlassKind : kRegressionKind);
   h.u(uint64_t(w.out.size()));
   h.u(fnv1a64(w.out.data(), w.out.size()));
   h.out.insert(h.out.end(), w.out.begin(), w.out.end());
   return h.out;
 }
 
-mpsb_cuda_model* deserialize(const uint8_t* bytes, size_t size) {
+// expect: -1 either kind, 0 the regression loader, 1 the multiclass loader.
+mpsb_cuda_model* deserialize(const uint8_t* bytes, size_t size, int expect) {
   if (size < kHeaderBytes || std::memcmp(bytes, kMagic, 8) != 0)
     throw TrainingError("Model magic does not match or header is truncated");
   Reader hr{bytes + 8, size - 8};
@@ -217,23 +250,40 @@ mpsb_cuda_model* deserialize(const uint8_t* bytes, size_t size) {
   const uint64_t payload = hr.u<uint64_t>("payload size");
   const uint64_t checksum = hr.u<uint64_t>("checksum");
   if (major != kMajor) throw TrainingError("Model major version is unsupported");
-  if (kind != kRegressionKind) throw TrainingError("model kind is incompatible with regression loader");
+  if (expect == 0 && kind != kRegressionKind)
+    throw TrainingError("model kind is incompatible with regression loader");
+  if (expect == 1 && kind != kMulticlassKind)
+    throw TrainingError("model kind is incompatible with multiclass loader");
+  if (kind != kRegressionKind && kind != kMulticlassKind) throw TrainingError("model kind is unsupported");
   if (payload != size - kHeaderBytes) throw TrainingError("Model payload length does not match");
   const uint8_t* p = bytes + kHeaderBytes;
   if (fnv1a64(p, payload) != checksum) throw TrainingError("Model integrity check failed");
   Reader r{p, size_t(payload)};
   std::unique_ptr<mpsb_cuda_model> m(new mpsb_cuda_model);
-  m->features = r.u<uint32_t>("features");
-  m->max_bins = r.u<uint32_t>("max_bins");
-  m->base = r.f64("base_score");
-  m->learning_rate = r.f64("learning_rate");
-  if (minor >= 1) {
-    m->objective = r.u<uint32_t>("objective");
-    if (m->objective > 4) throw TrainingError("model objective is unsupported");
-  }
-  if (minor >= 4) {
-    m->objective_alpha = r.f64("objective_alpha");
-    m->tweedie_variance_power = r.f64("tweedie_variance_power");
+  if (kind == kMulticlassKind) {  // ParseMulticlassPayload, model_payload.cpp
+    if (minor < 3) throw TrainingError("multiclass model format is unsupported");
+    m->class_count = r.u<uint32_t>("class_count");
+    m->learning_rate = r.f64("learning_rate");
+    if (m->class_count > payload / 16) throw TrainingError("softmax model metadata is invalid");
+    m->base_scores.resize(m->class_count);
+    for (auto& v : m->base_scores) v = r.f64("softmax base_score");
+    m->class_labels.resize(m->class_count);
+    for (auto& v : m->class_labels) v = r.f64("softmax class label");
+    m->features = r.u<uint32_t>("features");
+    m->max_bins = r.u<uint32_t>("max_bins");
+  } else {
+    m->features = r.u<uint32_t>("features");
+    m->max_bins = r.u<uint32_t>("max_bins");
+    m->base = r.f64("base_score");
+    m->learning_rate = r.f64("learning_rate");
+    if (minor >= 1) {
+      m->objective = r.u<uint32_t>("objective");
+      if (m->objective > 4) throw TrainingError("model objective is unsupported");
+    }
+    if (minor >= 4) {
+      m->objective_alpha = r.f64("objective_alpha");
+      m->tweedie_variance_power = r.f64("tweedie_variance_power");
+    }
   }
   const uint64_t n_bounds = r.u<uint64_t>("boundary_count");
   if (n_bounds > payload / sizeof(float)) throw TrainingError("Model boundary_count exceeds the payload range");
@@ -421,10 +471,11 @@ int mpsb_cuda_model_serialize(const mpsb_cuda_model* m, uint8_t* out, uint64_t c
   });
 }
 
-int mpsb_cuda_model_deserialize(const uint8_t* data, uint64_t size, mpsb_cuda_model** out) {
+int mpsb_cuda_model_deserialize(const uint8_t* data, uint64_t size, int kind,
+                                mpsb_cuda_model** out) {
   return guard([&] {
     if (!data || !out) throw TrainingError("null argument");
-    *out = deserialize(data, size_t(size));
+    *out = deserialize(data, size_t(size), kind);
   });
 }
 
@@ -435,11 +486,11 @@ int mpsb_cuda_model_save(const mpsb_cuda_model* m, const char* path) {
   });
 }
 
-int mpsb_cuda_model_load(const char* path, mpsb_cuda_model** out) {
+int mpsb_cuda_model_load(const char* path, int kind, mpsb_cuda_model** out) {
   return guard([&] {
     if (!path || !out) throw TrainingError("null argument");
     const std::vector<uint8_t> bytes = read_file(path);
-    *out = deserialize(bytes.data(), bytes.size());
+    *out = deserialize(bytes.data(), bytes.size(), kind);
   });
 }
 

@@ -251,6 +251,26 @@ class Model:
             pass
 
 
+@dataclass
+class SoftmaxModel:
+    base_scores: np.ndarray
+    trees: list
+    handle: int
+    oracle: "Oracle"
+
+    def predict_margins(self, dataset: Dataset) -> np.ndarray:
+        out = np.empty((dataset.rows, self.base_scores.size), dtype=np.float64)
+        self.oracle._check(self.oracle._fn("softmax_predict_margins")(C.c_void_p(self.handle),
+                                                                      C.c_void_p(dataset.handle), _ptr(out)))
+        return out
+
+    def __del__(self):
+        try:
+            self.oracle._fn("softmax_free")(C.c_void_p(self.handle))
+        except Exception:
+            pass
+
+
 def _ptr(a: np.ndarray):
     return C.c_void_p(a.ctypes.data)
 
@@ -272,7 +292,8 @@ class Oracle:
         self.kind = kind
         self.lib = C.CDLL(path)
         getattr(self.lib, self.prefix + "last_error").restype = C.c_char_p
-        for name in ("tree_node_count", "model_tree_count", "model_tree_node_count"):
+        for name in ("tree_node_count", "model_tree_count", "model_tree_node_count", "softmax_tree_count",
+                     "softmax_class_count", "softmax_tree_node_count"):
             self._fn(name).restype = C.c_uint32
         self._fn("model_base_score").restype = C.c_double
 
@@ -416,6 +437,35 @@ class Oracle:
             trees.append(nodes)
         return Model(self._fn("model_base_score")(out), trees, out.value, self)
 
+    def train_softmax(self, dataset: Dataset, labels, n_classes: int, weights=None,
+                      hist_mode: int | None = None, **params) -> "SoftmaxModel":
+        """TrainMulticlassSoftmaxModel (multiclass_trainer.cpp:104-149)."""
+
+        y = np.ascontiguousarray(labels, dtype=np.float64)
+        w = np.ones_like(y) if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        params.setdefault("max_bins", dataset.max_bins)
+        p, keep = make_params(**params)
+        out = C.c_void_p()
+        if hist_mode is None or hist_mode == HIST_FP64 and self.kind == "reference":
+            rc = self._fn("train_softmax")(C.c_void_p(dataset.handle), _ptr(y), _ptr(w), C.c_uint64(y.size),
+                                           C.byref(p), C.c_uint32(n_classes), C.byref(out))
+        else:
+            self._port_only()
+            rc = self.lib.orc_train_softmax_mode(C.c_void_p(dataset.handle), _ptr(y), _ptr(w), C.c_uint64(y.size),
+                                                 C.byref(p), C.c_uint32(n_classes), C.c_int(hist_mode),
+                                                 C.byref(out))
+        self._check(rc)
+        del keep
+        k = self._fn("softmax_class_count")(out)
+        base = np.empty(k, np.float64)
+        self._check(self._fn("softmax_base_scores")(out, _ptr(base)))
+        trees = []
+        for t in range(self._fn("softmax_tree_count")(out)):
+            nodes = np.empty(self._fn("softmax_tree_node_count")(out, C.c_uint32(t)), NODE_DTYPE)
+            self._check(self._fn("softmax_tree_nodes")(out, C.c_uint32(t), _ptr(nodes)))
+            trees.append(nodes)
+        return SoftmaxModel(base, trees, out.value, self)
+
     # -- the reference's model file codec (reference only) --------------------------------
     def model_to_bytes(self, model: Model) -> bytes:
         """SerializeModel of a model trained by the compiled reference."""
@@ -428,6 +478,36 @@ class Oracle:
         self._check(self.lib.ref_model_serialize(C.c_void_p(model.handle), _ptr(out), C.c_uint64(out.size),
                                                  C.byref(size)))
         return out.tobytes()
+
+    def softmax_to_bytes(self, model: "SoftmaxModel") -> bytes:
+        """SerializeModel of a softmax model trained by the compiled reference."""
+
+        if self.kind != "reference":
+            raise ValueError("only available with the compiled reference")
+        size = C.c_uint64()
+        self._check(self.lib.ref_softmax_serialize(C.c_void_p(model.handle), None, C.c_uint64(0), C.byref(size)))
+        out = np.empty(size.value, np.uint8)
+        self._check(self.lib.ref_softmax_serialize(C.c_void_p(model.handle), _ptr(out), C.c_uint64(out.size),
+                                                   C.byref(size)))
+        return out.tobytes()
+
+    def softmax_from_bytes(self, data: bytes) -> "SoftmaxModel":
+        """DeserializeMulticlassModel of the reference."""
+
+        if self.kind != "reference":
+            raise ValueError("only available with the compiled reference")
+        buf = np.frombuffer(bytes(data), np.uint8).copy()
+        out = C.c_void_p()
+        self._check(self.lib.ref_softmax_deserialize(_ptr(buf), C.c_uint64(buf.size), C.byref(out)))
+        k = self._fn("softmax_class_count")(out)
+        base = np.empty(k, np.float64)
+        self._check(self._fn("softmax_base_scores")(out, _ptr(base)))
+        trees = []
+        for t in range(self._fn("softmax_tree_count")(out)):
+            nodes = np.empty(self._fn("softmax_tree_node_count")(out, C.c_uint32(t)), NODE_DTYPE)
+            self._check(self._fn("softmax_tree_nodes")(out, C.c_uint32(t), _ptr(nodes)))
+            trees.append(nodes)
+        return SoftmaxModel(base, trees, out.value, self)
 
     def model_from_bytes(self, data: bytes) -> Model:
         """DeserializeModel of the reference."""

@@ -1501,6 +1501,195 @@ int orc_model_predict(const void* m, const void* dataset, double* out) {
 }
 
 /* ------------------------------------------------------------------------------------
+ * Native softmax boosting (multiclass_trainer.cpp:104-149): per round, one tree per class
+ * in class order, each fitted to the softmax gradients of the current margins, which
+ * include the earlier classes' trees of the same round.
+ * ---------------------------------------------------------------------------------- */
+typedef struct {
+  uint32_t class_count;
+  double learning_rate;
+  double* base_scores;
+  uint32_t n_trees;
+  tree_t** trees;
+  uint32_t features, max_bins;
+  float* boundaries;
+  uint64_t n_boundaries;
+} softmax_t;
+
+void orc_softmax_free(void* m) {
+  softmax_t* model = (softmax_t*)m;
+  if (!model) return;
+  for (uint32_t i = 0; i < model->n_trees; ++i) orc_tree_free(model->trees[i]);
+  free(model->trees);
+  free(model->base_scores);
+  free(model->boundaries);
+  free(model);
+}
+
+/* ComputeMulticlassSoftmaxGradients + SoftmaxProbabilities (objective.cpp:130-152,
+   242-287): pairs for target_class from margins [rows][class_count]. */
+static int softmax_gradients(const double* labels, const double* margins, uint64_t n,
+                             uint32_t K, uint32_t target, double* probs, double* out) {
+  for (uint64_t r = 0; r < n; ++r) {
+    const double label = labels[r];
+    if (!isfinite(label)) return fail(ORC_TRAINING_ERROR, "softmax label must be finite");
+    if (floor(label) != label || label < 0.0 || label >= (double)K)
+      return fail(ORC_TRAINING_ERROR, "softmax labels must be encoded class ids");
+    double maximum = -INFINITY;
+    for (uint32_t k = 0; k < K; ++k) {
+      const double m = margins[r * K + k];
+      if (!isfinite(m)) return fail(ORC_TRAINING_ERROR, "softmax margin must be finite");
+      if (m > maximum) maximum = m;
+    }
+    double normalizer = 0.0;
+    for (uint32_t k = 0; k < K; ++k) {
+      probs[k] = exp(margins[r * K + k] - maximum);
+      normalizer += probs[k];
+    }
+    if (!isfinite(normalizer) || normalizer <= 0.0)
+      return fail(ORC_TRAINING_ERROR, "softmax normalizer must be finite and positive");
+    const double p = probs[target] / normalizer;
+    const double indicator = (uint32_t)label == target ? 1.0 : 0.0;
+    const double g = p - indicator, h = p * (1.0 - p);
+    if (!isfinite(g) || !isfinite(h) || h < 0.0)
+      return fail(ORC_TRAINING_ERROR, "softmax gradient/Hessian overflowed");
+    out[2 * r] = g;
+    out[2 * r + 1] = h;
+  }
+  return ORC_OK;
+}
+
+int orc_train_softmax_mode(const void* dataset, const double* labels, const double* weights,
+                           uint64_t n, const orc_params* p, uint32_t K, int hist_mode,
+                           void** out) {
+  const dataset_t* d = (const dataset_t*)dataset;
+  TRY(validate_training_params(p));
+  if (d->rows != n || d->max_bins != p->max_bins)
+    return fail(ORC_TRAINING_ERROR, "training data, labels, or max_bins contract mismatch");
+  double total;
+  TRY(validate_weights(weights, n, &total));
+  if (K < 2) return fail(ORC_TRAINING_ERROR, "softmax class_count must be at least two");
+  for (uint64_t r = 0; r < n; ++r) {  /* ValidateMulticlassLabels, multiclass_trainer.cpp:22-37 */
+    if (!isfinite(labels[r])) return fail(ORC_TRAINING_ERROR, "softmax labels must be finite");
+    if (floor(labels[r]) != labels[r] || labels[r] < 0.0 || labels[r] >= (double)K)
+      return fail(ORC_TRAINING_ERROR, "softmax labels must be encoded class ids");
+  }
+  softmax_t* m = (softmax_t*)calloc(1, sizeof(softmax_t));
+  m->class_count = K;
+  m->learning_rate = p->learning_rate;
+  m->features = d->features;
+  m->max_bins = d->max_bins;
+  m->n_boundaries = d->n_boundaries;
+  m->boundaries = (float*)malloc((d->n_boundaries ? d->n_boundaries : 1) * sizeof(float));
+  memcpy(m->boundaries, d->boundaries, d->n_boundaries * sizeof(float));
+  m->base_scores = (double*)calloc(K, sizeof(double));
+  m->trees = (tree_t**)calloc((size_t)p->n_estimators * K, sizeof(tree_t*));
+  int rc = ORC_OK;
+  /* WeightedClassBaseScores, multiclass_trainer.cpp:39-67. */
+  double* cw = (double*)calloc(K, sizeof(double));
+  for (uint64_t r = 0; r < n && rc == ORC_OK; ++r) {
+    const uint32_t c = (uint32_t)labels[r];
+    cw[c] += weights[r];
+    if (!isfinite(cw[c])) rc = fail(ORC_TRAINING_ERROR, "softmax class prior overflowed");
+  }
+  for (uint32_t k = 0; k < K && rc == ORC_OK; ++k) {
+    double prob = cw[k] / total;
+    if (prob < 1e-15) prob = 1e-15;
+    m->base_scores[k] = log(prob);
+    if (!isfinite(m->base_scores[k])) rc = fail(ORC_TRAINING_ERROR, "softmax base score is not finite");
+  }
+  free(cw);
+  double* margins = (double*)malloc(n * K * sizeof(double));
+  double* pairs = (double*)malloc(2 * n * sizeof(double));
+  float* pairs32 = (float*)malloc(2 * n * sizeof(float));
+  double* update = (double*)malloc(n * sizeof(double));
+  double* probs = (double*)malloc(K * sizeof(double));
+  for (uint64_t r = 0; r < n; ++r)
+    for (uint32_t k = 0; k < K; ++k) margins[r * K + k] = m->base_scores[k];
+  ctx_t x;
+  make_ctx(d, p, &x);
+  for (uint32_t round = 0; round < p->n_estimators && rc == ORC_OK; ++round) {
+    for (uint32_t k = 0; k < K && rc == ORC_OK; ++k) {
+      rc = softmax_gradients(labels, margins, n, K, k, probs, pairs);
+      if (rc == ORC_OK) rc = apply_sample_weights(pairs, weights, n);
+      if (rc != ORC_OK) break;
+      x.pairs = pairs;
+      x.mode.fixed = 0;
+      if (hist_mode == ORC_HIST_FIXED) {
+        for (uint64_t i = 0; i < 2 * n; ++i) pairs32[i] = (float)pairs[i];
+        rc = orc_fixed_scales(pairs32, n, &x.kg, &x.kh);
+        if (rc != ORC_OK) break;
+        x.pairs32 = pairs32;
+        x.mode.fixed = 1;
+        x.mode.inv_g = ldexp(1.0, -x.kg);
+        x.mode.inv_h = ldexp(1.0, -x.kh);
+      }
+      tree_t* t = NULL;
+      rc = train_tree(&x, &t);
+      if (rc != ORC_OK) break;
+      m->trees[m->n_trees++] = t;
+      rc = tree_predict(t, d, update);
+      for (uint64_t r = 0; r < n && rc == ORC_OK; ++r) {  /* AddClassUpdate */
+        double* margin = &margins[r * K + k];
+        *margin += p->learning_rate * update[r];
+        if (!isfinite(*margin)) rc = fail(ORC_TRAINING_ERROR, "softmax margin update overflowed");
+      }
+    }
+  }
+  free(x.offset);
+  free(margins); free(pairs); free(pairs32); free(update); free(probs);
+  if (rc != ORC_OK) { orc_softmax_free(m); return rc; }
+  *out = m;
+  return ORC_OK;
+}
+
+int orc_train_softmax(const void* dataset, const double* labels, const double* weights,
+                      uint64_t n, const orc_params* p, uint32_t K, void** out) {
+  return orc_train_softmax_mode(dataset, labels, weights, n, p, K, ORC_HIST_FP64, out);
+}
+
+uint32_t orc_softmax_tree_count(const void* m) { return ((const softmax_t*)m)->n_trees; }
+uint32_t orc_softmax_class_count(const void* m) { return ((const softmax_t*)m)->class_count; }
+int orc_softmax_base_scores(const void* m, double* out) {
+  const softmax_t* s = (const softmax_t*)m;
+  memcpy(out, s->base_scores, s->class_count * sizeof(double));
+  return ORC_OK;
+}
+uint32_t orc_softmax_tree_node_count(const void* m, uint32_t t) {
+  return ((const softmax_t*)m)->trees[t]->n;
+}
+int orc_softmax_tree_nodes(const void* m, uint32_t t, orc_tree_node* out) {
+  const softmax_t* s = (const softmax_t*)m;
+  if (t >= s->n_trees) return fail(ORC_OTHER_ERROR, "tree index out of range");
+  return orc_tree_nodes(s->trees[t], out);
+}
+
+/* MulticlassModel::PredictMargins, multiclass_trainer.cpp:212-235: [rows][class_count]. */
+int orc_softmax_predict_margins(const void* m, const void* dataset, double* out) {
+  const softmax_t* s = (const softmax_t*)m;
+  const dataset_t* d = (const dataset_t*)dataset;
+  if (d->features != s->features || d->max_bins != s->max_bins ||
+      d->n_boundaries != s->n_boundaries ||
+      memcmp(d->boundaries, s->boundaries, d->n_boundaries * sizeof(float)) != 0)
+    return fail(ORC_TRAINING_ERROR, "prediction data does not use the frozen model binning schema");
+  const uint32_t K = s->class_count;
+  for (uint64_t r = 0; r < d->rows; ++r)
+    for (uint32_t k = 0; k < K; ++k) out[r * K + k] = s->base_scores[k];
+  double* update = (double*)malloc(d->rows * sizeof(double));
+  for (uint32_t t = 0; t < s->n_trees; ++t) {
+    const int rc = tree_predict(s->trees[t], d, update);
+    if (rc != ORC_OK) { free(update); return rc; }
+    const uint32_t k = t % K;
+    for (uint64_t r = 0; r < d->rows; ++r) {
+      out[r * K + k] += s->learning_rate * update[r];
+      if (!isfinite(out[r * K + k])) { free(update); return fail(ORC_TRAINING_ERROR, "softmax margin update overflowed"); }
+    }
+  }
+  free(update);
+  return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------------------
  * Finer-grained hooks mirroring MpsBackend::ScanSplitsForTest / PartitionRowsForTest
  * (mps_split_partition.mm:14-236) with full reference semantics.
  * ---------------------------------------------------------------------------------- */

@@ -129,7 +129,18 @@ typedef struct {
   uint32_t P##model_tree_node_count(const void* model, uint32_t tree);               \
   int P##model_tree_nodes(const void* model, uint32_t tree, orc_tree_node* out);     \
   int P##model_predict(const void* model, const void* dataset, double* out);         \
-  void P##model_free(void* model);
+  void P##model_free(void* model);                                                   \
+  /* TrainMulticlassSoftmaxModel (trainer.hpp:141-147) and MulticlassModel */          \
+  int P##train_softmax(const void* dataset, const double* labels,                    \
+                       const double* weights, uint64_t n, const orc_params* params,  \
+                       uint32_t class_count, void** model_out);                      \
+  uint32_t P##softmax_tree_count(const void* model);                                 \
+  uint32_t P##softmax_class_count(const void* model);                                \
+  int P##softmax_base_scores(const void* model, double* out);                        \
+  uint32_t P##softmax_tree_node_count(const void* model, uint32_t tree);             \
+  int P##softmax_tree_nodes(const void* model, uint32_t tree, orc_tree_node* out);   \
+  int P##softmax_predict_margins(const void* model, const void* dataset, double* out); \
+  void P##softmax_free(void* model);
 
 ORC_DECLARE_API(orc_)
 ORC_DECLARE_API(ref_)
@@ -138,6 +149,8 @@ ORC_DECLARE_API(ref_)
    trainer.hpp:152-153), used to pin the library's model files ---- */
 int ref_model_serialize(const void* model, uint8_t* out, uint64_t capacity, uint64_t* size);
 int ref_model_deserialize(const uint8_t* data, uint64_t size, void** model_out);
+int ref_softmax_serialize(const void* model, uint8_t* out, uint64_t capacity, uint64_t* size);
+int ref_softmax_deserialize(const uint8_t* data, uint64_t size, void** model_out);
 
 /* ---- orc_* only: the fixed-point replica and finer-grained hooks ---- */
 
@@ -151,6 +164,9 @@ int orc_fixed_histograms(const void* dataset, const float* pairs32, int32_t kg,
 int orc_train_single_tree_fixed(const void* dataset, const float* pairs32, uint64_t n,
                                 int32_t kg, int32_t kh, const orc_params* params,
                                 void** tree_out);
+int orc_train_softmax_mode(const void* dataset, const double* labels, const double* weights,
+                           uint64_t n, const orc_params* params, uint32_t class_count,
+                           int hist_mode, void** model_out);
 int orc_train_regressor_mode(const void* dataset, const double* labels,
                              const double* weights, uint64_t n, const orc_params* params,
                              int hist_mode, void** model_out);

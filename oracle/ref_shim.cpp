@@ -9,6 +9,7 @@
 //   CpuReferenceBackend::BuildHistograms  backend.hpp:79-90
 //   TrainSingleRegressionTree             tree.hpp:104-108
 //   TrainRegressionModel                  trainer.hpp:133-139
+//   TrainMulticlassSoftmaxModel           trainer.hpp:141-147
 //   RegressionTree/RegressionModel::Predict
 //   SerializeModel / DeserializeModel     trainer.hpp:152-153
 #include <cstring>
@@ -305,12 +306,73 @@ int ref_model_predict(const void* model, const void* dataset, double* out) {
 
 void ref_model_free(void* model) { delete static_cast<RegressionModel*>(model); }
 
+int ref_train_softmax(const void* dataset, const double* labels, const double* weights,
+                      std::uint64_t n, const orc_params* params, std::uint32_t class_count,
+                      void** model_out) {
+  return Guard([&] {
+    CpuReferenceBackend backend;
+    *model_out = new MulticlassModel(TrainMulticlassSoftmaxModel(
+        DS(dataset), std::vector<double>(labels, labels + n),
+        std::vector<double>(weights, weights + n), Params(params), class_count, backend));
+  });
+}
+
+std::uint32_t ref_softmax_tree_count(const void* model) {
+  return static_cast<const MulticlassModel*>(model)->tree_count();
+}
+
+std::uint32_t ref_softmax_class_count(const void* model) {
+  return static_cast<const MulticlassModel*>(model)->class_count();
+}
+
+int ref_softmax_base_scores(const void* model, double* out) {
+  return Guard([&] {
+    const auto& b = static_cast<const MulticlassModel*>(model)->base_scores();
+    std::memcpy(out, b.data(), b.size() * sizeof(double));
+  });
+}
+
+std::uint32_t ref_softmax_tree_node_count(const void* model, std::uint32_t tree) {
+  return static_cast<std::uint32_t>(
+      static_cast<const MulticlassModel*>(model)->trees()[tree].nodes().size());
+}
+
+int ref_softmax_tree_nodes(const void* model, std::uint32_t tree, orc_tree_node* out) {
+  return Guard([&] {
+    CopyNodes(static_cast<const MulticlassModel*>(model)->trees().at(tree), out);
+  });
+}
+
+int ref_softmax_predict_margins(const void* model, const void* dataset, double* out) {
+  return Guard([&] {
+    const auto p = static_cast<const MulticlassModel*>(model)->PredictMargins(DS(dataset));
+    std::memcpy(out, p.data(), p.size() * sizeof(double));
+  });
+}
+
+void ref_softmax_free(void* model) { delete static_cast<MulticlassModel*>(model); }
+
 int ref_model_serialize(const void* model, std::uint8_t* out, std::uint64_t capacity,
                         std::uint64_t* size) {
   return Guard([&] {
     const std::vector<std::uint8_t> bytes = SerializeModel(*static_cast<const RegressionModel*>(model));
     *size = bytes.size();
     if (out != nullptr && capacity >= bytes.size()) std::memcpy(out, bytes.data(), bytes.size());
+  });
+}
+
+int ref_softmax_serialize(const void* model, std::uint8_t* out, std::uint64_t capacity,
+                          std::uint64_t* size) {
+  return Guard([&] {
+    const std::vector<std::uint8_t> bytes = SerializeModel(*static_cast<const MulticlassModel*>(model));
+    *size = bytes.size();
+    if (out != nullptr && capacity >= bytes.size()) std::memcpy(out, bytes.data(), bytes.size());
+  });
+}
+
+int ref_softmax_deserialize(const std::uint8_t* data, std::uint64_t size, void** model_out) {
+  return Guard([&] {
+    *model_out = new MulticlassModel(DeserializeMulticlassModel(std::vector<std::uint8_t>(data, data + size)));
   });
 }
 

@@ -248,3 +248,32 @@ def test_scale_properties(backend):
         assert t1.tobytes() == t2.tobytes()
     stats = t.stats()
     assert stats["rounds"] == 2 and stats["kernel_launches"] > 0 and stats["hist_cells"] >= n * f
+
+
+def test_softmax_against_replica(backend, port):
+    """Native softmax: K trees per round in class order, each on the margins updated by
+    the earlier classes. Base scores bit-exact; tree structures equal to the oracle's
+    fixed-point replica; leaves and margins within 1e-9 (the device's FP64 exp and the
+    host's may differ in the last bit)."""
+    rng = np.random.default_rng(46)
+    x = rng.normal(size=(6000, 7)).astype(np.float32)
+    x[rng.random(x.shape) < 0.05] = np.nan
+    y = (np.nan_to_num(x) @ rng.normal(size=(7, 4)) + rng.gumbel(size=(6000, 4))).argmax(1).astype(np.float64)
+    w = rng.uniform(0.5, 1.5, 6000)
+    params = dict(n_estimators=3, learning_rate=0.3, max_depth=5, min_samples_leaf=3)
+    binned = mb.quantize_dense(x, 64)
+    ds = port.quantize_dense(x, 64)
+    model = mb.train_softmax(backend, binned, y, 4, w, **params)
+    want = port.train_softmax(ds, y, 4, w, hist_mode=oracle.HIST_FIXED, **params)
+    assert model.base_scores.tobytes() == want.base_scores.tobytes()
+    assert len(model.trees) == 12
+    assert _structure(model.trees) == _structure(want.trees)
+    for got, exp in zip(model.trees, want.trees):
+        np.testing.assert_allclose(got["leaf_value"], exp["leaf_value"], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(model.train_margins, want.predict_margins(ds), rtol=1e-9, atol=1e-12)
+    assert model.predict_margins(backend, binned).tobytes() == model.train_margins.tobytes()
+    again = mb.train_softmax(backend, binned, y, 4, w, graph=False, **params)
+    for t1, t2 in zip(model.trees, again.trees):
+        assert t1.tobytes() == t2.tobytes()
+    with pytest.raises(mb.TrainingError, match="class"):
+        mb.train_softmax(backend, binned, y + 0.5, 4, **params)

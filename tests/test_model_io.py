@@ -255,3 +255,25 @@ def test_reads_older_minor_versions(minor, request):
     theirs = ref.model_from_bytes(old)
     for t1, t2 in zip(theirs.trees, model.trees):
         assert t1.tobytes() == np.ascontiguousarray(t2).tobytes()
+
+
+def test_softmax_bytes_equal_reference(reference):
+    rng = np.random.default_rng(77)
+    x = rng.normal(size=(400, 4)).astype(np.float32)
+    x[rng.random(x.shape) < 0.05] = np.nan
+    y = (np.nan_to_num(x) @ rng.normal(size=(4, 3)) + rng.gumbel(size=(400, 3))).argmax(1).astype(np.float64)
+    ds = reference.quantize_dense(x, 16)
+    model = reference.train_softmax(ds, y, 3, n_estimators=2, learning_rate=0.4, max_depth=3)
+    want = reference.softmax_to_bytes(model)
+    ours = mb.MulticlassModel(model.base_scores, 0.4, model.trees)
+    assert ours.to_bytes(ds) == want
+    back = mb.MulticlassModel.from_bytes(want)
+    assert back.base_scores.tobytes() == model.base_scores.tobytes()
+    assert np.array_equal(back.class_labels, [0.0, 1.0, 2.0])
+    for t1, t2 in zip(back.trees, model.trees):
+        assert t1.tobytes() == t2.tobytes()
+    theirs = reference.softmax_from_bytes(ours.to_bytes(ds))
+    for t1, t2 in zip(theirs.trees, model.trees):
+        assert t1.tobytes() == t2.tobytes()
+    with pytest.raises(mb.TrainingError, match="multiclass"):
+        mb.MulticlassModel.from_bytes(_golden_files()[0])

@@ -87,3 +87,24 @@ def test_gradients_match_reference(port, reference):
     p = rng.normal(size=500) * 3
     for obj in ("squared_error", "binary_logistic", "quantile", "poisson", "tweedie"):
         assert port.gradients(obj, y, p, 0.3, 1.4).tobytes() == reference.gradients(obj, y, p, 0.3, 1.4).tobytes()
+
+
+@pytest.mark.parametrize("nan,weighted,max_leaves", [(0.0, False, 0), (0.08, True, 0), (0.03, True, 5)])
+def test_softmax_port_matches_reference(port, reference, nan, weighted, max_leaves):
+    """TrainMulticlassSoftmaxModel: base scores, every (round, class) tree and the margins
+    bit for bit (both sides take exp and log from the same libm)."""
+    rng = np.random.default_rng(int(nan * 100) + max_leaves)
+    x = rng.normal(size=(500, 5)).astype(np.float32)
+    x[rng.random(x.shape) < nan] = np.nan
+    scores = np.nan_to_num(x) @ rng.normal(size=(5, 3)) + rng.gumbel(size=(500, 3))
+    y = scores.argmax(axis=1).astype(np.float64)
+    w = rng.uniform(0.5, 1.5, 500) if weighted else None
+    params = dict(n_estimators=3, learning_rate=0.3, max_depth=4, min_samples_leaf=2, max_leaves=max_leaves)
+    a = port.train_softmax(port.quantize_dense(x, 32), y, 3, w, **params)
+    ds = reference.quantize_dense(x, 32)
+    b = reference.train_softmax(ds, y, 3, w, **params)
+    assert a.base_scores.tobytes() == b.base_scores.tobytes()
+    assert len(a.trees) == len(b.trees) == 9
+    for t1, t2 in zip(a.trees, b.trees):
+        assert t1.tobytes() == t2.tobytes()
+    assert a.predict_margins(port.quantize_dense(x, 32)).tobytes() == b.predict_margins(ds).tobytes()

@@ -34,6 +34,8 @@ enum : uint32_t {
   kErrGradient = 1u << 7,        // invalid label / prediction / weight / gradient
   kErrPrefix = 1u << 8,          // prefix exceeded the non-missing parent (tree_split.cpp:212-214)
   kErrRootCache = 1u << 9,       // the hessian scale of a reused root histogram changed
+  kErrLeafQueue = 1u << 10,      // leaf-wise active queue beyond max_active_leaves
+                                 // (tree_leafwise.cpp:80-83, 130-134)
 };
 
 // Tree parameters resolved on the host (tree.hpp:47-72, tree_structure.cpp:54-62).
@@ -85,6 +87,15 @@ struct SplitRec {
 };
 static_assert(sizeof(SplitRec) % 8 == 0 && sizeof(SplitRec) / 8 <= 32,
               "a warp copies a SplitRec one 8-byte word per lane");
+
+// An active leaf of leaf-wise growth (ActiveNode, tree_internal.hpp:44-53): its node, the
+// row buffer holding its segment, and its best split once scanned.
+struct LeafActive {
+  NodeRec node;
+  SplitRec best;
+  uint32_t parity;
+  uint32_t scanned;
+};
 
 // Output tree node, layout of mpsb_tree_node.
 struct TreeNodeOut {

@@ -42,6 +42,7 @@ std::string describe_device_error(uint32_t bits) {
   if (bits & kErrGradient) m += " invalid label, prediction, weight or gradient;";
   if (bits & kErrPrefix) m += " non-missing histogram prefix exceeded parent;";
   if (bits & kErrRootCache) m += " hessian scale of the reused root histogram changed;";
+  if (bits & kErrLeafQueue) m += " leaf-wise active queue reached max_active_leaves;";
   return m;
 }
 
@@ -74,8 +75,7 @@ void validate_tree_params(const mpsb_train_params& p, uint32_t features) {  // t
         throw TrainingError("interaction constraint feature index out of range");
   }
   if (p.split_strategy > 1) throw TrainingError("unknown split strategy");
-  if (p.growth_strategy != 0)
-    throw UnsupportedError("the CUDA backend grows trees level-wise only (growth_strategy=level_wise)");
+  if (p.growth_strategy > 1) throw TrainingError("unknown growth strategy");
 }
 
 void validate_training_params(const mpsb_train_params& p) {  // trainer.cpp:22-42
@@ -363,6 +363,8 @@ struct mpsb_cuda_trainer {
   // hessian histograms.
   cudaGraph_t graph[2] = {nullptr, nullptr};
   cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  bool leafwise = false;   // growth_strategy leaf_wise: steps instead of depth levels
+  uint32_t lw_steps = 0;    // split steps per tree and round (max leaves - 1)
   bool root_reuse = false;  // the hessian does not depend on the prediction
   uint32_t softmax_classes = 0;  // native softmax: one tree per class per round
   bool root_saved = false;  // a round has saved the roots' count/hessian histograms
@@ -402,6 +404,12 @@ struct mpsb_cuda_trainer {
     CK(launch_round_begin(dev, s)); ++k;
     CK(launch_gradients(dev, std::max(1, std::min(grid(4), int((dev.seg_stride + 255) / 256))), s)); ++k;
     CK(launch_round_setup(dev, s)); ++k;
+    if (leafwise) {
+      k += enqueue_leafwise(root_gradient_only);
+      CK(launch_apply_leaves(dev, grid(8), s)); ++k;
+      CK(launch_round_end(dev, s)); ++k;
+      return k;
+    }
     const uint32_t levels = std::max<uint32_t>(depth, 1);
     for (uint32_t d = 0; d < levels; ++d) {
       const int parity = int(d & 1);
@@ -437,6 +445,37 @@ struct mpsb_cuda_trainer {
     }
     CK(launch_apply_leaves(dev, grid(8), s)); ++k;
     CK(launch_round_end(dev, s)); ++k;
+    return k;
+  }
+
+  // Leaf-wise round body: the root as a depth-0 level, then lw_steps split steps
+  // (select, partition, smaller-child histogram, subtraction, children's split scan,
+  // merge), then the leaf segments.
+  uint64_t enqueue_leafwise(bool root_gradient_only) {
+    cudaStream_t s = b->stream;
+    uint64_t k = 0;
+    CK(launch_zero_build_slots(dev, grid(8), s)); ++k;
+    TrainerDev view = level_view(0);
+    if (root_gradient_only) view.mode = kModeFixedG;
+    CK(launch_hist_build(view, hcfg, grid(1), s)); ++k;
+    if (root_reuse) {
+      CK(launch_root_cache(dev, root_gradient_only ? 0 : 1, grid(4), s)); ++k;
+    }
+    CK(launch_root_stats(dev, s)); ++k;
+    if (depth > 0) {
+      CK(launch_split_scan(dev, 0, grid(4), s)); ++k;
+    }
+    CK(launch_leafwise_init(dev, s)); ++k;
+    for (uint32_t step = 0; step < lw_steps && depth > 0; ++step) {
+      CK(launch_leafwise_select(dev, s)); ++k;
+      CK(launch_partition(dev, grid(4), s)); k += kPartitionKernels;
+      CK(launch_zero_build_slots(dev, grid(8), s)); ++k;
+      CK(launch_hist_build(dev, hcfg, grid(1), s)); ++k;
+      CK(launch_subtract(dev, grid(8), s)); ++k;
+      CK(launch_split_scan(dev, 1, grid(4), s)); ++k;
+      CK(launch_leafwise_merge(dev, s)); ++k;
+    }
+    CK(launch_leafwise_finish(dev, s)); ++k;
     return k;
   }
 
@@ -481,7 +520,7 @@ struct mpsb_cuda_trainer {
     b->activate();
     if (rounds_enqueued + rounds > dev.max_rounds)
       throw TrainingError("training session round capacity exceeded");
-    const bool timing = options & MPSB_OPT_TIMING;
+    const bool timing = (options & MPSB_OPT_TIMING) && !leafwise;  // events are per depth level
     // Events captured into a graph cannot be timed, so timing runs launch directly.
     const bool use_graph = !(options & (MPSB_OPT_NO_GRAPH | MPSB_OPT_PER_NODE | MPSB_OPT_TIMING));
     for (uint32_t r = 0; r < rounds; ++r) {
@@ -574,6 +613,9 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   t->params = *p;
   t->options = options;
   t->depth = p->max_depth;
+  t->leafwise = p->growth_strategy == 1;
+  if (t->leafwise && (forest || n_classes > 1024))
+    throw UnsupportedError("leaf-wise growth on the CUDA backend trains boosting, one-vs-rest (<= 1024 classes) and softmax models");
   t->ovr = n_classes > 0;
   t->n_trees = forest ? forest->n_trees : (t->ovr ? n_classes : 1);
   if (t->ovr && p->objective != MPSB_BINARY_LOGISTIC)
@@ -749,6 +791,26 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.trees = t->alloc<TreeState>(T);
   a.max_level_nodes = uint32_t(T * level_nodes);
   a.n_slots = a.max_level_nodes;
+  if (t->leafwise) {
+    // Active leaves <= leaves; each active leaf above max_depth keeps a histogram slot
+    // from its tree's stack (slot t is the root's).
+    const uint64_t max_active = p->max_active_leaves ? p->max_active_leaves : max_leaves_eff;
+    a.lw_max_leaves = uint32_t(std::min<uint64_t>(max_leaves_eff, 0xFFFFFFFFull));
+    a.lw_max_active = uint32_t(std::min<uint64_t>(max_active, 0xFFFFFFFFull));
+    a.lw_cap = uint32_t(std::min<uint64_t>(max_active, leaves) + 2);
+    a.lw_slot_cap = uint32_t(std::min<uint64_t>(max_active, leaves) + 1);
+    a.n_slots = T + T * a.lw_slot_cap;
+    a.max_level_nodes = std::max<uint32_t>(a.max_level_nodes, 2 * T);
+    a.lw_active = t->alloc<LeafActive>(size_t(T) * a.lw_cap);
+    a.lw_path = t->alloc<uint32_t>(size_t(T) * a.lw_cap * W);
+    a.lw_allowed = t->alloc<uint32_t>(size_t(T) * a.lw_cap * W);
+    a.lw_count = t->alloc<uint32_t>(T);
+    a.lw_done = t->alloc<uint32_t>(T);
+    a.lw_slots = t->alloc<uint32_t>(size_t(T) * a.lw_slot_cap);
+    a.lw_slot_top = t->alloc<uint32_t>(T);
+    a.lw_scan_map = t->alloc<uint32_t>(2 * size_t(T));
+    t->lw_steps = uint32_t(leaves > 0 ? leaves - 1 : 0);
+  }
   const uint64_t slot_words = uint64_t(F) * kSlots * 3;
   a.hist = t->alloc<unsigned long long>(uint64_t(a.n_slots) * slot_words);
   a.free_stack = t->alloc<uint32_t>(a.n_slots);

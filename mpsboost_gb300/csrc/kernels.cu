@@ -1371,6 +1371,310 @@ __global__ void __launch_bounds__(kPartThreads) partition_scatter_kernel(Trainer
 }
 
 // ------------------------------------------------------------------------------------
+// Leaf-wise growth (TrainLeafWiseRegressionTree, tree_leafwise.cpp:56-142)
+//
+// Each step splits, in every tree, the active leaf with the largest gain (the smaller
+// node index on equal gains); leaves at max_depth stay active but never split. A leaf's
+// best split depends only on its rows, so it is scanned once, when the leaf is created
+// (in fixed point the reference's re-evaluation reproduces the same split exactly). A
+// step is: select (this kernel: choose, ApplySplit, children, work lists), partition of
+// the chosen leaves, histogram of each smaller child, subtraction for its sibling, split
+// scan of the children, merge (the children's best splits into the active lists).
+// ------------------------------------------------------------------------------------
+__device__ SplitRec merged_split(const TrainerDev& a, uint32_t i) {
+  SplitRec b = a.partial[size_t(i) * a.n_fchunks];
+  for (uint32_t c = 1; c < a.n_fchunks; ++c) {
+    const SplitRec x = a.partial[size_t(i) * a.n_fchunks + c];
+    if (better_split(x, b)) b = x;
+  }
+  return b;
+}
+
+__device__ __forceinline__ SplitRec no_split() {
+  SplitRec b;
+  b.gain = 0.0;
+  b.valid = 0;
+  b.feature = b.threshold = 0;
+  b.default_left = 1;
+  return b;
+}
+
+// Root of every tree becomes its first active leaf (after the level-0 split scan).
+__global__ void leafwise_init_kernel(TrainerDev a) {
+  const TreeParams& P = a.params;
+  const uint32_t W = P.path_words, T = a.n_trees, S = a.lw_slot_cap;
+  for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) {
+    // Slot t holds the root (round_setup); the tree's other slots form its stack.
+    for (uint32_t j = 0; j < S; ++j) a.lw_slots[size_t(t) * S + j] = T + t * S + j;
+    a.lw_slot_top[t] = S;
+    LeafActive r;
+    r.node = a.nodes[0][t];
+    r.best = P.max_depth > 0 ? merged_split(a, t) : no_split();
+    r.parity = 0;
+    r.scanned = 1;
+    a.lw_active[size_t(t) * a.lw_cap] = r;
+    for (uint32_t w = 0; w < W; ++w) {
+      a.lw_path[size_t(t) * a.lw_cap * W + w] = 0;
+      a.lw_allowed[size_t(t) * a.lw_cap * W + w] = a.node_allowed[0][t * W + w];
+    }
+    a.lw_count[t] = 1;
+    a.lw_done[t] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(1024) leafwise_select_kernel(TrainerDev a) {
+  __shared__ uint32_t sh[33 * 3];
+  __shared__ unsigned long long built_rows;
+  const TreeParams& P = a.params;
+  const uint32_t W = P.path_words, cap = a.lw_cap, S = a.lw_slot_cap;
+  const uint32_t t = threadIdx.x;
+  if (t == 0) built_rows = 0;
+  __syncthreads();
+  uint32_t err = 0;
+  bool split = false, build = false;
+  uint32_t n_scan = 0, kid_at[2] = {0, 0};
+  PartEntry pe{};
+  BuildEntry be{};
+  SubEntry se{};
+  if (t < a.n_trees && !a.lw_done[t]) {
+    LeafActive* act = a.lw_active + size_t(t) * cap;
+    uint32_t* path = a.lw_path + size_t(t) * cap * W;
+    uint32_t* allowed = a.lw_allowed + size_t(t) * cap * W;
+    TreeState& ts = a.trees[t];
+    const uint32_t cnt = a.lw_count[t];
+    int best = -1;
+    if (cnt > a.lw_max_active) {
+      err |= kErrLeafQueue;
+    } else if (ts.leaf_count < a.lw_max_leaves) {
+      for (uint32_t j = 0; j < cnt; ++j) {  // IsBetterLeafWiseCandidate (tree_leafwise.cpp:16-27)
+        const LeafActive& l = act[j];
+        if (l.node.depth >= P.max_depth || !l.scanned || !l.best.valid) continue;
+        if (best < 0 || l.best.gain > act[best].best.gain ||
+            (l.best.gain == act[best].best.gain && l.node.node_index < act[best].node.node_index))
+          best = int(j);
+      }
+    }
+    if (best < 0) {
+      a.lw_done[t] = 1;
+    } else {
+      const LeafActive c = act[best];
+      const SplitRec& b = c.best;
+      TreeNodeOut* tn = a.tree_nodes + size_t(t) * a.max_tree_nodes;
+      const uint32_t li = ts.n_tree_nodes, ri = li + 1;
+      const uint32_t depth = c.node.depth + 1;
+      const bool grow = depth < P.max_depth;
+      if (ri >= a.max_tree_nodes || cnt + 2 > cap || (grow && a.lw_slot_top[t] == 0)) {
+        err |= kErrCapacity;
+        a.lw_done[t] = 1;
+      } else {
+        // ApplySplit (tree_structure.cpp:118-148).
+        double lv = 0.0, rv = 0.0;
+        if (!bounded_leaf(P, b.lg, b.lh, b.ll, b.lu, &lv)) err |= kErrNonFinite;
+        if (!bounded_leaf(P, b.rg, b.rh, b.rl, b.ru, &rv)) err |= kErrNonFinite;
+        write_leaf(&tn[li], lv);
+        write_leaf(&tn[ri], rv);
+        TreeNodeOut& pn = tn[c.node.node_index];
+        pn.feature_index = b.feature;
+        pn.threshold_bin = b.threshold;
+        pn.left_child = li;
+        pn.right_child = ri;
+        pn.leaf_value = 0.0;
+        pn.gain = b.gain;
+        pn.default_left = uint8_t(b.default_left);
+        pn.flags = 0;
+        ts.n_tree_nodes += 2;
+        ts.leaf_count += 1;
+        if (b.lcount + b.rcount != c.node.seg_cnt) err |= kErrPartition;
+        // Children in the other row buffer: left rows, then right rows (the partition).
+        const uint32_t np = c.parity ^ 1u;
+        const bool build_left = b.lcount <= b.rcount;
+        uint32_t new_slot = 0xffffffffu;
+        if (grow) new_slot = a.lw_slots[size_t(t) * S + --a.lw_slot_top[t]];
+        else a.lw_slots[size_t(t) * S + a.lw_slot_top[t]++] = c.node.slot;  // no child histograms
+        LeafActive kid[2];
+        for (int k = 0; k < 2; ++k) {
+          NodeRec& n = kid[k].node;
+          const bool left = k == 0;
+          n.seg_off = left ? c.node.seg_off : c.node.seg_off + uint32_t(b.lcount);
+          n.seg_cnt = uint32_t(left ? b.lcount : b.rcount);
+          n.node_index = left ? li : ri;
+          n.slot = !grow ? 0xffffffffu : ((left == build_left) ? new_slot : c.node.slot);
+          n.count = left ? b.lcount : b.rcount;
+          n.qg = left ? b.lqg : b.rqg;
+          n.qh = left ? b.lqh : b.rqh;
+          n.g = left ? b.lg : b.rg;
+          n.h = left ? b.lh : b.rh;
+          n.lo = left ? b.ll : b.rl;
+          n.hi = left ? b.lu : b.ru;
+          n.tree = t;
+          n.depth = depth;
+          kid[k].best = no_split();
+          kid[k].parity = np;
+          kid[k].scanned = grow ? 0u : 1u;
+        }
+        // Children's path and allowed words go to positions cnt, cnt + 1 (free), the
+        // chosen leaf's place takes the last leaf, then the children move down by one.
+        for (int k = 0; k < 2; ++k)
+          for (uint32_t w = 0; w < W; ++w) {
+            uint32_t pw = path[size_t(best) * W + w];
+            if ((b.feature >> 5) == w) pw |= 1u << (b.feature & 31);
+            path[size_t(cnt + k) * W + w] = pw;
+          }
+        for (uint32_t w = 0; w < W; ++w) {
+          uint32_t al = 0xffffffffu;
+          if (P.n_groups > 0) {  // InteractionAllowsFeature (tree_interactions.cpp:32-45)
+            al = 0;
+            for (uint32_t g = 0; g < P.n_groups; ++g) {
+              bool subset = true;
+              for (uint32_t u = 0; u < W && subset; ++u)
+                subset = (path[size_t(cnt) * W + u] & ~a.group_masks[g * W + u]) == 0;
+              if (subset) al |= a.group_masks[g * W + w];
+            }
+          }
+          if (a.tree_feature_masks != nullptr) al &= a.tree_feature_masks[t * W + w];
+          allowed[size_t(cnt) * W + w] = al;
+          allowed[size_t(cnt + 1) * W + w] = al;
+        }
+        const uint32_t last = cnt - 1;
+        if (uint32_t(best) != last) {
+          act[best] = act[last];
+          for (uint32_t w = 0; w < W; ++w) {
+            path[size_t(best) * W + w] = path[size_t(last) * W + w];
+            allowed[size_t(best) * W + w] = allowed[size_t(last) * W + w];
+          }
+        }
+        for (int k = 0; k < 2; ++k) {
+          act[last + k] = kid[k];
+          for (uint32_t w = 0; w < W; ++w) {
+            path[size_t(last + k) * W + w] = path[size_t(cnt + k) * W + w];
+            allowed[size_t(last + k) * W + w] = allowed[size_t(cnt + k) * W + w];
+          }
+        }
+        a.lw_count[t] = cnt + 1;
+        // Room for both children (tree_leafwise.cpp:130-134).
+        if (!(cnt - 1 + 2 <= a.lw_max_active || ts.leaf_count >= a.lw_max_leaves)) {
+          err |= kErrLeafQueue;
+          a.lw_done[t] = 1;
+        }
+        split = true;
+        pe.tree = t;
+        pe.parity = c.parity;
+        pe.seg_off = c.node.seg_off;
+        pe.seg_cnt = c.node.seg_cnt;
+        pe.feature = b.feature;
+        pe.threshold = b.threshold;
+        pe.default_left = b.default_left;
+        pe.lcount = uint32_t(b.lcount);
+        if (grow) {
+          build = true;
+          be.tree = t;
+          be.parity = np;
+          be.seg_off = build_left ? kid[0].node.seg_off : kid[1].node.seg_off;
+          be.seg_cnt = build_left ? kid[0].node.seg_cnt : kid[1].node.seg_cnt;
+          be.slot = new_slot;
+          be.pad = 0;
+          se.parent_slot = c.node.slot;
+          se.built_slot = new_slot;
+          atomicAdd(&built_rows, (unsigned long long)be.seg_cnt);
+          n_scan = 2;
+          kid_at[0] = last;
+          kid_at[1] = last + 1;
+        }
+      }
+    }
+  }
+  if (err) raise(a.ctl, err);
+  uint32_t v[3] = {split ? 1u : 0u, build ? 1u : 0u, n_scan};
+  uint32_t tot[3];
+  block_scan<3>(v, tot, sh);
+  if (split) a.part[v[0]] = pe;
+  if (build) {
+    a.build[v[1]] = be;
+    a.sub[v[1]] = se;
+  }
+  for (uint32_t k = 0; k < n_scan; ++k) {
+    const uint32_t s = v[2] + k;
+    a.nodes[1][s] = a.lw_active[size_t(t) * cap + kid_at[k]].node;
+    for (uint32_t w = 0; w < W; ++w)
+      a.node_allowed[1][size_t(s) * W + w] = a.lw_allowed[(size_t(t) * cap + kid_at[k]) * W + w];
+    a.lw_scan_map[s] = (t << 16) | kid_at[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // work lists of the step (few entries: one per tree)
+    Control* ctl = a.ctl;
+    uint32_t acc = 0;
+    for (uint32_t e = 0; e < tot[0]; ++e) {
+      a.part_prefix[e] = acc;
+      acc += ceil_div(a.part[e].seg_cnt, kPartChunk);
+    }
+    a.part_prefix[tot[0]] = acc;
+    ctl->n_part = tot[0];
+    ctl->part_chunks = acc;
+    const uint32_t item_rows =
+        a.item_rows ? a.item_rows : adaptive_item_rows(built_rows, a.nfb, a.sm_count, a.items_per_sm);
+    acc = 0;
+    for (uint32_t e = 0; e < tot[1]; ++e) {
+      a.build_prefix[e] = acc;
+      acc += ceil_div(a.build[e].seg_cnt, item_rows);
+    }
+    a.build_prefix[tot[1]] = acc;
+    ctl->n_build = tot[1];
+    ctl->n_sub = tot[1];
+    ctl->hist_items = acc * a.nfb;
+    ctl->hist_counter = 0;
+    ctl->item_rows = item_rows;
+    ctl->n_nodes = tot[2];
+    ctl->split_items = tot[2] * a.n_fchunks;
+  }
+}
+
+// The children's best splits into their active entries.
+__global__ void leafwise_merge_kernel(TrainerDev a) {
+  for (uint32_t s = threadIdx.x; s < a.ctl->n_nodes; s += blockDim.x) {
+    const uint32_t m = a.lw_scan_map[s];
+    LeafActive& l = a.lw_active[size_t(m >> 16) * a.lw_cap + (m & 0xFFFFu)];
+    l.best = merged_split(a, s);
+    l.scanned = 1;
+  }
+}
+
+// Every active leaf becomes a leaf segment of the prediction update.
+__global__ void leafwise_finish_kernel(TrainerDev a) {
+  if (threadIdx.x != 0) return;
+  Control* ctl = a.ctl;
+  uint32_t n = 0, chunks = 0, err = 0;
+  for (uint32_t t = 0; t < a.n_trees; ++t) {
+    const LeafActive* act = a.lw_active + size_t(t) * a.lw_cap;
+    const TreeNodeOut* tn = a.tree_nodes + size_t(t) * a.max_tree_nodes;
+    for (uint32_t j = 0; j < a.lw_count[t]; ++j) {
+      if (n >= a.max_leafsegs) {
+        err |= kErrCapacity;
+        break;
+      }
+      LeafSeg ls;
+      ls.tree = t;
+      ls.parity = act[j].parity;
+      ls.seg_off = act[j].node.seg_off;
+      ls.seg_cnt = act[j].node.seg_cnt;
+      ls.split = 0;
+      ls.feature = ls.threshold = ls.default_left = 0;
+      ls.value = tn[act[j].node.node_index].leaf_value;
+      ls.left_value = ls.right_value = 0.0;
+      a.leafseg[n] = ls;
+      a.leaf_prefix[n] = chunks;
+      chunks += ceil_div(ls.seg_cnt, kApplyChunk);
+      ++n;
+    }
+  }
+  a.leaf_prefix[n] = chunks;
+  ctl->n_leafseg = n;
+  ctl->leaf_chunks = chunks;
+  ctl->n_nodes = ctl->n_build = ctl->n_sub = ctl->n_part = 0;
+  ctl->hist_items = ctl->part_chunks = ctl->split_items = 0;
+  if (err) raise(ctl, err);
+}
+
+// ------------------------------------------------------------------------------------
 // Leaf application and round end
 // ------------------------------------------------------------------------------------
 __global__ void apply_leaves_kernel(TrainerDev a) {
@@ -1562,6 +1866,22 @@ cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStr
   const size_t smem = (sizeof(SplitRec) + 16 * 32 * sizeof(float)) * (threads / 32);
   if (a.mode == kModeFixed) split_scan_kernel<true><<<grid, threads, smem, s>>>(a, parity);
   else split_scan_kernel<false><<<grid, threads, smem, s>>>(a, parity);
+  return cudaGetLastError();
+}
+cudaError_t launch_leafwise_init(const TrainerDev& a, cudaStream_t s) {
+  leafwise_init_kernel<<<1, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_leafwise_select(const TrainerDev& a, cudaStream_t s) {
+  leafwise_select_kernel<<<1, 1024, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_leafwise_merge(const TrainerDev& a, cudaStream_t s) {
+  leafwise_merge_kernel<<<1, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch_leafwise_finish(const TrainerDev& a, cudaStream_t s) {
+  leafwise_finish_kernel<<<1, 32, 0, s>>>(a);
   return cudaGetLastError();
 }
 cudaError_t launch_finalize(const TrainerDev& a, int parity, uint32_t depth, cudaStream_t s) {

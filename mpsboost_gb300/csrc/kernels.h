@@ -92,6 +92,19 @@ struct TrainerDev {
   // Histogram item range of one launch: [item_begin, item_end); item_end 0 = the whole
   // level (ctl->hist_items). Per-node launches of the plain path set a node's range.
   uint32_t item_begin, item_end;
+  // Leaf-wise growth (growth_strategy 1; null for level-wise): per tree the active leaves
+  // with their interaction path and allowed-feature words, the active count, a done flag,
+  // and a private stack of histogram slots; the scanned children of a step map to
+  // (tree << 16 | active index).
+  LeafActive* lw_active;        // [n_trees][lw_cap]
+  uint32_t* lw_path;            // [n_trees][lw_cap][path_words]
+  uint32_t* lw_allowed;         // [n_trees][lw_cap][path_words]
+  uint32_t* lw_count;           // [n_trees]
+  uint32_t* lw_done;            // [n_trees]
+  uint32_t* lw_slots;           // [n_trees][lw_slot_cap] free slots
+  uint32_t* lw_slot_top;        // [n_trees]
+  uint32_t* lw_scan_map;        // [2 * n_trees]
+  uint32_t lw_cap, lw_slot_cap, lw_max_active, lw_max_leaves;
   // Root count/hessian histograms of the fit's first round: [n_trees][features][256]
   // {count, qh} and the hessian scale they were built with (null: not reused).
   unsigned long long* root_cache;
@@ -111,6 +124,13 @@ cudaError_t launch_gradients(const TrainerDev& a, int grid, cudaStream_t stream)
 cudaError_t launch_round_setup(const TrainerDev& a, cudaStream_t stream);
 cudaError_t launch_zero_build_slots(const TrainerDev& a, int grid, cudaStream_t stream);
 cudaError_t launch_root_stats(const TrainerDev& a, cudaStream_t stream);
+// Leaf-wise growth: after the root's split scan (init), per step (select before the
+// partition / histogram / subtraction / split scan of the chosen leaves' children, merge
+// after), and the leaf segments at the end (finish).
+cudaError_t launch_leafwise_init(const TrainerDev& a, cudaStream_t stream);
+cudaError_t launch_leafwise_select(const TrainerDev& a, cudaStream_t stream);
+cudaError_t launch_leafwise_merge(const TrainerDev& a, cudaStream_t stream);
+cudaError_t launch_leafwise_finish(const TrainerDev& a, cudaStream_t stream);
 // save != 0: copy the roots' count and hessian words into root_cache; else restore them
 // into the roots' slots (after a gradient-only build).
 cudaError_t launch_root_cache(const TrainerDev& a, int save, int grid, cudaStream_t stream);

@@ -1270,6 +1270,154 @@ static int make_ctx(const dataset_t* d, const orc_params* p, ctx_t* x) {
   return ORC_OK;
 }
 
+/* TrainLeafWiseRegressionTree, tree_leafwise.cpp:56-142: repeatedly split the active
+   leaf with the largest gain (the smaller node index on equal gains) until max_leaves;
+   leaves at max_depth stay active but never split. A leaf's best split depends only on
+   its own rows, so it is found once and kept until the leaf is split. */
+static int grow_leaf_wise(const ctx_t* x, tree_t* tree) {
+  const dataset_t* d = x->d;
+  const orc_params* p = x->p;
+  int rc = ORC_OK;
+  const uint32_t max_leaves = effective_max_leaves(p);
+  const uint32_t max_active = p->max_active_leaves ? p->max_active_leaves : max_leaves;
+  uint64_t cap = 16, n_act = 1;
+  active_t* act = (active_t*)calloc(cap, sizeof(active_t));
+  candidate_t* cand = (candidate_t*)calloc(cap, sizeof(candidate_t));
+  int* scored = (int*)calloc(cap, sizeof(int));
+  act[0].rows = (uint64_t*)malloc(d->rows * sizeof(uint64_t));
+  for (uint64_t r = 0; r < d->rows; ++r) act[0].rows[r] = r;
+  act[0].n_rows = d->rows;
+  act[0].lo = -INFINITY;
+  act[0].hi = INFINITY;
+  rc = sum_rows(x, act[0].rows, d->rows, &act[0].stats);
+  if (rc == ORC_OK) {
+    double leaf;
+    rc = bounded_leaf(p, &act[0].stats, -INFINITY, INFINITY, &leaf);
+    uint32_t idx;
+    if (rc == ORC_OK) rc = append_node(tree, leaf_node(leaf), &idx);
+  }
+  uint32_t leaf_count = 1;
+  stats_t* miss = (stats_t*)malloc(d->features * sizeof(stats_t));
+  while (rc == ORC_OK && n_act > 0 && leaf_count < max_leaves) {
+    if (n_act > max_active) { rc = fail(ORC_TRAINING_ERROR, "active leaf queue exceeded max_active_leaves"); break; }
+    int64_t best = -1;
+    for (uint64_t i = 0; i < n_act && rc == ORC_OK; ++i) {
+      active_t* a = &act[i];
+      if (a->depth >= p->max_depth) continue;
+      if (a->hist.fp == NULL && a->hist.fx == NULL) rc = build_hist(x, a->rows, a->n_rows, &a->hist);
+      if (rc != ORC_OK) break;
+      if (!scored[i]) {  /* PrepareSplitRows, tree_split.cpp:236-291 */
+        node_missing(x, a, &a->hist, miss);
+        rc = find_best_split(x, a, &a->hist, miss, &cand[i]);
+        scored[i] = 1;
+        if (rc != ORC_OK) break;
+      }
+      if (!cand[i].valid) continue;
+      /* IsBetterLeafWiseCandidate, tree_leafwise.cpp:16-27 */
+      if (best < 0 || cand[i].gain > cand[best].gain ||
+          (cand[i].gain == cand[best].gain && a->node_index < act[best].node_index)) {
+        /* The superseded best leaf's histogram was moved into the step's best slot and is
+           overwritten there (tree_leafwise.cpp:94-100): that leaf is rebuilt from its rows
+           the next time it is evaluated, and its split found again. */
+        if (best >= 0) {
+          free_hist(&act[best].hist);
+          memset(&act[best].hist, 0, sizeof act[best].hist);
+          scored[best] = 0;
+        }
+        best = (int64_t)i;
+      }
+    }
+    if (rc != ORC_OK || best < 0) break;
+    active_t chosen = act[best];
+    const candidate_t split = cand[best];
+    for (uint64_t i = (uint64_t)best; i + 1 < n_act; ++i) {  /* erase, order kept */
+      act[i] = act[i + 1];
+      cand[i] = cand[i + 1];
+      scored[i] = scored[i + 1];
+    }
+    --n_act;
+    uint64_t* lrows = (uint64_t*)malloc((split.left.count ? split.left.count : 1) * sizeof(uint64_t));
+    uint64_t* rrows = (uint64_t*)malloc((split.right.count ? split.right.count : 1) * sizeof(uint64_t));
+    uint64_t nl = 0, nr = 0;
+    for (uint64_t k = 0; k < chosen.n_rows; ++k) {
+      const uint64_t row = chosen.rows[k];
+      if (goes_left(d, row, split.feature, split.threshold, split.default_left)) {
+        if (nl < split.left.count) lrows[nl] = row;
+        ++nl;
+      } else {
+        if (nr < split.right.count) rrows[nr] = row;
+        ++nr;
+      }
+    }
+    if (nl != split.left.count || nr != split.right.count) {
+      free(lrows); free(rrows); free_active(&chosen);
+      rc = fail(ORC_TRAINING_ERROR, "Sample partition counts do not match histogram statistics");
+      break;
+    }
+    double lv = 0.0, rv = 0.0;  /* ApplySplit, tree_structure.cpp:118-148 */
+    uint32_t li = 0, ri = 0;
+    rc = bounded_leaf(p, &split.left, split.ll, split.lu, &lv);
+    if (rc == ORC_OK) rc = append_node(tree, leaf_node(lv), &li);
+    if (rc == ORC_OK) rc = bounded_leaf(p, &split.right, split.rl, split.ru, &rv);
+    if (rc == ORC_OK) rc = append_node(tree, leaf_node(rv), &ri);
+    if (rc != ORC_OK) { free(lrows); free(rrows); free_active(&chosen); break; }
+    orc_tree_node* parent = &tree->nodes[chosen.node_index];
+    parent->feature_index = split.feature;
+    parent->threshold_bin = split.threshold;
+    parent->left_child = li;
+    parent->right_child = ri;
+    parent->leaf_value = 0.0;
+    parent->gain = split.gain;
+    parent->default_left = (uint8_t)split.default_left;
+    parent->flags = 0;
+    ++leaf_count;
+    const uint32_t child_depth = chosen.depth + 1;
+    uint32_t* path = (uint32_t*)malloc((chosen.n_path + 1) * sizeof(uint32_t));
+    memcpy(path, chosen.path, chosen.n_path * sizeof(uint32_t));
+    uint32_t n_path = chosen.n_path;
+    int seen = 0;
+    for (uint32_t k = 0; k < n_path; ++k) seen |= path[k] == split.feature;
+    if (!seen) path[n_path++] = split.feature;
+    active_t L, R;
+    memset(&L, 0, sizeof L);
+    memset(&R, 0, sizeof R);
+    L.node_index = li; L.depth = child_depth; L.rows = lrows; L.n_rows = nl;
+    L.stats = split.left; L.lo = split.ll; L.hi = split.lu; L.path = path; L.n_path = n_path;
+    R.node_index = ri; R.depth = child_depth; R.rows = rrows; R.n_rows = nr;
+    R.stats = split.right; R.lo = split.rl; R.hi = split.ru;
+    R.path = (uint32_t*)malloc((n_path ? n_path : 1) * sizeof(uint32_t));
+    memcpy(R.path, path, n_path * sizeof(uint32_t));
+    R.n_path = n_path;
+    if (child_depth < p->max_depth) {  /* CacheChildHistograms, tree_leafwise.cpp:29-52 */
+      const int build_left = split.left.count <= split.right.count;
+      active_t* built = build_left ? &L : &R;
+      active_t* other = build_left ? &R : &L;
+      rc = build_hist(x, built->rows, built->n_rows, &built->hist);
+      if (rc == ORC_OK) rc = subtract_hist(x, &chosen.hist, &built->hist, &other->hist);
+    }
+    free_active(&chosen);
+    if (rc != ORC_OK) { free_active(&L); free_active(&R); break; }
+    if (!(n_act + 2 <= max_active || leaf_count >= max_leaves)) {
+      free_active(&L); free_active(&R);
+      rc = fail(ORC_TRAINING_ERROR, "leaf-wise active queue reached max_active_leaves");
+      break;
+    }
+    if (n_act + 2 > cap) {
+      cap *= 2;
+      act = (active_t*)realloc(act, cap * sizeof(active_t));
+      cand = (candidate_t*)realloc(cand, cap * sizeof(candidate_t));
+      scored = (int*)realloc(scored, cap * sizeof(int));
+    }
+    act[n_act] = L;
+    scored[n_act++] = 0;
+    act[n_act] = R;
+    scored[n_act++] = 0;
+  }
+  for (uint64_t i = 0; i < n_act; ++i) free_active(&act[i]);
+  free(act); free(cand); free(scored); free(miss);
+  return rc;
+}
+
 /* TrainSingleRegressionTree, tree.cpp:151-177. */
 static int train_tree(ctx_t* x, tree_t** out) {
   const orc_params* p = x->p;
@@ -1286,11 +1434,10 @@ static int train_tree(ctx_t* x, tree_t** out) {
       if (p->interaction_features[i] >= x->d->features)
         return fail(ORC_TRAINING_ERROR, "interaction constraint feature index out of range");
   }
-  if (p->growth_strategy != 0)
-    return fail(ORC_OTHER_ERROR, "leaf-wise growth is outside the restated hot path");
+  if (p->growth_strategy > 1) return fail(ORC_TRAINING_ERROR, "unknown growth strategy");
   tree_t* t = (tree_t*)calloc(1, sizeof(tree_t));
   t->features = x->d->features;
-  const int rc = grow_level_wise(x, t);
+  const int rc = p->growth_strategy == 1 ? grow_leaf_wise(x, t) : grow_level_wise(x, t);
   if (rc != ORC_OK) { free(t->nodes); free(t); return rc; }
   *out = t;
   return ORC_OK;

@@ -218,8 +218,6 @@ def test_training_errors(backend):
         mb.train_regressor(backend, binned, y, -w, n_estimators=1, max_depth=2)
     with pytest.raises(mb.TrainingError, match="learning_rate"):
         mb.train_regressor(backend, binned, y, learning_rate=0.0)
-    with pytest.raises(mb.UnsupportedError, match="level-wise"):
-        mb.train_regressor(backend, binned, y, growth_strategy="leaf_wise", n_estimators=1)
     with pytest.raises(mb.TrainingError, match="binary"):
         mb.train_regressor(backend, binned, y, objective="binary_logistic", n_estimators=1)
 
@@ -277,3 +275,68 @@ def test_softmax_against_replica(backend, port):
         assert t1.tobytes() == t2.tobytes()
     with pytest.raises(mb.TrainingError, match="class"):
         mb.train_softmax(backend, binned, y + 0.5, 4, **params)
+
+
+LEAFWISE_CASES = {
+    "max_leaves": dict(seed=61, rows=6000, feats=8, nan=0.05, ints=2, max_bins=128,
+                       params=dict(n_estimators=3, learning_rate=0.2, max_depth=6, max_leaves=12)),
+    "depth_bound": dict(seed=62, rows=4000, feats=6, nan=0.0, ints=0, max_bins=64,
+                        params=dict(n_estimators=2, learning_rate=0.3, max_depth=4)),
+    "deep": dict(seed=63, rows=20000, feats=20, nan=0.02, ints=3, max_bins=255,
+                 params=dict(n_estimators=2, learning_rate=0.1, max_depth=10, max_leaves=40,
+                             min_samples_leaf=5)),
+    "monotone": dict(seed=64, rows=3000, feats=4, nan=0.0, ints=0, max_bins=64,
+                     params=dict(n_estimators=2, learning_rate=0.3, max_depth=6, max_leaves=9,
+                                 monotonic_constraints=[1, 0, -1, 0])),
+    "interaction": dict(seed=65, rows=3000, feats=6, nan=0.0, ints=0, max_bins=64,
+                        params=dict(n_estimators=2, learning_rate=0.3, max_depth=6, max_leaves=16,
+                                    max_active_leaves=16, interaction_constraints=[[0, 1], [1, 2, 3], [4, 5]])),
+    "regularized": dict(seed=66, rows=3000, feats=5, nan=0.1, ints=1, max_bins=64,
+                        params=dict(n_estimators=2, learning_rate=0.3, max_depth=5, max_leaves=10,
+                                    reg_lambda=2.0, reg_alpha=0.2, min_child_weight=0.5, gamma=0.001)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LEAFWISE_CASES))
+def test_leafwise_bit_exact_to_replica(backend, port, name):
+    """Leaf-wise growth (tree_leafwise.cpp:56-142): every node, leaf value and training
+    prediction equal the oracle's fixed-point replica."""
+    c = LEAFWISE_CASES[name]
+    x, y, w = _data(c["seed"], c["rows"], c["feats"], c["nan"], c["ints"])
+    params = dict(c["params"], growth_strategy="leaf_wise")
+    binned = mb.quantize_dense(x, c["max_bins"])
+    model = mb.train_regressor(backend, binned, y, w, **params)
+    ds = port.quantize_dense(x, c["max_bins"])
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FIXED, **params)
+    assert len(model.trees) == len(want.trees)
+    for got, exp in zip(model.trees, want.trees):
+        assert got.tobytes() == exp.tobytes()
+    assert model.train_predictions.tobytes() == want.predict(ds).tobytes()
+
+
+def test_leafwise_ovr_and_softmax(backend, port):
+    rng = np.random.default_rng(67)
+    x = rng.normal(size=(5000, 6)).astype(np.float32)
+    x[rng.random(x.shape) < 0.03] = np.nan
+    y = (np.nan_to_num(x) @ rng.normal(size=(6, 3)) + rng.gumbel(size=(5000, 3))).argmax(1).astype(np.float64)
+    binned = mb.quantize_dense(x, 64)
+    params = dict(n_estimators=2, learning_rate=0.3, max_depth=5, max_leaves=10, min_samples_leaf=3,
+                  growth_strategy="leaf_wise")
+    models = mb.train_ovr(backend, binned, y, 3, **params)
+    for k, m in enumerate(models):
+        single = mb.train_regressor(backend, binned, (y == k).astype(np.float64), objective="binary_logistic", **params)
+        for t1, t2 in zip(m.trees, single.trees):
+            assert t1.tobytes() == t2.tobytes()
+    soft = mb.train_softmax(backend, binned, y, 3, **params)
+    want = port.train_softmax(port.quantize_dense(x, 64), y, 3, hist_mode=oracle.HIST_FIXED, **params)
+    assert _structure(soft.trees) == _structure(want.trees)
+
+
+def test_leafwise_active_queue_limit(backend, port):
+    """max_active_leaves below the leaves the growth needs fails as in the reference."""
+    x, y, w = _data(68, 3000, 5)
+    params = dict(n_estimators=1, max_depth=6, max_active_leaves=4, growth_strategy="leaf_wise")
+    with pytest.raises(oracle.OracleError, match="max_active_leaves"):
+        port.train_regressor(port.quantize_dense(x, 32), y, w, hist_mode=oracle.HIST_FIXED, **params)
+    with pytest.raises(mb.TrainingError, match="max_active_leaves"):
+        mb.train_regressor(backend, mb.quantize_dense(x, 32), y, w, **params)

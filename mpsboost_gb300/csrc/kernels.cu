@@ -193,6 +193,12 @@ __device__ __forceinline__ bool softmax_pair(const TrainerDev& a, double label, 
   return f64_finite(*g) && f64_finite(*h) && *h >= 0.0;
 }
 
+// x / y for the split screen: the fast reciprocal division (within 2 ulp) where the
+// divisor is a normal float below 2^125, the IEEE division elsewhere.
+__device__ __forceinline__ float screen_div(float x, float y) {
+  return (y > 0x1p-125f && y < 0x1p125f) ? __fdividef(x, y) : __fdiv_rn(x, y);
+}
+
 // True for a double with the sign bit set and a non-zero magnitude (x < 0).
 __device__ __forceinline__ bool f64_negative(double x) {
   const long long b = __double_as_longlong(x);
@@ -705,8 +711,9 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
                       node.node_index, node.depth, nb - 1)
                 : 0xffffffffu;
         // Exact FP32 pre-screen. Every eligible candidate's score S = gL^2/(hL+lambda) +
-        // gR^2/(hR+lambda) is computed in FP32 with relative error <= 13u (u = 2^-24; each
-        // int64 -> FP32 conversion below is within 3u, lambda is rounded once). A candidate
+        // gR^2/(hR+lambda) is computed in FP32 with relative error <= 14u (u = 2^-24; each
+        // int64 -> FP32 conversion below is within 3u, lambda is rounded once, a division
+        // within 2u). A candidate
         // whose FP32 score is below M(1 - 2^-18), M the warp's best FP32 score over certainly
         // eligible candidates, then has an exact score at least 30u*M below that candidate's,
         // far outside the FP64 evaluation's own rounding (a few 2^-53 * M, the parent score
@@ -753,7 +760,7 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
             if (lh <= hi || rh <= hi) cls = 2;
           }
           const float lg = to32(cl.g, inv_g32), rg = to32(cr.g, inv_g32);
-          const float sc = __fdiv_rn(lg * lg, lh + lam32) + __fdiv_rn(rg * rg, rh + lam32);
+          const float sc = screen_div(lg * lg, lh + lam32) + screen_div(rg * rg, rh + lam32);
           if (!isfinite(sc)) cls = 2;
           *s32 = sc;
           return cls;
@@ -1260,17 +1267,23 @@ __global__ void __launch_bounds__(kPartThreads) partition_count_kernel(TrainerDe
     const uint32_t count = min(kPartChunk, pe.seg_cnt - start);
     const uint32_t* rows = a.rows + (size_t(pe.tree) * 2 + pe.parity) * a.seg_stride + pe.seg_off + start;
     uint32_t mine = 0;
+    // All row ids, then all bin gathers, then the stores: nothing in flight waits on a
+    // store that might alias it.
+    uint32_t r[kPartPerThread];
 #pragma unroll
     for (int k = 0; k < kPartPerThread; ++k) {
       const uint32_t p = uint32_t(k * kPartThreads) + threadIdx.x;
-      bool left = false;
-      if (p < count) {
-        const uint32_t r = rows[p];
-        left = r < a.n_rows && row_goes_left(a, r, pe.feature, pe.threshold, pe.default_left);
-      }
-      const uint32_t word = __ballot_sync(0xffffffffu, left);
+      r[k] = p < count ? __ldg(rows + p) : 0xffffffffu;
+    }
+    bool left[kPartPerThread];
+#pragma unroll
+    for (int k = 0; k < kPartPerThread; ++k)
+      left[k] = r[k] < a.n_rows && row_goes_left(a, r[k], pe.feature, pe.threshold, pe.default_left);
+#pragma unroll
+    for (int k = 0; k < kPartPerThread; ++k) {
+      const uint32_t word = __ballot_sync(0xffffffffu, left[k]);
       if (lane == 0) a.part_flags[size_t(c) * (kPartChunk / 32) + k * (kPartThreads / 32) + warp] = word;
-      mine += left;
+      mine += left[k];
     }
     for (int off = 16; off > 0; off >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, off);
     if (lane == 0) warp_counts[warp] = mine;
@@ -1346,20 +1359,28 @@ __global__ void __launch_bounds__(kPartThreads) partition_scatter_kernel(Trainer
     float2* gh_dst = a.gh_ordered ? a.gh + dst_off : nullptr;
     const uint32_t left_before_chunk = a.part_offsets[c];
     const uint32_t right_before_chunk = start - left_before_chunk;
+    // Loads first (flag words, row ids, g/h), then the stores.
+    uint32_t word[kPartPerThread], r[kPartPerThread];
+    float2 g[kPartPerThread];
+#pragma unroll
+    for (int k = 0; k < kPartPerThread; ++k) {
+      const uint32_t p = uint32_t(k * kPartThreads) + threadIdx.x;
+      word[k] = __ldg(flags + k * (kPartThreads / 32) + warp);
+      r[k] = p < count ? __ldg(src + p) : 0u;
+      g[k] = (p < count && a.gh_ordered) ? __ldg(gh_src + p) : make_float2(0.f, 0.f);
+    }
 #pragma unroll
     for (int k = 0; k < kPartPerThread; ++k) {
       const uint32_t p = uint32_t(k * kPartThreads) + threadIdx.x;
       const int wi = k * (kPartThreads / 32) + warp;
-      const uint32_t word = flags[wi];
       if (p < count) {
-        const uint32_t below = __popc(word & ((1u << lane) - 1u));
+        const uint32_t below = __popc(word[k] & ((1u << lane) - 1u));
         const uint32_t lpos = word_prefix[wi] + below;  // left rows before p in the chunk
-        const bool left = (word >> lane) & 1u;
-        const uint32_t r = src[p];
+        const bool left = (word[k] >> lane) & 1u;
         const uint32_t rel = left ? left_before_chunk + lpos : pe.lcount + right_before_chunk + (p - lpos);
         if (rel < pe.seg_cnt) {  // always true when the counts agree
-          dst[rel] = r;
-          if (a.gh_ordered) gh_dst[rel] = gh_src[p];
+          dst[rel] = r[k];
+          if (a.gh_ordered) gh_dst[rel] = g[k];
         } else {
           err = kErrPartition;
         }
@@ -1696,18 +1717,39 @@ __global__ void apply_leaves_kernel(TrainerDev a) {
     const double step = __dmul_rn(lr, ls.value);
     const double step_l = ls.split ? __dmul_rn(lr, ls.left_value) : step;
     const double step_r = ls.split ? __dmul_rn(lr, ls.right_value) : step;
-    for (uint32_t p = threadIdx.x; p < count; p += blockDim.x) {
-      const uint32_t r = rows[p];
-      if (r >= a.n_rows) {
-        err = kErrCapacity;
-        continue;
+    // Eight rows per thread at a time: row ids, then routing gathers and predictions,
+    // then the stores (a segment's rows are distinct, so the updates do not collide).
+    constexpr int B = 8;
+    for (uint32_t p0 = 0; p0 < count; p0 += B * blockDim.x) {
+      uint32_t r[B];
+#pragma unroll
+      for (int k = 0; k < B; ++k) {
+        const uint32_t p = p0 + k * blockDim.x + threadIdx.x;
+        r[k] = p < count ? __ldg(rows + p) : 0xffffffffu;
       }
-      double v = step;
-      if (ls.split)
-        v = row_goes_left(a, r, ls.feature, ls.threshold, ls.default_left) ? step_l : step_r;
-      const double out = __dadd_rn(pred[r], v);
-      if (!f64_finite(out)) err = kErrNonFinite;
-      pred[r] = out;
+      double v[B], old[B];
+#pragma unroll
+      for (int k = 0; k < B; ++k) {
+        v[k] = step;
+        old[k] = 0.0;
+        if (r[k] < a.n_rows) {
+          if (ls.split)
+            v[k] = row_goes_left(a, r[k], ls.feature, ls.threshold, ls.default_left) ? step_l : step_r;
+          old[k] = pred[r[k]];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < B; ++k) {
+        const uint32_t p = p0 + k * blockDim.x + threadIdx.x;
+        if (p >= count) continue;
+        if (r[k] >= a.n_rows) {
+          err = kErrCapacity;
+          continue;
+        }
+        const double out = __dadd_rn(old[k], v[k]);
+        if (!f64_finite(out)) err = kErrNonFinite;
+        pred[r[k]] = out;
+      }
     }
   }
   if (err) raise(a.ctl, err);

@@ -228,6 +228,10 @@ int mpsb_cuda_dataset_create(mpsb_cuda_backend* backend, const void* bins,
                              uint64_t rows, uint32_t features, const uint32_t* bin_count,
                              mpsb_cuda_dataset** out);
 void mpsb_cuda_dataset_destroy(mpsb_cuda_dataset* dataset);
+/* 1 when the dataset's row-major bins carry a TMA tensor map (row-major histogram levels
+   stage their gathered rows with tile::gather4 copies), else 0 (cp.async staging); set at
+   creation when the environment variable MPSB_HIST_TMA is 1. */
+int mpsb_cuda_dataset_uses_tma(const mpsb_cuda_dataset* dataset);
 
 /* ---- node-level entries (the backend.hpp contract) ----------------------------------- */
 int mpsb_cuda_squared_error(mpsb_cuda_backend* backend, const double* labels,

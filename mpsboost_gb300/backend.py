@@ -242,6 +242,11 @@ class DeviceDataset:
         )
         self.handle = handle
 
+    @property
+    def uses_tma(self) -> bool:
+        """Row-major histogram levels stage gathered rows with TMA gather4 copies."""
+        return bool(_lib.load().mpsb_cuda_dataset_uses_tma(self.handle))
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             _lib.load().mpsb_cuda_dataset_destroy(self.handle)

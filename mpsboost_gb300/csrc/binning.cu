@@ -381,6 +381,7 @@ mpsb_cuda_dataset* finish_dataset(mpsb_cuda_backend* b, const uint8_t* bins_fm, 
                       d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(), d->bins_fm.as<uint8_t>(),
                       b->error.as<uint32_t>(), s));
   if (b->take_error()) throw DataError("Binned value exceeds the feature histogram range");
+  attach_bins_tmap(d.get());
   return d.release();
 }
 

@@ -35,6 +35,7 @@ enum : uint32_t {
   kErrPrefix = 1u << 8,          // prefix exceeded the non-missing parent (tree_split.cpp:212-214)
   kErrRootCache = 1u << 9,       // the hessian scale of a reused root histogram changed
   kErrLeafQueue = 1u << 10,      // leaf-wise active queue beyond max_active_leaves
+  kErrCopy = 1u << 11,           // a tensor copy did not complete within its time limit
                                  // (tree_leafwise.cpp:80-83, 130-134)
 };
 

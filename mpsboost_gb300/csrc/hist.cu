@@ -43,6 +43,57 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
 
+// ---- TMA gather4 staging (row-major levels) ------------------------------------------
+// A warp's stage is filled by up to eight `cp.async.bulk.tensor.2d ... tile::gather4`
+// copies (four 32-byte rows each, 128 bytes into a 128-byte aligned slot) that complete
+// on the stage's mbarrier. The L1 tag stage sees none of it (the cp.async path costs one
+// L1 wavefront per gathered row's line), but on GB300 the copies complete later than
+// cp.async ones and the row-major levels build about 8 % slower, so this path is opt-in.
+constexpr unsigned long long kCopyTimeoutNs = 1000000000ull;  // 1 s per stage wait
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+// The waiting thread sleeps until the phase completes or 20 us pass (no spinning issue
+// slots or shared-memory requests while the copies are in flight).
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 20000;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+// Waits for the phase of the given parity to complete; false after kCopyTimeoutNs.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > kCopyTimeoutNs) return false;
+  }
+}
+__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap* map, int32_t x,
+                                            int32_t r0, int32_t r1, int32_t r2, int32_t r3,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(bar)
+      : "memory");
+}
+
 template <uint32_t OFF = 0>
 __device__ __forceinline__ void red_shared_u32(uint32_t addr, uint32_t v) {
   asm volatile("red.shared.add.u32 [%0+%2], %1;\n" ::"r"(addr), "r"(v), "n"(OFF));
@@ -73,16 +124,22 @@ struct HistSmem<kModeFloat> {
 // each), gradient-only mode {g_lo | g_hi << 16, 0}, float mode {g, h}.
 constexpr int kRowBytes = 32 + 8;
 
-template <int MODE, int THREADS, int NSTAGE>
-__global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
+// TMA: stage gathered rows with tile::gather4 copies through `tmap` (row-major bins);
+// otherwise with cp.async (either layout; `tmap` unused).
+template <int MODE, int THREADS, int NSTAGE, bool TMA>
+__global__ void __launch_bounds__(THREADS, 1)
+    hist_build_kernel(TrainerDev a, const __grid_constant__ CUtensorMap tmap) {
   constexpr int WARPS = THREADS / 32;
   constexpr int CELLS = kSlots * kBlockFeatures;
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* hist_smem = smem;
   uint8_t* stage_bins = smem + HistSmem<MODE>::kBytes;  // [WARPS][NSTAGE][32 rows][32]
   uint2* stage_val = reinterpret_cast<uint2*>(stage_bins + size_t(NSTAGE) * THREADS * 32);  // [WARPS][NSTAGE][32]
+  // TMA: one mbarrier per warp and stage, [WARPS][NSTAGE].
+  const uint32_t bar_base =
+      static_cast<uint32_t>(__cvta_generic_to_shared(stage_val + size_t(NSTAGE) * THREADS));
 
-  __shared__ uint32_t s_item, s_entry;
+  __shared__ uint32_t s_item, s_entry, s_abort;
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -90,6 +147,21 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
   const uint32_t n = a.n_rows;
   const uint32_t nfb = a.nfb;
   const uint32_t hist_base = static_cast<uint32_t>(__cvta_generic_to_shared(hist_smem));
+  const uint32_t stage_base = static_cast<uint32_t>(__cvta_generic_to_shared(stage_bins));
+
+  if constexpr (TMA) {
+    // gather4 writes 128-byte slots; the staging area starts 128-byte aligned.
+    if (stage_base & 127u) {
+      if (tid == 0) atomicOr(&a.ctl->error, uint32_t(kErrCopy));
+      return;
+    }
+    if (lane == 0)
+      for (int st = 0; st < NSTAGE; ++st) mbar_init(bar_base + uint32_t(warp * NSTAGE + st) * 8u, 1u);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (tid == 0) s_abort = 0;
+  __syncthreads();
+  uint32_t warp_tiles = 0;  // tiles this warp staged so far (stage and mbarrier phase)
 
   for (;;) {
     const uint32_t limit = a.item_end ? a.item_end : a.ctl->hist_items;
@@ -108,7 +180,7 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
     }
     __syncthreads();
     const uint32_t item = s_item;
-    if (item >= limit) break;
+    if (item >= limit || s_abort) break;
     const uint32_t fb = item % nfb;
     const uint32_t chunk = item / nfb;
     const BuildEntry e = a.build[s_entry];
@@ -132,12 +204,12 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
     }
     __syncthreads();
 
-    // Each warp runs its own two-stage pipeline over 32-row tiles (tiles warp, warp +
+    // Each warp runs its own NSTAGE-stage pipeline over 32-row tiles (tiles warp, warp +
     // WARPS, ...): lane l stages row l's quantized values by a shared store, and lanes 2j,
-    // 2j+1 copy the two 16-byte halves of a row's 32-byte bin block with cp.async, while
-    // the warp reduces the previous tile. Only
-    // __syncwarp orders a warp's stages, so warps drift freely and keep the shared-memory
-    // reduction pipe busy; the CTA meets only at item boundaries.
+    // 2j+1 copy the two 16-byte halves of a row's 32-byte bin block with cp.async (or
+    // lane 4j gathers four rows with TMA), while the warp reduces the tile NSTAGE - 1
+    // back. Only __syncwarp orders a warp's stages, so warps drift freely and keep the
+    // shared-memory reduction pipe busy; the CTA meets only at item boundaries.
     const uint32_t ntiles = (row_count + 31u) / 32u;
     const uint32_t my_tiles = uint32_t(warp) < ntiles ? (ntiles - uint32_t(warp) + WARPS - 1) / WARPS : 0u;
     uint8_t* wbins = stage_bins + size_t(warp) * NSTAGE * 32 * 32;        // [NSTAGE][32][32]
@@ -180,9 +252,11 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
         red_shared_f32<2u * CELLS * 4u>(addr, __uint_as_float(q.y));
       }
     };
-    for (uint32_t k = 0; k < my_tiles + 1; ++k) {
+    // Iteration k stages tile k and reduces tile k - AHEAD.
+    constexpr uint32_t AHEAD = NSTAGE - 1;
+    for (uint32_t k = 0; k < my_tiles + AHEAD; ++k) {
       if (k < my_tiles) {
-        const int st = int(k % NSTAGE);
+        const int st = int((warp_tiles + k) % NSTAGE);
         const uint32_t pos = pos_of(k);
         const uint32_t r = r_cur;
         const float2 p = g_cur;
@@ -190,16 +264,37 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
         g_cur = k + 1 < my_tiles ? gh_at(pos_of(k + 1), r_nxt) : make_float2(0.f, 0.f);
         r_cur = r_nxt;
         r_nxt = r_far;
-        // Two lanes per row: each copy instruction touches 16 rows' lines instead of 32.
         const uint32_t valid = min(32u, row_count - (uint32_t(warp) + k * WARPS) * 32u);
+        if constexpr (TMA) {
+          // Lane 4j gathers rows 4j..4j+3 of the tile into slot j; positions past the
+          // tile's end carry row 0, so every coordinate is a row of the matrix.
+          const int quad = lane & ~3;
+          const uint32_t r1 = __shfl_sync(0xffffffffu, r, quad + 1);
+          const uint32_t r2 = __shfl_sync(0xffffffffu, r, quad + 2);
+          const uint32_t r3 = __shfl_sync(0xffffffffu, r, quad + 3);
+          const uint32_t groups = (valid + 3u) / 4u;
+          const uint32_t bar = bar_base + uint32_t(warp * NSTAGE + st) * 8u;
+          if (lane == 0) mbar_arrive_expect_tx(bar, groups * 128u);
+          __syncwarp();
+          // The slot's previous contents were read by the reduction NSTAGE tiles back,
+          // whose loaded words fed its reductions before the __syncwarp that ended it:
+          // those reads are complete, so the async-proxy write needs no proxy fence.
+          if ((lane & 3) == 0 && uint32_t(lane >> 2) < groups) {
+            tma_gather4(stage_base + uint32_t((warp * NSTAGE + st) * 32 + lane) * 32u, &tmap,
+                        int32_t(fb * kBlockFeatures), int32_t(r), int32_t(r1), int32_t(r2),
+                        int32_t(r3), bar);
+          }
+        } else {
+          // Two lanes per row: each copy instruction touches 16 rows' lines instead of 32.
 #pragma unroll
-        for (uint32_t i = 0; i < 2; ++i) {
-          const uint32_t row_in_tile = 16u * i + uint32_t(lane >> 1);
-          const uint32_t rr = __shfl_sync(0xffffffffu, r, int(row_in_tile));
-          const uint32_t half = uint32_t(lane & 1) * 16u;
-          if (row_in_tile < valid)
-            cp_async16(wbins + (size_t(st) * 32 + row_in_tile) * 32 + half,
-                       bins + size_t(rr) * a.bins_row_stride + half);
+          for (uint32_t i = 0; i < 2; ++i) {
+            const uint32_t row_in_tile = 16u * i + uint32_t(lane >> 1);
+            const uint32_t rr = __shfl_sync(0xffffffffu, r, int(row_in_tile));
+            const uint32_t half = uint32_t(lane & 1) * 16u;
+            if (row_in_tile < valid)
+              cp_async16(wbins + (size_t(st) * 32 + row_in_tile) * 32 + half,
+                         bins + size_t(rr) * a.bins_row_stride + half);
+          }
         }
         if (pos < row_count) {
           uint2 v;
@@ -221,12 +316,32 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
           wval[st * 32 + lane] = v;
         }
       }
-      cp_async_commit();
-      if (k >= 1) {
-        cp_async_wait<1>();
+      if constexpr (!TMA) cp_async_commit();
+      if (k >= AHEAD) {
+        const uint32_t ct = k - AHEAD;
+        const int st = int((warp_tiles + ct) % NSTAGE);
+        if constexpr (TMA) {
+          const uint32_t phase = ((warp_tiles + ct) / NSTAGE) & 1u;
+          const bool ok = __all_sync(0xffffffffu,
+                                     mbar_wait_bounded(bar_base + uint32_t(warp * NSTAGE + st) * 8u, phase));
+          if (!ok) {
+            // Wait (bounded) for the later tiles' copies, already issued, then give up
+            // the launch: the host sees kErrCopy and discards the round.
+            for (uint32_t t = ct + 1; t <= k && t < my_tiles; ++t) {
+              const uint32_t nt = warp_tiles + t;
+              mbar_wait_bounded(bar_base + uint32_t(warp * NSTAGE + int(nt % NSTAGE)) * 8u,
+                                (nt / NSTAGE) & 1u);
+            }
+            if (lane == 0) {
+              atomicOr(&a.ctl->error, uint32_t(kErrCopy));
+              *reinterpret_cast<volatile uint32_t*>(&s_abort) = 1u;
+            }
+            break;
+          }
+        } else {
+          cp_async_wait<AHEAD>();
+        }
         __syncwarp();
-        const uint32_t ct = k - 1;
-        const int st = int(ct % NSTAGE);
         const uint32_t tile_pos = (uint32_t(warp) + ct * WARPS) * 32u;
         const int nrows = int(min(32u, row_count - tile_pos));
         const uint8_t* sb = wbins + size_t(st) * 32 * 32;
@@ -246,7 +361,8 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
         __syncwarp();
       }
     }
-    cp_async_wait<0>();
+    warp_tiles += my_tiles;
+    if constexpr (!TMA) cp_async_wait<0>();
     __syncthreads();
 
     // Flush non-empty cells into the node's slot.
@@ -288,23 +404,27 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_kernel(TrainerDev a) {
   }
 }
 
-template <int MODE, int THREADS, int NSTAGE>
+template <int MODE, int THREADS, int NSTAGE, bool TMA>
 size_t hist_smem_bytes() {
-  return HistSmem<MODE>::kBytes + size_t(NSTAGE) * THREADS * kRowBytes;
+  return HistSmem<MODE>::kBytes + size_t(NSTAGE) * THREADS * kRowBytes +
+         (TMA ? size_t(THREADS / 32) * NSTAGE * 8 : 0);
 }
 
-template <int MODE, int THREADS, int NSTAGE>
-cudaError_t launch_variant(const TrainerDev& a, int grid, cudaStream_t stream) {
-  const size_t smem = hist_smem_bytes<MODE, THREADS, NSTAGE>();
+template <int MODE, int THREADS, int NSTAGE, bool TMA = false>
+cudaError_t launch_variant(const TrainerDev& a, int grid, cudaStream_t stream,
+                           const CUtensorMap* tmap = nullptr) {
+  static_assert(HistSmem<MODE>::kBytes % 128 == 0, "stage slots must stay 128-byte aligned");
+  const size_t smem = hist_smem_bytes<MODE, THREADS, NSTAGE, TMA>();
   static bool configured = false;  // per variant; the attribute is per function
   if (!configured) {
-    const cudaError_t err = cudaFuncSetAttribute(hist_build_kernel<MODE, THREADS, NSTAGE>,
+    const cudaError_t err = cudaFuncSetAttribute(hist_build_kernel<MODE, THREADS, NSTAGE, TMA>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  int(smem));
     if (err != cudaSuccess) return err;
     configured = true;
   }
-  hist_build_kernel<MODE, THREADS, NSTAGE><<<grid, THREADS, smem, stream>>>(a);
+  static const CUtensorMap kNoMap{};
+  hist_build_kernel<MODE, THREADS, NSTAGE, TMA><<<grid, THREADS, smem, stream>>>(a, tmap ? *tmap : kNoMap);
   return cudaGetLastError();
 }
 
@@ -319,6 +439,13 @@ cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int gr
     return launch_variant<kModeFixedG, 768, 2>(a, grid, stream);
   }
   if (a.mode == kModeFixed) {
+    // Row-major view of the matrix the tensor map describes: gather with TMA.
+    const bool tma = cfg.bins_tmap && a.bins_block_stride == kBlockFeatures &&
+                     a.bins_row_stride == uint64_t(a.nfb) * kBlockFeatures;
+    if (tma && cfg.threads == 768) return launch_variant<kModeFixed, 768, 2, true>(a, grid, stream, cfg.bins_tmap);
+    if (tma && cfg.threads == 512 && cfg.stages == 3)
+      return launch_variant<kModeFixed, 512, 3, true>(a, grid, stream, cfg.bins_tmap);
+    if (tma && cfg.threads == 512) return launch_variant<kModeFixed, 512, 2, true>(a, grid, stream, cfg.bins_tmap);
     if (cfg.threads == 768) return launch_variant<kModeFixed, 768, 2>(a, grid, stream);
     if (cfg.threads == 640) return launch_variant<kModeFixed, 640, 2>(a, grid, stream);
     if (cfg.stages == 2) return launch_variant<kModeFixed, 512, 2>(a, grid, stream);
@@ -328,6 +455,36 @@ cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int gr
   if (cfg.threads == 768) return launch_variant<kModeFloat, 768, 2>(a, grid, stream);
   if (cfg.stages == 2) return launch_variant<kModeFloat, 512, 2>(a, grid, stream);
   return launch_variant<kModeFloat, 512, 3>(a, grid, stream);
+}
+
+}  // namespace mpsb
+
+namespace mpsb {
+
+bool encode_bins_tmap(CUtensorMap* map, const uint8_t* bins, uint64_t row_stride, uint32_t n_rows) {
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                              CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                              CUtensorMapFloatOOBfill);
+  static Encode encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return Encode(nullptr);
+    return reinterpret_cast<Encode>(fn);
+  }();
+  if (!encode || !bins || n_rows == 0 || row_stride % 16 != 0) return false;
+  // Dimension 0: the row's bytes (feature blocks of 32 bins), dimension 1: rows. A box is
+  // one 32-byte feature block of one row (gather4 takes four rows of it).
+  const cuuint64_t dims[2] = {row_stride, n_rows};
+  const cuuint64_t strides[1] = {row_stride};
+  const cuuint32_t box[2] = {uint32_t(kBlockFeatures), 1u};
+  const cuuint32_t elem[2] = {1u, 1u};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(bins), dims, strides, box,
+                elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace mpsb

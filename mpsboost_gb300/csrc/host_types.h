@@ -68,6 +68,7 @@ struct DevBuf {
 };
 
 std::string describe_device_error(uint32_t bits);
+void attach_bins_tmap(mpsb_cuda_dataset* d);
 void fixed_scales(const float* pairs32, uint64_t n, uint64_t n_rows, int32_t* kg, int32_t* kh);
 void validate_tree_params(const mpsb_train_params& p, uint32_t features);
 
@@ -101,6 +102,8 @@ struct mpsb_cuda_dataset {
   mpsb_cuda_backend* backend = nullptr;
   uint32_t n_rows = 0, features = 0, nfb = 0;
   mpsb::DevBuf bins, bins_blocked, bins_fm, bin_count, has_missing;
+  CUtensorMap bins_tmap{};  // row-major bins for TMA gathers (valid when has_bins_tmap)
+  bool has_bins_tmap = false;
   std::vector<uint32_t> h_bin_count;
   std::vector<uint8_t> h_has_missing;
   // Quantization schema (datasets binned on the device): boundaries per feature.

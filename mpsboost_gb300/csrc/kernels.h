@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "device.cuh"
@@ -115,7 +116,14 @@ struct HistConfig {
   int threads = 768;        // fixed and float builds
   int stages = 2;
   int root_threads = 1024;  // gradient-only root builds (64 KB histogram)
+  // Tensor map of the row-major bins ({row stride, n_rows} u8, box 32 x 1): row-major
+  // fixed-point builds stage gathered rows with TMA gather4 copies (opt-in). Null: cp.async.
+  const CUtensorMap* bins_tmap = nullptr;
 };
+
+// Encodes the tensor map of a row-major bins matrix (rows x row_stride bytes). Returns
+// false where the driver offers no tensor maps.
+bool encode_bins_tmap(CUtensorMap* map, const uint8_t* bins, uint64_t row_stride, uint32_t n_rows);
 
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,
                               cudaStream_t stream);

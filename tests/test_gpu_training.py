@@ -176,6 +176,27 @@ def test_root_reuse_is_exact(backend, monkeypatch, objective):
     assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
 
 
+@pytest.mark.parametrize("threads", ["768", "512"])
+def test_tma_staging_equals_cp_async(backend, monkeypatch, threads):
+    """Row-major levels whose gathered rows arrive by TMA gather4 copies give the same
+    trees as cp.async staging: depth 9 (levels 2-8 read the row-major bins), 70 features
+    (a partial third feature block), small nodes with partial tiles."""
+    x, y, w = _data(46, 40000, 70, 0.05, 3)
+    params = dict(n_estimators=3, learning_rate=0.2, max_depth=9, min_samples_leaf=1)
+    monkeypatch.setenv("MPSB_HIST_THREADS", threads)
+    monkeypatch.setenv("MPSB_HIST_TMA", "1")
+    tma_bins = mb.quantize_dense(x, 255)
+    a = mb.train_regressor(backend, tma_bins, y, w, **params)
+    assert backend.dataset(tma_bins).uses_tma
+    monkeypatch.setenv("MPSB_HIST_TMA", "0")
+    plain_bins = mb.quantize_dense(x, 255)
+    b = mb.train_regressor(backend, plain_bins, y, w, **params)
+    assert not backend.dataset(plain_bins).uses_tma
+    for t1, t2 in zip(a.trees, b.trees):
+        assert t1.tobytes() == t2.tobytes()
+    assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
+
+
 def test_logistic_against_replica(backend, port):
     x, y, w = _data(41, 6000, 8, 0.1, 2, "binary_logistic")
     params = dict(n_estimators=3, learning_rate=0.2, max_depth=5, min_samples_leaf=4,

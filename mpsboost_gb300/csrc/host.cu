@@ -837,6 +837,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     a.node_allowed[q] = t->alloc<uint32_t>(size_t(a.max_level_nodes) * W);
   }
   a.partial = t->alloc<SplitRec>(size_t(a.max_level_nodes) * a.n_fchunks);
+  a.node_screen = t->alloc<uint32_t>(a.max_level_nodes);
   a.build = t->alloc<BuildEntry>(a.max_level_nodes);
   a.build_prefix = t->alloc<uint32_t>(a.max_level_nodes + 1);
   a.sub = t->alloc<SubEntry>(a.max_level_nodes);

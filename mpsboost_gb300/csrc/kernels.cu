@@ -615,6 +615,21 @@ __device__ __forceinline__ void consider(const TreeParams& p, const Stat<FIXED>&
 // One warp per (node, feature); a CTA covers one node and blockDim/32 features and
 // writes the best split of its features to partial[node][chunk].
 constexpr int kScanThreadsMax = 512;
+constexpr uint32_t kScanQueue = 32;  // FP64 candidates queued per warp
+
+// A candidate waiting for the exact FP64 evaluation.
+template <bool FIXED>
+struct ScanCand {
+  Stat<FIXED> cl, cr;
+  uint32_t threshold, default_left;
+};
+
+// Shared memory per warp: its best split, the FP32 screen values of its lanes' 16
+// candidates each ([candidate][lane]) and its FP64 queue.
+template <bool FIXED>
+constexpr size_t scan_smem_per_warp() {
+  return sizeof(SplitRec) + 16 * 32 * sizeof(float) + kScanQueue * sizeof(ScanCand<FIXED>);
+}
 
 template <bool FIXED>
 __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev a, int parity) {
@@ -623,14 +638,18 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
   SplitRec* warp_best = reinterpret_cast<SplitRec*>(smem_raw);
-  // FP32 screen values of each lane's 16 candidates (8 thresholds x 2 missing directions),
-  // [warp][candidate][lane].
   float* s_scores = reinterpret_cast<float*>(smem_raw + sizeof(SplitRec) * nwarps);
+  ScanCand<FIXED>* s_queue = reinterpret_cast<ScanCand<FIXED>*>(
+      smem_raw + (sizeof(SplitRec) + 16 * 32 * sizeof(float)) * nwarps);
+  static_assert(sizeof(SplitRec) % 8 == 0, "queue entries stay 8-byte aligned");
   const TreeParams& P = a.params;
   const uint32_t n_chunks = a.n_fchunks;
-  const uint32_t items = a.ctl->n_nodes * n_chunks;
+  const uint32_t n_nodes = a.ctl->n_nodes;
+  const uint32_t items = n_nodes * n_chunks;
   for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
-    const uint32_t i = item / n_chunks, c = item % n_chunks;
+    // Chunk-major: the chunks of a node spread over the grid's waves, so later chunks
+    // screen against the node maximum the earlier ones published.
+    const uint32_t i = item % n_nodes, c = item / n_nodes;
     const NodeRec node = a.nodes[parity][i];
     const double inv_g = a.trees[node.tree].inv_g, inv_h = a.trees[node.tree].inv_h;
     const int st_kg = a.trees[node.tree].kg, st_kh = a.trees[node.tree].kh;
@@ -733,12 +752,12 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
         const float inv_h32 = FIXED && screen ? __int_as_float((127 - st_kh) << 23) : 1.0f;
         // |v| as hi * 2^32 + lo: float(hi) and float(lo) are each within u, and the fused
         // multiply-add rounds once more, so the result is within 3u of v (no cancellation:
-        // both parts are non-negative). 32-bit conversions stay off the FP64 pipe.
+        // both parts are non-negative). The conversions run on the FP32 pipe.
         auto to32 = [&](V v, float inv32) -> float {
           if constexpr (FIXED) {
             const unsigned long long m = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
-            const float f = __fmaf_rn(__uint2float_rn(uint32_t(m >> 32)), 4294967296.0f,
-                                      __uint2float_rn(uint32_t(m)));
+            const float f = __fmaf_rn(u32_to_f32_rn(uint32_t(m >> 32)), 4294967296.0f,
+                                      u32_to_f32_rn(uint32_t(m)));
             return (v < 0 ? -f : f) * inv32;
           } else {
             return f64_to_f32_rn(v);
@@ -766,10 +785,40 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
           return cls;
         };
         float best32 = -1.0f;
+        float cut = -1.0f;
         const Stat<FIXED> carry_in = left;
+        // Candidates that pass the screen queue up, and the warp evaluates them in FP64
+        // one per lane: the narrow FP64 pipe runs one pass per 32 survivors instead of one
+        // per (threshold, direction) step that has a survivor in any lane.
+        ScanCand<FIXED>* queue = s_queue + size_t(warp) * kScanQueue;
+        uint32_t queued = 0;
+        auto drain = [&]() {
+          __syncwarp();
+          if (uint32_t(lane) < queued) {
+            const ScanCand<FIXED> e = queue[lane];
+            consider<FIXED>(P, e.cl, e.cr, inv_g, inv_h, mono, node.lo, node.hi, f, e.threshold,
+                            e.default_left, best, err);
+          }
+          __syncwarp();
+          queued = 0;
+        };
         for (int pass = screen ? 0 : 1; pass < 2; ++pass) {
           left = carry_in;
-          const float cut = best32 >= 1e-30f ? best32 * (1.0f - 0x1p-18f) : -1.0f;
+          if (pass == 1 && screen) {
+            // The cut comes from the node's best certainly admissible FP32 score seen so
+            // far over all its features (this warp's included): a candidate below it has a
+            // strictly lower exact gain than that admissible candidate, which its own warp
+            // evaluates exactly, so it can win neither its feature's chunk nor the node.
+            float m = best32;
+            if (a.node_screen) {
+              uint32_t seen = 0;
+              if (lane == 0)
+                seen = best32 >= 1e-30f ? atomicMax(a.node_screen + i, __float_as_uint(best32))
+                                        : *reinterpret_cast<volatile uint32_t*>(a.node_screen + i);
+              m = fmaxf(m, __uint_as_float(__shfl_sync(0xffffffffu, seen, 0)));
+            }
+            cut = m >= 1e-30f ? m * (1.0f - 0x1p-18f) : -1.0f;
+          }
 #pragma unroll 1
           for (int k = 0; k < 8; ++k) {
             const int s = lane * 8 + k;
@@ -788,32 +837,45 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
               left = stat_add<FIXED>(left, b);
             }
             const uint32_t t = uint32_t(s);
-            if (t + 1 >= nb) continue;
             const Stat<FIXED> right = stat_sub<FIXED>(nmp, left);
-            if (left.count > nmp.count) {
+            bool cand = t + 1 < nb;
+            if (cand && left.count > nmp.count) {
               if (pass == 1) err |= kErrPrefix;
-              continue;
+              cand = false;
             }
-            if (left.count == 0 && right.count == 0) continue;
-            if (P.split_strategy == 1 && t != rnd) continue;
+            if (left.count == 0 && right.count == 0) cand = false;
+            if (P.split_strategy == 1 && t != rnd) cand = false;
             // After an empty bin the candidate repeats threshold t-1's statistics exactly and
             // loses the tie to it (IsBetterSplit prefers the lower threshold).
-            if (P.split_strategy == 0 && t > 0 && empty_bin) continue;
+            if (P.split_strategy == 0 && t > 0 && empty_bin) cand = false;
             for (int d = 0; d < 2; ++d) {
               const uint32_t dl = 1u - uint32_t(d);  // default_left 1, then 0
-              if (dl == 0 && miss.count == 0) break;
+              if (dl == 0 && miss.count == 0) break;  // warp-uniform
               const Stat<FIXED> cl = dl ? stat_add<FIXED>(left, miss) : left;
               const Stat<FIXED> cr = dl ? right : stat_add<FIXED>(right, miss);
               float& slot_score = s_scores[(warp * 16 + k * 2 + d) * 32 + lane];
               if (pass == 0) {
                 // The screen value: -inf rejects, +inf always evaluates.
+                if (!cand) continue;
                 float sc = 0.0f;
                 const int cls = classify(cl, cr, &sc);
                 if (cls == 1) best32 = fmaxf(best32, sc);
                 slot_score = cls == 0 ? -INFINITY : (cls == 2 ? INFINITY : sc);
               } else {
-                if (screen && cut > 0.0f && slot_score < cut) continue;
-                consider<FIXED>(P, cl, cr, inv_g, inv_h, mono, node.lo, node.hi, f, t, dl, best, err);
+                const bool want = cand && !(screen && cut > 0.0f && slot_score < cut);
+                const uint32_t ballot = __ballot_sync(0xffffffffu, want);
+                if (ballot == 0) continue;
+                const uint32_t n_new = uint32_t(__popc(ballot));
+                if (queued + n_new > kScanQueue) drain();
+                if (want) {
+                  ScanCand<FIXED> e;
+                  e.cl = cl;
+                  e.cr = cr;
+                  e.threshold = t;
+                  e.default_left = dl;
+                  queue[queued + uint32_t(__popc(ballot & ((1u << lane) - 1u)))] = e;
+                }
+                queued += n_new;
               }
             }
           }
@@ -822,6 +884,7 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
               best32 = fmaxf(best32, __shfl_xor_sync(0xffffffffu, best32, off));
           }
         }
+        if (queued) drain();
       }
     }
     if (err) raise(a.ctl, err);
@@ -1902,13 +1965,30 @@ cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t s) {
   subtract_kernel<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
+template <bool FIXED>
+cudaError_t launch_scan_variant(const TrainerDev& a, int parity, int grid, int threads, cudaStream_t s) {
+  const size_t smem = scan_smem_per_warp<FIXED>() * size_t(threads / 32);
+  static bool configured = false;
+  if (!configured) {
+    const cudaError_t err = cudaFuncSetAttribute(
+        split_scan_kernel<FIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        int(scan_smem_per_warp<FIXED>() * (kScanThreadsMax / 32)));
+    if (err != cudaSuccess) return err;
+    configured = true;
+  }
+  split_scan_kernel<FIXED><<<grid, threads, smem, s>>>(a, parity);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStream_t s) {
   const int threads = int(a.scan_threads);
   if (threads < 32 || threads > kScanThreadsMax || threads % 32) return cudaErrorInvalidValue;
-  const size_t smem = (sizeof(SplitRec) + 16 * 32 * sizeof(float)) * (threads / 32);
-  if (a.mode == kModeFixed) split_scan_kernel<true><<<grid, threads, smem, s>>>(a, parity);
-  else split_scan_kernel<false><<<grid, threads, smem, s>>>(a, parity);
-  return cudaGetLastError();
+  if (a.node_screen) {
+    const cudaError_t err = cudaMemsetAsync(a.node_screen, 0, size_t(a.max_level_nodes) * sizeof(uint32_t), s);
+    if (err != cudaSuccess) return err;
+  }
+  if (a.mode == kModeFixed) return launch_scan_variant<true>(a, parity, grid, threads, s);
+  return launch_scan_variant<false>(a, parity, grid, threads, s);
 }
 cudaError_t launch_leafwise_init(const TrainerDev& a, cudaStream_t s) {
   leafwise_init_kernel<<<1, 256, 0, s>>>(a);

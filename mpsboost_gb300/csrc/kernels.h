@@ -54,6 +54,10 @@ struct TrainerDev {
   uint32_t* node_allowed[2];    // [max_level_nodes][path_words]
   uint32_t max_level_nodes;
   SplitRec* partial;            // [max_level_nodes][n_fchunks]
+  // [max_level_nodes] running maximum of the FP32 screen scores of each node's certainly
+  // admissible candidates (float bits; zeroed before every split scan), or null: every
+  // chunk's best split is exact (the per-feature entry point).
+  uint32_t* node_screen;
   uint32_t n_fchunks;           // feature chunks of the split scan (32 features each)
   BuildEntry* build;            // [max_level_nodes]
   uint32_t* build_prefix;       // [max_level_nodes + 1] chunk prefix

@@ -452,7 +452,7 @@ struct mpsb_cuda_trainer {
         CK(launch_subtract(dev, grid(8), s)); ++k;
       }
       if (depth > 0) {
-        CK(launch_split_scan(dev, parity, grid(4), s)); ++k;
+        CK(launch_split_scan(dev, parity, grid(4), s)); k += split_scan_kernels(dev);
       }
       CK(launch_finalize(dev, parity, d, s)); ++k;
       if (d + 1 < depth) {
@@ -479,7 +479,7 @@ struct mpsb_cuda_trainer {
     }
     CK(launch_root_stats(dev, s)); ++k;
     if (depth > 0) {
-      CK(launch_split_scan(dev, 0, grid(4), s)); ++k;
+      CK(launch_split_scan(dev, 0, grid(4), s)); k += split_scan_kernels(dev);
     }
     CK(launch_leafwise_init(dev, s)); ++k;
     for (uint32_t step = 0; step < lw_steps && depth > 0; ++step) {
@@ -488,7 +488,7 @@ struct mpsb_cuda_trainer {
       CK(launch_zero_build_slots(dev, grid(8), s)); ++k;
       CK(launch_hist_build(dev, hcfg, grid(1), s)); ++k;
       CK(launch_subtract(dev, grid(8), s)); ++k;
-      CK(launch_split_scan(dev, 1, grid(4), s)); ++k;
+      CK(launch_split_scan(dev, 1, grid(4), s)); k += split_scan_kernels(dev);
       CK(launch_leafwise_merge(dev, s)); ++k;
     }
     CK(launch_leafwise_finish(dev, s)); ++k;
@@ -838,6 +838,8 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   }
   a.partial = t->alloc<SplitRec>(size_t(a.max_level_nodes) * a.n_fchunks);
   a.node_screen = t->alloc<uint32_t>(a.max_level_nodes);
+  a.chunk_screen = t->alloc<uint32_t>(size_t(a.max_level_nodes) * a.n_fchunks);
+  a.scan_two_phase = p->split_strategy == 0 && p->reg_alpha == 0.0 && p->reg_lambda > 0.0;
   a.build = t->alloc<BuildEntry>(a.max_level_nodes);
   a.build_prefix = t->alloc<uint32_t>(a.max_level_nodes + 1);
   a.sub = t->alloc<SubEntry>(a.max_level_nodes);

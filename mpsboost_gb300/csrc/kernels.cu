@@ -624,36 +624,110 @@ struct ScanCand {
   uint32_t threshold, default_left;
 };
 
-// Shared memory per warp: its best split, the FP32 screen values of its lanes' 16
-// candidates each ([candidate][lane]) and its FP64 queue.
-template <bool FIXED>
+// A feature's histogram staged in shared memory, [word][k][lane] for slot lane * 8 + k
+// (word 0 count, 1 g, 2 h): the lane's eight slots read conflict-free.
+constexpr size_t kScanHistBytes = size_t(kSlots) * 3 * sizeof(unsigned long long);
+
+// Shared memory per warp: its best split, its staged histogram and (exact phase) its FP64
+// queue.
+template <bool FIXED, bool SCREEN>
 constexpr size_t scan_smem_per_warp() {
-  return sizeof(SplitRec) + 16 * 32 * sizeof(float) + kScanQueue * sizeof(ScanCand<FIXED>);
+  return sizeof(SplitRec) + kScanHistBytes + (SCREEN ? 0 : kScanQueue * sizeof(ScanCand<FIXED>));
 }
 
-template <bool FIXED>
+// Copies a feature's histogram (kSlots x {count, g, h} 64-bit words, 6 KB, 16-byte
+// aligned) into the warp's staging area with coalesced 16-byte loads, all in flight
+// together.
+__device__ __forceinline__ void stage_feature_hist(const unsigned long long* src,
+                                                   unsigned long long* dst, int lane) {
+  constexpr int kChunks = int(kScanHistBytes / 16);  // 384
+  constexpr int kPerLane = kChunks / 32;              // 12
+  constexpr int kBatch = 4;
+  const ulonglong2* s2 = reinterpret_cast<const ulonglong2*>(src);
+#pragma unroll 1
+  for (int part = 0; part < kPerLane / kBatch; ++part) {
+    ulonglong2 v[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) v[j] = __ldg(s2 + (part * kBatch + j) * 32 + lane);
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const uint32_t w0 = uint32_t((part * kBatch + j) * 32 + lane) * 2u;
+#pragma unroll
+      for (uint32_t q = 0; q < 2; ++q) {
+        const uint32_t w = w0 + q, slot = w / 3u, word = w - slot * 3u;
+        dst[(word * 8u + (slot & 7u)) * 32u + (slot >> 3)] = q ? v[j].y : v[j].x;
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// Bit 31 of a chunk's screen word: some feature of the chunk is evaluated exactly whatever
+// the node's maximum (its screen is off, or a candidate is too close to call in FP32).
+// The low bits hold the chunk's best certainly admissible FP32 score (a non-negative
+// float's bits).
+constexpr uint32_t kChunkExact = 0x80000000u;
+
+// The split scan of a level, one warp per (node, feature), a CTA per (node, chunk of
+// blockDim/32 features). With the FP32 screen on (best-split strategy, no reg_alpha,
+// reg_lambda > 0) it runs in two launches:
+//  SCREEN: each warp forms its feature's prefix sums and the FP32 scores of its
+//    candidates, raises the node's running maximum of certainly admissible scores
+//    (node_screen, atomicMax on the float bits) and writes its chunk's maximum and exact
+//    flag (chunk_screen).
+//  EXACT: with the node's final maximum M, a chunk whose candidates all score below
+//    M(1 - 2^-18) and holds nothing to evaluate exactly writes "no split" at once; the
+//    other chunks evaluate in FP64, as the reference does, every candidate at or above
+//    that cut and every close call. A candidate below the cut has a strictly lower exact
+//    gain than the admissible candidate that scored M, which its own chunk evaluates, so
+//    it can win neither its chunk nor the node.
+// EXACT alone (screen off, or no node maxima: the per-feature entry point) screens each
+// feature against its own maximum. Each chunk's best split goes to partial[node][chunk].
+template <bool FIXED, bool SCREEN>
 __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev a, int parity) {
   using V = typename Stat<FIXED>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
   SplitRec* warp_best = reinterpret_cast<SplitRec*>(smem_raw);
-  float* s_scores = reinterpret_cast<float*>(smem_raw + sizeof(SplitRec) * nwarps);
+  uint32_t* warp_screen = reinterpret_cast<uint32_t*>(smem_raw);  // SCREEN: [warp]
+  unsigned long long* s_hist =
+      reinterpret_cast<unsigned long long*>(smem_raw + sizeof(SplitRec) * nwarps);
   ScanCand<FIXED>* s_queue = reinterpret_cast<ScanCand<FIXED>*>(
-      smem_raw + (sizeof(SplitRec) + 16 * 32 * sizeof(float)) * nwarps);
-  static_assert(sizeof(SplitRec) % 8 == 0, "queue entries stay 8-byte aligned");
+      smem_raw + (sizeof(SplitRec) + kScanHistBytes) * nwarps);
+  static_assert(sizeof(SplitRec) % 8 == 0, "staged words and queue entries stay 8-byte aligned");
+  __shared__ uint32_t s_skip;
   const TreeParams& P = a.params;
   const uint32_t n_chunks = a.n_fchunks;
   const uint32_t n_nodes = a.ctl->n_nodes;
   const uint32_t items = n_nodes * n_chunks;
+  const bool two_phase = !SCREEN && a.node_screen != nullptr && a.scan_two_phase != 0;
   for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
-    // Chunk-major: the chunks of a node spread over the grid's waves, so later chunks
-    // screen against the node maximum the earlier ones published.
-    const uint32_t i = item % n_nodes, c = item / n_nodes;
+    const uint32_t i = item / n_chunks, c = item % n_chunks;
     const NodeRec node = a.nodes[parity][i];
+    const uint32_t f = c * uint32_t(nwarps) + uint32_t(warp);
+    if (two_phase) {
+      if (threadIdx.x == 0) {
+        const uint32_t cs = a.chunk_screen[size_t(i) * n_chunks + c];
+        const float m = __uint_as_float(a.node_screen[i]);
+        s_skip = !(cs & kChunkExact) && m >= 1e-30f && __uint_as_float(cs) < m * (1.0f - 0x1p-18f);
+        if (s_skip) {
+          SplitRec none;
+          none.valid = 0;
+          none.gain = 0.0;
+          none.feature = c * uint32_t(nwarps);
+          none.threshold = 0;
+          none.default_left = 1;
+          a.partial[size_t(i) * n_chunks + c] = none;
+        }
+      }
+      __syncthreads();
+      const bool skip = s_skip != 0;
+      __syncthreads();
+      if (skip) continue;
+    }
     const double inv_g = a.trees[node.tree].inv_g, inv_h = a.trees[node.tree].inv_h;
     const int st_kg = a.trees[node.tree].kg, st_kh = a.trees[node.tree].kh;
-    const uint32_t f = c * uint32_t(nwarps) + uint32_t(warp);
     SplitRec best;
     best.valid = 0;
     best.gain = 0.0;
@@ -661,6 +735,8 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
     best.threshold = 0;
     best.default_left = 1;
     uint32_t err = 0;
+    float best32 = -1.0f;  // SCREEN: best certainly admissible FP32 score of the feature
+    bool exact = false;    // SCREEN: the feature needs the exact pass whatever the cut
     // A node with fewer than 2 * min_samples_leaf rows has no admissible split.
     bool active = f < a.features && node.count >= 2 * P.min_samples_leaf;
     if (active) {
@@ -670,8 +746,10 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
     if (active) {  // warp-uniform
       const uint32_t nb = a.bin_count[f];
       const bool hm = a.has_missing[f] != 0;
-      const unsigned long long* base =
-          a.hist + (size_t(node.slot) * a.features + f) * kSlots * 3;
+      unsigned long long* sh = s_hist + size_t(warp) * (kScanHistBytes / 8);
+      stage_feature_hist(a.hist + (size_t(node.slot) * a.features + f) * kSlots * 3, sh, lane);
+      // Slot lane * 8 + k: word w at sh[(w * 8 + k) * 32 + lane].
+      auto slot_word = [&](int k, int w) -> unsigned long long { return sh[(w * 8 + k) * 32 + lane]; };
       // Lane totals of 8 consecutive slots (the missing slot excluded from the scan).
       Stat<FIXED> sum = stat_zero<FIXED>(), miss = stat_zero<FIXED>();
       unsigned long long total_count = 0;
@@ -679,14 +757,14 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
       for (int k = 0; k < 8; ++k) {
         const int s = lane * 8 + k;
         Stat<FIXED> b;
-        const unsigned long long raw_count = base[s * 3 + 0];
+        const unsigned long long raw_count = slot_word(k, 0);
         b.count = uint32_t(raw_count);  // the total below checks the full word
         if constexpr (FIXED) {
-          b.g = (long long)base[s * 3 + 1];
-          b.h = (long long)base[s * 3 + 2];
+          b.g = (long long)slot_word(k, 1);
+          b.h = (long long)slot_word(k, 2);
         } else {
-          b.g = __longlong_as_double((long long)base[s * 3 + 1]);
-          b.h = __longlong_as_double((long long)base[s * 3 + 2]);
+          b.g = __longlong_as_double((long long)slot_word(k, 1));
+          b.h = __longlong_as_double((long long)slot_word(k, 2));
           if (!isfinite(b.g) || !isfinite(b.h) || b.h < 0.0) err |= kErrNonFinite;
         }
         total_count += raw_count;
@@ -705,8 +783,8 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
         const Stat<FIXED> y = shfl_up_stat<FIXED>(incl, off);
         if (lane >= off) incl = stat_add<FIXED>(y, incl);
       }
-      Stat<FIXED> left = shfl_up_stat<FIXED>(incl, 1);
-      if (lane == 0) left = stat_zero<FIXED>();
+      Stat<FIXED> carry_in = shfl_up_stat<FIXED>(incl, 1);
+      if (lane == 0) carry_in = stat_zero<FIXED>();
       if (total_count != node.count) err |= kErrCountMismatch;
       Stat<FIXED> parent;
       parent.count = node.count;
@@ -732,16 +810,16 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
         // Exact FP32 pre-screen. Every eligible candidate's score S = gL^2/(hL+lambda) +
         // gR^2/(hR+lambda) is computed in FP32 with relative error <= 14u (u = 2^-24; each
         // int64 -> FP32 conversion below is within 3u, lambda is rounded once, a division
-        // within 2u). A candidate
-        // whose FP32 score is below M(1 - 2^-18), M the warp's best FP32 score over certainly
-        // eligible candidates, then has an exact score at least 30u*M below that candidate's,
-        // far outside the FP64 evaluation's own rounding (a few 2^-53 * M, the parent score
-        // included), so its FP64 gain is strictly lower and it cannot win. Only the rest --
-        // and candidates whose min_child_weight test or score is too close to call in FP32
-        // -- run the FP64 evaluation of the reference. The score is quadratic only without
-        // reg_alpha, the admissible set monotone in it only without monotone constraints,
-        // and random thresholds leave one candidate: the screen is off for those, and where
-        // 2^-k leaves the FP32 normal range.
+        // within 2u). A candidate whose FP32 score is below M(1 - 2^-18), M the best FP32
+        // score of a certainly eligible candidate of the node, then has an exact score at
+        // least 30u*M below that candidate's, far outside the FP64 evaluation's own
+        // rounding (a few 2^-53 * M, the parent score included), so its FP64 gain is
+        // strictly lower and it cannot win. Only the rest -- and candidates whose
+        // min_child_weight test or score is too close to call in FP32 -- run the FP64
+        // evaluation of the reference. The score is quadratic only without reg_alpha, the
+        // admissible set monotone in it only without monotone constraints, and random
+        // thresholds leave one candidate: the screen is off for those, and where 2^-k
+        // leaves the FP32 normal range.
         const bool screen = P.split_strategy == 0 && mono == 0 && P.reg_alpha == 0.0 &&
                             P.reg_lambda > 0.0 &&
                             (!FIXED || (st_kg >= -120 && st_kg <= 120 && st_kh >= -120 && st_kh <= 120));
@@ -784,55 +862,25 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
           *s32 = sc;
           return cls;
         };
-        float best32 = -1.0f;
-        float cut = -1.0f;
-        const Stat<FIXED> carry_in = left;
-        // Candidates that pass the screen queue up, and the warp evaluates them in FP64
-        // one per lane: the narrow FP64 pipe runs one pass per 32 survivors instead of one
-        // per (threshold, direction) step that has a survivor in any lane.
-        ScanCand<FIXED>* queue = s_queue + size_t(warp) * kScanQueue;
-        uint32_t queued = 0;
-        auto drain = [&]() {
-          __syncwarp();
-          if (uint32_t(lane) < queued) {
-            const ScanCand<FIXED> e = queue[lane];
-            consider<FIXED>(P, e.cl, e.cr, inv_g, inv_h, mono, node.lo, node.hi, f, e.threshold,
-                            e.default_left, best, err);
-          }
-          __syncwarp();
-          queued = 0;
-        };
-        for (int pass = screen ? 0 : 1; pass < 2; ++pass) {
-          left = carry_in;
-          if (pass == 1 && screen) {
-            // The cut comes from the node's best certainly admissible FP32 score seen so
-            // far over all its features (this warp's included): a candidate below it has a
-            // strictly lower exact gain than that admissible candidate, which its own warp
-            // evaluates exactly, so it can win neither its feature's chunk nor the node.
-            float m = best32;
-            if (a.node_screen) {
-              uint32_t seen = 0;
-              if (lane == 0)
-                seen = best32 >= 1e-30f ? atomicMax(a.node_screen + i, __float_as_uint(best32))
-                                        : *reinterpret_cast<volatile uint32_t*>(a.node_screen + i);
-              m = fmaxf(m, __uint_as_float(__shfl_sync(0xffffffffu, seen, 0)));
-            }
-            cut = m >= 1e-30f ? m * (1.0f - 0x1p-18f) : -1.0f;
-          }
+        // Visits every (threshold, missing direction) step of the lane's 8 slots with the
+        // candidate's left/right statistics; `cand` is false where no candidate exists.
+        // Every lane visits every step (the visitor may use warp collectives).
+        auto scan_candidates = [&](auto&& visit) {
+          Stat<FIXED> left = carry_in;
 #pragma unroll 1
           for (int k = 0; k < 8; ++k) {
             const int s = lane * 8 + k;
             bool empty_bin = false;
-            if (!(hm && s == kMissingSlot)) {  // reload the slot (L1-resident)
+            if (!(hm && s == kMissingSlot)) {  // reload the slot from the staging area
               Stat<FIXED> b;
-              b.count = uint32_t(base[s * 3 + 0]);
+              b.count = uint32_t(slot_word(k, 0));
               empty_bin = b.count == 0;
               if constexpr (FIXED) {
-                b.g = (long long)base[s * 3 + 1];
-                b.h = (long long)base[s * 3 + 2];
+                b.g = (long long)slot_word(k, 1);
+                b.h = (long long)slot_word(k, 2);
               } else {
-                b.g = __longlong_as_double((long long)base[s * 3 + 1]);
-                b.h = __longlong_as_double((long long)base[s * 3 + 2]);
+                b.g = __longlong_as_double((long long)slot_word(k, 1));
+                b.h = __longlong_as_double((long long)slot_word(k, 2));
               }
               left = stat_add<FIXED>(left, b);
             }
@@ -840,90 +888,146 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
             const Stat<FIXED> right = stat_sub<FIXED>(nmp, left);
             bool cand = t + 1 < nb;
             if (cand && left.count > nmp.count) {
-              if (pass == 1) err |= kErrPrefix;
+              err |= kErrPrefix;
               cand = false;
             }
             if (left.count == 0 && right.count == 0) cand = false;
             if (P.split_strategy == 1 && t != rnd) cand = false;
-            // After an empty bin the candidate repeats threshold t-1's statistics exactly and
-            // loses the tie to it (IsBetterSplit prefers the lower threshold).
+            // After an empty bin the candidate repeats threshold t-1's statistics exactly
+            // and loses the tie to it (IsBetterSplit prefers the lower threshold).
             if (P.split_strategy == 0 && t > 0 && empty_bin) cand = false;
             for (int d = 0; d < 2; ++d) {
               const uint32_t dl = 1u - uint32_t(d);  // default_left 1, then 0
               if (dl == 0 && miss.count == 0) break;  // warp-uniform
               const Stat<FIXED> cl = dl ? stat_add<FIXED>(left, miss) : left;
               const Stat<FIXED> cr = dl ? right : stat_add<FIXED>(right, miss);
-              float& slot_score = s_scores[(warp * 16 + k * 2 + d) * 32 + lane];
-              if (pass == 0) {
-                // The screen value: -inf rejects, +inf always evaluates.
-                if (!cand) continue;
-                float sc = 0.0f;
-                const int cls = classify(cl, cr, &sc);
-                if (cls == 1) best32 = fmaxf(best32, sc);
-                slot_score = cls == 0 ? -INFINITY : (cls == 2 ? INFINITY : sc);
-              } else {
-                const bool want = cand && !(screen && cut > 0.0f && slot_score < cut);
-                const uint32_t ballot = __ballot_sync(0xffffffffu, want);
-                if (ballot == 0) continue;
-                const uint32_t n_new = uint32_t(__popc(ballot));
-                if (queued + n_new > kScanQueue) drain();
-                if (want) {
-                  ScanCand<FIXED> e;
-                  e.cl = cl;
-                  e.cr = cr;
-                  e.threshold = t;
-                  e.default_left = dl;
-                  queue[queued + uint32_t(__popc(ballot & ((1u << lane) - 1u)))] = e;
-                }
-                queued += n_new;
-              }
+              visit(cand, cl, cr, t, dl);
             }
           }
-          if (pass == 0) {
-            for (int off = 16; off > 0; off >>= 1)
-              best32 = fmaxf(best32, __shfl_xor_sync(0xffffffffu, best32, off));
+        };
+        // The lane's best certainly admissible FP32 score; close calls set `exact`.
+        auto screen_scores = [&]() {
+          scan_candidates([&](bool cand, const Stat<FIXED>& cl, const Stat<FIXED>& cr, uint32_t,
+                              uint32_t) {
+            if (!cand) return;
+            float sc = 0.0f;
+            const int cls = classify(cl, cr, &sc);
+            if (cls == 1) best32 = fmaxf(best32, sc);
+            if (cls == 2) exact = true;
+          });
+          for (int off = 16; off > 0; off >>= 1)
+            best32 = fmaxf(best32, __shfl_xor_sync(0xffffffffu, best32, off));
+        };
+        if constexpr (SCREEN) {
+          if (screen) screen_scores();
+          else exact = true;
+        } else {
+          float cut = -1.0f;
+          if (screen) {
+            float m;
+            if (two_phase) {
+              m = __uint_as_float(a.node_screen[i]);
+            } else {
+              screen_scores();
+              m = best32;
+            }
+            cut = m >= 1e-30f ? m * (1.0f - 0x1p-18f) : -1.0f;
           }
+          // Candidates that pass the screen queue up, and the warp evaluates them in FP64
+          // one per lane: the narrow FP64 pipe runs one pass per 32 survivors instead of
+          // one per (threshold, direction) step that has a survivor in any lane.
+          ScanCand<FIXED>* queue = s_queue + size_t(warp) * kScanQueue;
+          uint32_t queued = 0;
+          auto drain = [&]() {
+            __syncwarp();
+            if (uint32_t(lane) < queued) {
+              const ScanCand<FIXED> e = queue[lane];
+              consider<FIXED>(P, e.cl, e.cr, inv_g, inv_h, mono, node.lo, node.hi, f, e.threshold,
+                              e.default_left, best, err);
+            }
+            __syncwarp();
+            queued = 0;
+          };
+          scan_candidates([&](bool cand, const Stat<FIXED>& cl, const Stat<FIXED>& cr, uint32_t t,
+                              uint32_t dl) {
+            bool want = cand;
+            if (want && screen && cut > 0.0f) {
+              float sc = 0.0f;
+              const int cls = classify(cl, cr, &sc);
+              want = cls == 2 || (cls == 1 && sc >= cut);
+            }
+            const uint32_t ballot = __ballot_sync(0xffffffffu, want);
+            if (ballot == 0) return;
+            const uint32_t n_new = uint32_t(__popc(ballot));
+            if (queued + n_new > kScanQueue) drain();
+            if (want) {
+              ScanCand<FIXED> e;
+              e.cl = cl;
+              e.cr = cr;
+              e.threshold = t;
+              e.default_left = dl;
+              queue[queued + uint32_t(__popc(ballot & ((1u << lane) - 1u)))] = e;
+            }
+            queued += n_new;
+          });
+          if (queued) drain();
         }
-        if (queued) drain();
       }
     }
     if (err) raise(a.ctl, err);
-    // Warp argmax (all lanes share the feature): every lane ends with the winner's id.
-    uint32_t win = uint32_t(lane);
-    {
-      double g = best.gain;
-      uint32_t v = best.valid, thr = best.threshold, dl = best.default_left;
-      for (int off = 16; off > 0; off >>= 1) {
-        const double og = __shfl_xor_sync(0xffffffffu, g, off);
-        const uint32_t ov = __shfl_xor_sync(0xffffffffu, v, off);
-        const uint32_t ot = __shfl_xor_sync(0xffffffffu, thr, off);
-        const uint32_t od = __shfl_xor_sync(0xffffffffu, dl, off);
-        const uint32_t ow = __shfl_xor_sync(0xffffffffu, win, off);
-        bool take;
-        if (ov != v) take = ov > v;
-        else if (!v) take = ow < win;
-        else if (og != g) take = og > g;
-        else if (ot != thr) take = ot < thr;
-        else if (od != dl) take = od > dl;
-        else take = ow < win;
-        if (take) {
-          g = og;
-          v = ov;
-          thr = ot;
-          dl = od;
-          win = ow;
+    if constexpr (SCREEN) {
+      exact = __any_sync(0xffffffffu, exact);
+      if (lane == 0) {
+        if (best32 >= 1e-30f) atomicMax(a.node_screen + i, __float_as_uint(best32));
+        warp_screen[warp] = (exact ? kChunkExact : 0u) | (best32 > 0.0f ? __float_as_uint(best32) : 0u);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        uint32_t word = 0;
+        for (int w = 0; w < nwarps; ++w)
+          word = (word & kChunkExact) | (warp_screen[w] & kChunkExact) |
+                 max(word & ~kChunkExact, warp_screen[w] & ~kChunkExact);
+        a.chunk_screen[size_t(i) * n_chunks + c] = word;
+      }
+      __syncthreads();
+    } else {
+      // Warp argmax (all lanes share the feature): every lane ends with the winner's id.
+      uint32_t win = uint32_t(lane);
+      {
+        double g = best.gain;
+        uint32_t v = best.valid, thr = best.threshold, dl = best.default_left;
+        for (int off = 16; off > 0; off >>= 1) {
+          const double og = __shfl_xor_sync(0xffffffffu, g, off);
+          const uint32_t ov = __shfl_xor_sync(0xffffffffu, v, off);
+          const uint32_t ot = __shfl_xor_sync(0xffffffffu, thr, off);
+          const uint32_t od = __shfl_xor_sync(0xffffffffu, dl, off);
+          const uint32_t ow = __shfl_xor_sync(0xffffffffu, win, off);
+          bool take;
+          if (ov != v) take = ov > v;
+          else if (!v) take = ow < win;
+          else if (og != g) take = og > g;
+          else if (ot != thr) take = ot < thr;
+          else if (od != dl) take = od > dl;
+          else take = ow < win;
+          if (take) {
+            g = og;
+            v = ov;
+            thr = ot;
+            dl = od;
+            win = ow;
+          }
         }
       }
+      if (uint32_t(lane) == win) warp_best[warp] = best;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        SplitRec b = warp_best[0];
+        for (int w = 1; w < nwarps; ++w)
+          if (better_split(warp_best[w], b)) b = warp_best[w];
+        a.partial[size_t(i) * n_chunks + c] = b;
+      }
+      __syncthreads();
     }
-    if (uint32_t(lane) == win) warp_best[warp] = best;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      SplitRec b = warp_best[0];
-      for (int w = 1; w < nwarps; ++w)
-        if (better_split(warp_best[w], b)) b = warp_best[w];
-      a.partial[size_t(i) * n_chunks + c] = b;
-    }
-    __syncthreads();
   }
   (void)sizeof(V);
 }
@@ -1965,30 +2069,39 @@ cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t s) {
   subtract_kernel<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
-template <bool FIXED>
+template <bool FIXED, bool SCREEN>
 cudaError_t launch_scan_variant(const TrainerDev& a, int parity, int grid, int threads, cudaStream_t s) {
-  const size_t smem = scan_smem_per_warp<FIXED>() * size_t(threads / 32);
+  const size_t smem = scan_smem_per_warp<FIXED, SCREEN>() * size_t(threads / 32);
   static bool configured = false;
   if (!configured) {
     const cudaError_t err = cudaFuncSetAttribute(
-        split_scan_kernel<FIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        int(scan_smem_per_warp<FIXED>() * (kScanThreadsMax / 32)));
+        split_scan_kernel<FIXED, SCREEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        int(scan_smem_per_warp<FIXED, SCREEN>() * (kScanThreadsMax / 32)));
     if (err != cudaSuccess) return err;
     configured = true;
   }
-  split_scan_kernel<FIXED><<<grid, threads, smem, s>>>(a, parity);
+  split_scan_kernel<FIXED, SCREEN><<<grid, threads, smem, s>>>(a, parity);
   return cudaGetLastError();
+}
+
+uint32_t split_scan_kernels(const TrainerDev& a) {
+  return a.node_screen && a.scan_two_phase ? 2u : 1u;
 }
 
 cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStream_t s) {
   const int threads = int(a.scan_threads);
   if (threads < 32 || threads > kScanThreadsMax || threads % 32) return cudaErrorInvalidValue;
-  if (a.node_screen) {
-    const cudaError_t err = cudaMemsetAsync(a.node_screen, 0, size_t(a.max_level_nodes) * sizeof(uint32_t), s);
+  const bool fixed = a.mode == kModeFixed;
+  if (split_scan_kernels(a) == 2) {
+    cudaError_t err = cudaMemsetAsync(a.node_screen, 0, size_t(a.max_level_nodes) * sizeof(uint32_t), s);
+    if (err != cudaSuccess) return err;
+    // The screen phase holds about half the registers: twice the CTAs.
+    err = fixed ? launch_scan_variant<true, true>(a, parity, 2 * grid, threads, s)
+                : launch_scan_variant<false, true>(a, parity, 2 * grid, threads, s);
     if (err != cudaSuccess) return err;
   }
-  if (a.mode == kModeFixed) return launch_scan_variant<true>(a, parity, grid, threads, s);
-  return launch_scan_variant<false>(a, parity, grid, threads, s);
+  return fixed ? launch_scan_variant<true, false>(a, parity, grid, threads, s)
+               : launch_scan_variant<false, false>(a, parity, grid, threads, s);
 }
 cudaError_t launch_leafwise_init(const TrainerDev& a, cudaStream_t s) {
   leafwise_init_kernel<<<1, 256, 0, s>>>(a);

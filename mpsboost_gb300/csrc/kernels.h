@@ -54,10 +54,14 @@ struct TrainerDev {
   uint32_t* node_allowed[2];    // [max_level_nodes][path_words]
   uint32_t max_level_nodes;
   SplitRec* partial;            // [max_level_nodes][n_fchunks]
-  // [max_level_nodes] running maximum of the FP32 screen scores of each node's certainly
-  // admissible candidates (float bits; zeroed before every split scan), or null: every
-  // chunk's best split is exact (the per-feature entry point).
+  // Two-phase split scan (scan_two_phase: the FP32 screen applies): [max_level_nodes]
+  // maximum FP32 screen score of each node's certainly admissible candidates (float
+  // bits; zeroed before every scan) and [max_level_nodes][n_fchunks] each chunk's maximum
+  // and exact flag. Null node_screen: one launch, each feature screened on its own (the
+  // per-feature entry point needs every feature's best split).
   uint32_t* node_screen;
+  uint32_t* chunk_screen;
+  uint32_t scan_two_phase;
   uint32_t n_fchunks;           // feature chunks of the split scan (32 features each)
   BuildEntry* build;            // [max_level_nodes]
   uint32_t* build_prefix;       // [max_level_nodes + 1] chunk prefix
@@ -148,6 +152,7 @@ cudaError_t launch_leafwise_finish(const TrainerDev& a, cudaStream_t stream);
 cudaError_t launch_root_cache(const TrainerDev& a, int save, int grid, cudaStream_t stream);
 cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t stream);
 cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStream_t stream);
+uint32_t split_scan_kernels(const TrainerDev& a);  // launches per launch_split_scan
 cudaError_t launch_finalize(const TrainerDev& a, int parity, uint32_t depth, cudaStream_t stream);
 cudaError_t launch_partition(const TrainerDev& a, int grid, cudaStream_t stream);
 cudaError_t launch_partition_count(const TrainerDev& a, int grid, cudaStream_t stream);

@@ -212,7 +212,9 @@ __device__ __forceinline__ bool split_gain(double lg, double lh, double rg, doub
 }
 
 // StableRandomThreshold (tree_split.cpp:14-29).
-__device__ __forceinline__ uint32_t stable_random_threshold(uint32_t seed, uint32_t feature,
+// Not inlined: its 64-bit remainder is a long subroutine that must not be speculated
+// into scans that use no random thresholds.
+static __device__ __noinline__ uint32_t stable_random_threshold(uint32_t seed, uint32_t feature,
                                                             uint32_t node, uint32_t depth,
                                                             uint32_t candidates) {
   unsigned long long v = seed;

@@ -542,6 +542,12 @@ __device__ __forceinline__ Stat<FIXED> shfl_stat(Stat<FIXED> s, int src) {
   return r;
 }
 
+// q_image(x) > q_image(y), out of line: the FP64 conversions are not speculated into
+// the common case.
+static __device__ __noinline__ bool images_above(long long x, long long y, double inv) {
+  return q_image(x, inv) > q_image(y, inv);
+}
+
 template <bool FIXED>
 __device__ __forceinline__ double image(typename Stat<FIXED>::V v, double inv) {
   if constexpr (FIXED) return q_image(v, inv);
@@ -702,6 +708,11 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
   const uint32_t n_nodes = a.ctl->n_nodes;
   const uint32_t items = n_nodes * n_chunks;
   const bool two_phase = !SCREEN && a.node_screen != nullptr && a.scan_two_phase != 0;
+  // Launch-wide screen constants (FP64 tests and conversions stay out of the item loop).
+  const bool screen_params = P.split_strategy == 0 && P.reg_alpha == 0.0 && P.reg_lambda > 0.0;
+  const float lam32 = float(P.reg_lambda), mcw32 = float(P.min_child_weight);
+  const bool mcw_on = P.min_child_weight > 0.0;
+  const float mcw_lo = mcw32 * (1.0f - 3e-6f), mcw_hi = mcw32 * (1.0f + 3e-6f);
   for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
     const uint32_t i = item / n_chunks, c = item % n_chunks;
     const NodeRec node = a.nodes[parity][i];
@@ -796,8 +807,17 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
         parent.h = node.h;
       }
       if (nb >= 2 && total_count == node.count) {
-        if (miss.count > parent.count || image<FIXED>(miss.h, inv_h) > image<FIXED>(parent.h, inv_h))
-          err |= kErrMissing;
+        bool miss_h_above;
+        if constexpr (FIXED) {
+          // The images q * 2^-k compare as the quantized sums while those convert exactly.
+          const long long lim = 1ll << 53;
+          miss_h_above = (miss.h > -lim && miss.h < lim && parent.h > -lim && parent.h < lim)
+                             ? miss.h > parent.h
+                             : images_above(miss.h, parent.h, inv_h);
+        } else {
+          miss_h_above = miss.h > parent.h;
+        }
+        if (miss.count > parent.count || miss_h_above) err |= kErrMissing;
         const Stat<FIXED> nmp = stat_sub<FIXED>(parent, miss);
         const int8_t mono = P.has_monotonic ? a.monotonic[f] : 0;
         const uint32_t rnd =
@@ -820,11 +840,8 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
         // admissible set monotone in it only without monotone constraints, and random
         // thresholds leave one candidate: the screen is off for those, and where 2^-k
         // leaves the FP32 normal range.
-        const bool screen = P.split_strategy == 0 && mono == 0 && P.reg_alpha == 0.0 &&
-                            P.reg_lambda > 0.0 &&
+        const bool screen = screen_params && mono == 0 &&
                             (!FIXED || (st_kg >= -120 && st_kg <= 120 && st_kh >= -120 && st_kh <= 120));
-        const float lam32 = float(P.reg_lambda), mcw32 = float(P.min_child_weight);
-        const bool mcw_on = P.min_child_weight > 0.0;
         // 2^-k exactly, built from the exponent field.
         const float inv_g32 = FIXED && screen ? __int_as_float((127 - st_kg) << 23) : 1.0f;
         const float inv_h32 = FIXED && screen ? __int_as_float((127 - st_kh) << 23) : 1.0f;
@@ -852,9 +869,8 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
           const float lh = to32(cl.h, inv_h32), rh = to32(cr.h, inv_h32);
           int cls = 1;
           if (mcw_on) {
-            const float lo = mcw32 * (1.0f - 3e-6f), hi = mcw32 * (1.0f + 3e-6f);
-            if (lh < lo || rh < lo) return 0;
-            if (lh <= hi || rh <= hi) cls = 2;
+            if (lh < mcw_lo || rh < mcw_lo) return 0;
+            if (lh <= mcw_hi || rh <= mcw_hi) cls = 2;
           }
           const float lg = to32(cl.g, inv_g32), rg = to32(cr.g, inv_g32);
           const float sc = screen_div(lg * lg, lh + lam32) + screen_div(rg * rg, rh + lam32);

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -20,6 +22,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "host_types.h"
@@ -29,6 +32,26 @@ using namespace mpsb;
 namespace mpsb {
 
 thread_local std::string g_error;
+
+// MPSB_TRACE=1: host-side phase times of session setup and export on stderr.
+struct PhaseTrace {
+  bool on = false;
+  std::chrono::steady_clock::time_point t0, last;
+  const char* what;
+  explicit PhaseTrace(const char* w) : what(w) {
+    const char* v = std::getenv("MPSB_TRACE");
+    on = v && std::atoi(v) != 0;
+    t0 = last = std::chrono::steady_clock::now();
+  }
+  void mark(const char* phase) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[mpsb %s] %-28s %8.3f ms (total %8.3f)\n", what, phase,
+                 std::chrono::duration<double, std::milli>(now - last).count(),
+                 std::chrono::duration<double, std::milli>(now - t0).count());
+    last = now;
+  }
+};
 
 std::string describe_device_error(uint32_t bits) {
   std::string m = "device reported:";
@@ -104,36 +127,139 @@ void validate_training_params(const mpsb_train_params& p) {  // trainer.cpp:22-4
   if (p.objective > 4) throw TrainingError("unknown training objective");
 }
 
-double validate_weights(const double* w, uint64_t n) {  // trainer.cpp:44-66
-  if (n == 0) throw TrainingError("labels must be non-empty");
-  double total = 0.0;
+// One pass over the rows: the weight total of ValidateWeights (trainer.cpp:44-66) and,
+// for the mean-type objectives (label_mode 1: squared error, finite labels; 2: poisson and
+// tweedie, non-negative labels), the weighted label sum of InitialBaseScore
+// (trainer.cpp:68-176), both accumulated in row order as the reference does. The two sums
+// are independent chains, so one loop costs about one chain. Errors keep the reference's
+// order: every weight check before any label check, each at its first failing row.
+struct RowSums {
+  double total = 0.0;      // sum of weights
+  double label_sum = 0.0;  // sum of label * weight (label_mode != 0)
+  int label_mode = 0;
+};
+
+// The reference's sequential loop, which also finds the first failing row and its error.
+RowSums row_sums_checked(const double* w, const double* y, uint64_t n, int label_mode,
+                         const char* name) {
+  RowSums r;
+  r.label_mode = y ? label_mode : 0;
+  double total = 0.0, s = 0.0;
+  uint64_t w_bad = n, w_ovf = n, y_bad = n, y_ovf = n;
   for (uint64_t i = 0; i < n; ++i) {
     const double x = w ? w[i] : 1.0;
-    if (!std::isfinite(x) || x < 0.0) throw TrainingError("sample weights must be finite non-negative values");
+    if (!std::isfinite(x) || x < 0.0) { w_bad = i; break; }
     total += x;
-    if (!std::isfinite(total)) throw TrainingError("sample weight sum overflowed");
+    if (!std::isfinite(total)) { w_ovf = i; break; }
+    if (r.label_mode && y_bad == n && y_ovf == n) {
+      const double v = y[i];
+      if (!std::isfinite(v) || (r.label_mode == 2 && v < 0.0)) {
+        y_bad = i;
+      } else {
+        s += v * x;
+        if (!std::isfinite(s)) y_ovf = i;
+      }
+    }
   }
+  if (w_bad < n) throw TrainingError("sample weights must be finite non-negative values");
+  if (w_ovf < n) throw TrainingError("sample weight sum overflowed");
   if (total <= 0.0) throw TrainingError("sample weights must contain positive total weight");
-  return total;
+  if (y_bad < n) {
+    if (r.label_mode == 1) throw TrainingError("Labels must be finite");
+    throw TrainingError(std::string(name) + " labels must be non-negative");
+  }
+  if (y_ovf < n) {
+    if (r.label_mode == 1) throw TrainingError("Label accumulation overflowed");
+    throw TrainingError(std::string(name) + " label sum overflowed");
+  }
+  r.total = total;
+  r.label_sum = s;
+  return r;
+}
+
+// Fast path: the two row-order sums in a tight loop (the same additions, so the same
+// results) while worker threads check every weight and label; any failed check or
+// non-finite sum reruns the sequential loop above for the reference's exact error.
+RowSums row_sums(const double* w, const double* y, uint64_t n, int label_mode, const char* name) {
+  if (n == 0) throw TrainingError("labels must be non-empty");
+  const int mode = y ? label_mode : 0;
+  std::atomic<bool> bad{false};
+  const uint32_t workers = uint32_t(std::min<uint64_t>(
+      std::max(1u, std::min(16u, std::thread::hardware_concurrency())), (n + (1u << 20) - 1) >> 20));
+  auto check = [&](uint32_t k, uint32_t of) {
+    const uint64_t lo = n * k / of, hi = n * (k + 1) / of;
+    bool ok = true;
+    for (uint64_t i = lo; i < hi; ++i) {
+      const double x = w ? w[i] : 1.0;
+      ok &= std::isfinite(x) && !(x < 0.0);
+      if (mode) {
+        const double v = y[i];
+        ok &= std::isfinite(v) && !(mode == 2 && v < 0.0);
+      }
+    }
+    if (!ok) bad.store(true, std::memory_order_relaxed);
+  };
+  std::vector<std::thread> pool;
+  if (workers > 1)
+    for (uint32_t k = 0; k < workers; ++k) pool.emplace_back(check, k, workers);
+  else
+    check(0, 1);
+  double total = 0.0, s = 0.0;
+  if (mode) {
+    for (uint64_t i = 0; i < n; ++i) {
+      const double x = w ? w[i] : 1.0;
+      total += x;
+      s += y[i] * x;
+    }
+  } else if (w) {
+    for (uint64_t i = 0; i < n; ++i) total += w[i];
+  } else {
+    for (uint64_t i = 0; i < n; ++i) total += 1.0;
+  }
+  for (auto& t : pool) t.join();
+  if (bad.load() || !std::isfinite(total) || !(total > 0.0) || (mode && !std::isfinite(s)))
+    return row_sums_checked(w, y, n, label_mode, name);
+  RowSums r;
+  r.label_mode = mode;
+  r.total = total;
+  r.label_sum = s;
+  return r;
+}
+
+double validate_weights(const double* w, uint64_t n) {  // trainer.cpp:44-66
+  return row_sums(w, nullptr, n, 0, nullptr).total;
+}
+
+const char* count_objective_name(uint32_t objective) {
+  return objective == MPSB_POISSON ? "poisson" : "tweedie";
+}
+
+// The label mode of row_sums for a boosting objective (0: the base score needs another pass).
+int label_mode_of(uint32_t objective) {
+  if (objective == MPSB_SQUARED_ERROR) return 1;
+  if (objective == MPSB_POISSON || objective == MPSB_TWEEDIE) return 2;
+  return 0;
 }
 
 // InitialBaseScore (trainer.cpp:68-176) on host FP64 in row order. `cls` >= 0 selects the
-// one-vs-rest binary labels (label == cls).
+// one-vs-rest binary labels (label == cls). `pre`: this fit's row sums, when they carry
+// the label sum of the objective (cls < 0).
 double base_score(const mpsb_train_params& p, const double* y, const double* w, uint64_t n,
-                  int64_t cls) {
-  const double total = validate_weights(w, n);
+                  int64_t cls, const RowSums* pre = nullptr) {
+  const int mode = cls < 0 ? label_mode_of(p.objective) : 0;
+  if (mode && pre && pre->label_mode == mode) {
+    if (mode == 1) return pre->label_sum / pre->total;
+    return std::log(std::max(1e-15, pre->label_sum / pre->total));
+  }
+  if (mode) {
+    const RowSums r = row_sums(w, y, n, mode, count_objective_name(p.objective));
+    if (mode == 1) return r.label_sum / r.total;
+    return std::log(std::max(1e-15, r.label_sum / r.total));
+  }
+  const double total = pre ? pre->total : validate_weights(w, n);
   auto W = [&](uint64_t i) { return w ? w[i] : 1.0; };
   auto Y = [&](uint64_t i) { return cls >= 0 ? (y[i] == double(cls) ? 1.0 : 0.0) : y[i]; };
   switch (p.objective) {
-    case MPSB_SQUARED_ERROR: {
-      double s = 0.0;
-      for (uint64_t i = 0; i < n; ++i) {
-        if (!std::isfinite(Y(i))) throw TrainingError("Labels must be finite");
-        s += Y(i) * W(i);
-        if (!std::isfinite(s)) throw TrainingError("Label accumulation overflowed");
-      }
-      return s / total;
-    }
     case MPSB_BINARY_LOGISTIC: {
       double pos = 0.0;
       for (uint64_t i = 0; i < n; ++i) {
@@ -162,16 +288,8 @@ double base_score(const mpsb_train_params& p, const double* y, const double* w, 
       }
       return o.back().first;
     }
-    default: {
-      const char* name = p.objective == MPSB_POISSON ? "poisson" : "tweedie";
-      double s = 0.0;
-      for (uint64_t i = 0; i < n; ++i) {
-        if (!std::isfinite(Y(i)) || Y(i) < 0.0) throw TrainingError(std::string(name) + " labels must be non-negative");
-        s += Y(i) * W(i);
-        if (!std::isfinite(s)) throw TrainingError(std::string(name) + " label sum overflowed");
-      }
-      return std::log(std::max(1e-15, s / total));
-    }
+    default:  // squared error, poisson and tweedie take the row_sums path above
+      throw TrainingError("unknown training objective");
   }
 }
 
@@ -308,6 +426,7 @@ int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t wi
     if (rows == 0 || features == 0) throw DataError("dataset must contain at least one row and one feature");
     if (rows >= 0xFFFFFFFFull) throw UnsupportedError("the CUDA backend indexes rows with uint32");
     b->activate();
+    PhaseTrace trace("dataset");
     std::unique_ptr<mpsb_cuda_dataset> d(new mpsb_cuda_dataset);
     d->backend = b;
     d->n_rows = uint32_t(rows);
@@ -329,14 +448,7 @@ int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t wi
           throw UnsupportedError("a feature with missing values may have at most 255 bins on the CUDA backend");
       }
     }
-    const size_t cells = size_t(rows) * features;
-    DevBuf src, miss;
-    src.alloc(cells * width);
-    CK(cudaMemcpyAsync(src.p, bins, cells * width, cudaMemcpyHostToDevice, b->stream));
-    if (missing) {
-      miss.alloc(cells);
-      CK(cudaMemcpyAsync(miss.p, missing, cells, cudaMemcpyHostToDevice, b->stream));
-    }
+    trace.mark("bin counts, missing scan");
     d->bin_count.alloc(features * sizeof(uint32_t));
     d->has_missing.alloc(features);
     CK(cudaMemcpyAsync(d->bin_count.p, bin_count, features * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
@@ -344,11 +456,46 @@ int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t wi
     d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
     d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
     d->bins_fm.alloc(size_t(features) * rows);
-    CK(launch_pack_bins(src.p, width, missing ? miss.as<uint8_t>() : nullptr,
-                        d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb,
-                        d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(),
-                        d->bins_fm.as<uint8_t>(), b->error.as<uint32_t>(), b->stream));
+    trace.mark("allocs");
+    // Feature block by feature block (32 feature columns, contiguous in the feature-major
+    // source): the copy stream uploads block fb + 1 into one staging buffer while the
+    // compute stream packs block fb from the other.
+    if (!b->copy_stream) CK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+    const size_t block_cells = size_t(kBlockFeatures) * rows;
+    DevBuf stage[2], mstage[2];
+    const int nstage = d->nfb > 1 ? 2 : 1;
+    for (int k = 0; k < nstage; ++k) {
+      stage[k].alloc(block_cells * width);
+      if (missing) mstage[k].alloc(block_cells);
+    }
+    struct Events {
+      cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+      ~Events() {
+        for (cudaEvent_t x : e)
+          if (x) cudaEventDestroy(x);
+      }
+    } ev;  // copied[2], packed[2]
+    for (cudaEvent_t& x : ev.e) CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    for (uint32_t fb = 0; fb < d->nfb; ++fb) {
+      const int k = int(fb & 1);
+      const uint32_t nf = std::min<uint32_t>(kBlockFeatures, features - fb * kBlockFeatures);
+      const size_t first = size_t(fb) * block_cells;
+      if (fb >= 2) CK(cudaStreamWaitEvent(b->copy_stream, ev.e[2 + k], 0));  // block fb-2 packed
+      CK(cudaMemcpyAsync(stage[k].p, static_cast<const uint8_t*>(bins) + first * width,
+                         size_t(nf) * rows * width, cudaMemcpyHostToDevice, b->copy_stream));
+      if (missing)
+        CK(cudaMemcpyAsync(mstage[k].p, missing + first, size_t(nf) * rows, cudaMemcpyHostToDevice,
+                           b->copy_stream));
+      CK(cudaEventRecord(ev.e[k], b->copy_stream));
+      CK(cudaStreamWaitEvent(b->stream, ev.e[k], 0));
+      CK(launch_pack_bins_block(stage[k].p, width, missing ? mstage[k].as<uint8_t>() : nullptr,
+                                d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb, fb,
+                                d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(),
+                                d->bins_fm.as<uint8_t>(), b->error.as<uint32_t>(), b->stream));
+      CK(cudaEventRecord(ev.e[2 + k], b->stream));
+    }
     if (b->take_error()) throw DataError("Binned value exceeds the feature histogram range");
+    trace.mark("upload + pack (synchronized)");
     attach_bins_tmap(d.get());
     *out = d.release();
   });
@@ -539,6 +686,7 @@ struct mpsb_cuda_trainer {
     const bool timing = (options & MPSB_OPT_TIMING) && !leafwise;  // events are per depth level
     // Events captured into a graph cannot be timed, so timing runs launch directly.
     const bool use_graph = !(options & (MPSB_OPT_NO_GRAPH | MPSB_OPT_PER_NODE | MPSB_OPT_TIMING));
+    PhaseTrace capture_trace("run");
     for (uint32_t r = 0; r < rounds; ++r) {
       const bool g_only = root_reuse && root_saved;
       const int gi = g_only ? 1 : 0;
@@ -557,6 +705,7 @@ struct mpsb_cuda_trainer {
           CK(cudaStreamEndCapture(b->stream, &graph[gi]));
           CK(cudaGraphInstantiate(&graph_exec[gi], graph[gi], 0));
           kernels_per_round[gi] = k;
+          capture_trace.mark(gi ? "capture + instantiate (1)" : "capture + instantiate (0)");
         }
         CK(cudaGraphLaunch(graph_exec[gi], b->stream));
         stats.kernel_launches += kernels_per_round[gi];
@@ -619,10 +768,16 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
                    const mpsb_train_params* p, uint32_t options, uint32_t n_classes,
                    const ForestSpec* forest = nullptr, uint32_t softmax_classes = 0) {
   if (!b || !ds || !labels || !p) throw TrainingError("null argument");
+  PhaseTrace trace("setup");
   validate_training_params(*p);
   validate_tree_params(*p, ds->features);
   if (n != ds->n_rows) throw TrainingError("Training data, labels, or max_bins contract does not match");
-  validate_weights(weights, n);
+  // Weight checks and total; for a single boosted tree of a mean-type objective also the
+  // base score's label sum, in the same pass.
+  const bool single_mean = !forest && !softmax_classes && n_classes == 0 && label_mode_of(p->objective) != 0;
+  const RowSums sums = row_sums(weights, single_mean ? labels : nullptr, n, label_mode_of(p->objective),
+                                count_objective_name(p->objective));
+  trace.mark("validate weights, label sum");
   b->activate();
   t->b = b;
   t->ds = ds;
@@ -716,6 +871,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   cudaStream_t s = b->stream;
   const uint32_t W = tp.path_words;
 
+  trace.mark("parameters, root cache");
   // inputs
   double* d_labels = t->alloc<double>(n);
   CK(cudaMemcpyAsync(d_labels, labels, n * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -729,7 +885,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     // Margins [K][n] from the class priors (WeightedClassBaseScores,
     // multiclass_trainer.cpp:39-67); labels must be class ids (22-37).
     const uint32_t K = softmax_classes;
-    const double total = validate_weights(weights, n);
+    const double total = sums.total;
     std::vector<double> cw(K, 0.0);
     for (uint64_t i = 0; i < n; ++i) {
       const double y = labels[i];
@@ -744,24 +900,18 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
       t->base_scores[k] = std::log(std::max(1e-15, cw[k] / total));
       if (!std::isfinite(t->base_scores[k])) throw TrainingError("softmax base score is not finite");
     }
-    std::vector<double> init(static_cast<size_t>(n));
     a.preds = t->alloc<double>(size_t(K) * n);
-    for (uint32_t k = 0; k < K; ++k) {
-      std::fill(init.begin(), init.end(), t->base_scores[k]);
-      CK(cudaMemcpyAsync(a.preds + size_t(k) * n, init.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
-      CK(cudaStreamSynchronize(s));
-    }
+    for (uint32_t k = 0; k < K; ++k) CK(launch_fill_f64(a.preds + size_t(k) * n, n, t->base_scores[k], s));
   }
+  trace.mark("label/weight upload");
   if (!softmax_classes) t->base_scores.resize(T);
-  std::vector<double> init(static_cast<size_t>(n));
   if (!softmax_classes) a.preds = t->alloc<double>(size_t(T) * n);
   for (uint32_t k = 0; k < T && !softmax_classes; ++k) {
     t->base_scores[k] = forest ? forest->base_scores[k]
-                               : base_score(*p, labels, weights, n, t->ovr ? int64_t(k) : -1);
-    std::fill(init.begin(), init.end(), t->base_scores[k]);
-    CK(cudaMemcpyAsync(a.preds + size_t(k) * n, init.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
-    CK(cudaStreamSynchronize(s));
+                               : base_score(*p, labels, weights, n, t->ovr ? int64_t(k) : -1, &sums);
+    CK(launch_fill_f64(a.preds + size_t(k) * n, n, t->base_scores[k], s));
   }
+  trace.mark("base scores, predictions");
   if (p->n_monotonic) {
     int8_t* m = t->alloc<int8_t>(F);
     CK(cudaMemcpyAsync(m, p->monotonic_constraints, F, cudaMemcpyHostToDevice, s));
@@ -872,11 +1022,13 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     t->level_cells = t->alloc<unsigned long long>(std::max<uint32_t>(D, 1));
   }
   CK(cudaStreamSynchronize(s));
+  trace.mark("working state");
 }
 
 mpsb_cuda_model* export_model(mpsb_cuda_trainer* t, uint32_t tree_index,
                               bool with_predictions = true) {
   const TrainerDev& a = t->dev;
+  PhaseTrace trace("export");
   uint32_t rounds = 0;
   CK(cudaMemcpy(&rounds, a.round_counter, sizeof rounds, cudaMemcpyDeviceToHost));
   std::vector<uint32_t> counts(size_t(rounds) * a.n_trees);
@@ -908,10 +1060,16 @@ mpsb_cuda_model* export_model(mpsb_cuda_trainer* t, uint32_t tree_index,
                   a.model_nodes + (size_t(r) * a.n_trees + tree_index) * a.max_tree_nodes,
                   size_t(c) * sizeof(mpsb_tree_node), cudaMemcpyDeviceToHost));
   }
+  trace.mark("trees");
   if (with_predictions) {
-    m->train_predictions.resize(a.n_rows);
-    CK(cudaMemcpy(m->train_predictions.data(), a.preds + size_t(tree_index) * a.n_rows,
-                  size_t(a.n_rows) * sizeof(double), cudaMemcpyDeviceToHost));
+    const size_t bytes = size_t(a.n_rows) * sizeof(double);
+    m->device_predictions.alloc(bytes);
+    m->device_prediction_count = a.n_rows;
+    m->device = t->b->device;
+    CK(cudaMemcpyAsync(m->device_predictions.p, a.preds + size_t(tree_index) * a.n_rows, bytes,
+                       cudaMemcpyDeviceToDevice, t->b->stream));
+    CK(cudaStreamSynchronize(t->b->stream));
+    trace.mark("prediction copy (device)");
   }
   return m.release();
 }
@@ -1173,6 +1331,12 @@ int mpsb_cuda_model_tree_nodes(const mpsb_cuda_model* m, uint32_t t, mpsb_tree_n
 }
 int mpsb_cuda_model_train_predictions(const mpsb_cuda_model* m, double* out) {
   return guard([&] {
+    if (m->device_prediction_count) {
+      CK(cudaSetDevice(m->device));
+      CK(cudaMemcpy(out, m->device_predictions.p, m->device_prediction_count * sizeof(double),
+                    cudaMemcpyDeviceToHost));
+      return;
+    }
     if (m->train_predictions.empty())
       throw TrainingError("this model holds no training predictions (forest tree or loaded model)");
     std::memcpy(out, m->train_predictions.data(), m->train_predictions.size() * sizeof(double));

@@ -4,8 +4,10 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/mpsb_cuda.h"
@@ -15,6 +17,27 @@
 namespace mpsb {
 
 extern thread_local std::string g_error;
+
+// Allocator whose resize() leaves new elements uninitialized: buffers that a device copy
+// fills right away skip the zero fill (and its first-touch page faults).
+template <class T>
+struct NoInitAllocator : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInitAllocator<U>;
+  };
+  NoInitAllocator() = default;
+  template <class U>
+  NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <class U, class... Args>
+  void construct(U* p, Args&&... args) {
+    ::new (static_cast<void*>(p)) U(std::forward<Args>(args)...);
+  }
+};
 
 template <class F>
 int guard(F&& body) {
@@ -77,6 +100,7 @@ void validate_tree_params(const mpsb_train_params& p, uint32_t features);
 struct mpsb_cuda_backend {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host-to-device uploads that overlap kernels
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   int hist_mode = MPSB_HIST_FIXED;
   int sm_count = 0;
@@ -94,6 +118,7 @@ struct mpsb_cuda_backend {
   ~mpsb_cuda_backend() {
     if (t0) cudaEventDestroy(t0);
     if (t1) cudaEventDestroy(t1);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -119,7 +144,12 @@ struct mpsb_cuda_model {
   uint32_t n_trees = 0;
   double base = 0.0, learning_rate = 0.1;
   std::vector<std::vector<mpsb_tree_node>> trees;
-  std::vector<double> train_predictions;
+  std::vector<double, mpsb::NoInitAllocator<double>> train_predictions;  // softmax margins
+  // Training predictions of a trained regression model stay on the device (a copy of the
+  // trainer's) until a caller asks for them.
+  mpsb::DevBuf device_predictions;
+  uint64_t device_prediction_count = 0;
+  int device = 0;
   // Native softmax models: class count (0 for regression), per-class base scores and
   // class labels; trees are ordered (round, class).
   uint32_t class_count = 0;

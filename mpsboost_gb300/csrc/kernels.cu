@@ -2011,34 +2011,112 @@ __global__ void predict_kernel(const uint8_t* bins_fm, uint32_t n_rows, const ui
 // layouts with missing rows at 255: rows padded to nfb * 32 bytes and column blocks
 // [nfb][rows][32] (histograms of sparse and dense levels), and a feature-major copy (row
 // routing). Out-of-range bins set bit 0 of `error`.
+// Feature block fb0 + blockIdx.y of the dataset. `src` and `missing` hold the features from
+// src_f0 on (the whole matrix: src_f0 = 0; one staged feature block: src_f0 = 32 * fb0).
 __global__ void pack_bins_kernel(const void* src, uint32_t width, const uint8_t* missing,
                                  const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
                                  uint32_t nfb, uint8_t* out, uint8_t* out_blocked,
-                                 uint8_t* out_fm, uint32_t* error) {
+                                 uint8_t* out_fm, uint32_t* error, uint32_t fb0, uint32_t src_f0) {
   __shared__ uint8_t tile[32][129];
-  const uint32_t fb = blockIdx.y;
+  const uint32_t fb = fb0 + blockIdx.y;
   uint32_t bad = 0;
   for (uint32_t r0 = blockIdx.x * 128; r0 < n_rows; r0 += gridDim.x * 128) {
     // load 32 features x 128 rows (coalesced along rows)
-    for (uint32_t k = threadIdx.x; k < 32 * 128; k += blockDim.x) {
-      const uint32_t c = k / 128, r = k % 128;
-      const uint32_t f = fb * 32 + c, row = r0 + r;
-      uint8_t v = 0;
-      if (f < features && row < n_rows) {
-        const size_t idx = size_t(f) * n_rows + row;
-        const uint32_t b = width == 1 ? static_cast<const uint8_t*>(src)[idx]
-                                      : static_cast<const uint16_t*>(src)[idx];
-        const bool miss = missing != nullptr && missing[idx] != 0;
-        if (miss) {
-          if (bin_count[f] > 255) bad = 1;
-          v = uint8_t(kMissingSlot);
+    if (width == 1 && n_rows % 16 == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0 &&
+        (reinterpret_cast<uintptr_t>(missing) & 15u) == 0) {
+      // Sixteen rows per thread: 8 threads read one feature's 128 rows, a warp four
+      // features (four 128-byte requests per instruction).
+      for (uint32_t k = threadIdx.x; k < 32 * 8; k += blockDim.x) {
+        const uint32_t c = k / 8, r = (k % 8) * 16;
+        const uint32_t f = fb * 32 + c, row = r0 + r;
+        uint4 out4 = make_uint4(0, 0, 0, 0);
+        if (f < features && row < n_rows) {  // n_rows % 16 == 0: all sixteen rows exist
+          const size_t idx = size_t(f) * n_rows + row, sidx = size_t(f - src_f0) * n_rows + row;
+          const uint4 b16 = *reinterpret_cast<const uint4*>(static_cast<const uint8_t*>(src) + sidx);
+          const uint4 m16 = missing ? *reinterpret_cast<const uint4*>(missing + sidx) : make_uint4(0, 0, 0, 0);
+          const uint32_t nb = bin_count[f];
+          const uint32_t bw[4] = {b16.x, b16.y, b16.z, b16.w}, mw[4] = {m16.x, m16.y, m16.z, m16.w};
+          uint32_t ow[4];
+#pragma unroll
+          for (uint32_t j = 0; j < 4; ++j) {
+            uint32_t word = 0;
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+              const uint32_t b = (bw[j] >> (8 * q)) & 0xFFu;
+              uint32_t v;
+              if ((mw[j] >> (8 * q)) & 0xFFu) {
+                if (nb > 255) bad = 1;
+                v = kMissingSlot;
+              } else {
+                if (b >= nb) bad = 1;
+                v = b;
+              }
+              tile[c][r + 4 * j + q] = uint8_t(v);
+              word |= v << (8 * q);
+            }
+            ow[j] = word;
+          }
+          out4 = make_uint4(ow[0], ow[1], ow[2], ow[3]);
+          *reinterpret_cast<uint4*>(out_fm + idx) = out4;
         } else {
-          if (b >= bin_count[f]) bad = 1;
-          v = uint8_t(b);
+#pragma unroll
+          for (uint32_t q = 0; q < 16; ++q) tile[c][r + q] = 0;
         }
       }
-      tile[c][r] = v;
-      if (f < features && row < n_rows) out_fm[size_t(f) * n_rows + row] = v;
+    } else if (width == 1 && n_rows % 4 == 0 && (reinterpret_cast<uintptr_t>(src) & 3u) == 0 &&
+               (reinterpret_cast<uintptr_t>(missing) & 3u) == 0) {
+      // Four rows per thread: a warp reads one feature's 128 rows as one 128-byte request
+      // (the source may be page-locked host memory read over the host link).
+      for (uint32_t k = threadIdx.x; k < 32 * 32; k += blockDim.x) {
+        const uint32_t c = k / 32, r = (k % 32) * 4;
+        const uint32_t f = fb * 32 + c, row = r0 + r;
+        uint32_t word = 0;
+        if (f < features && row < n_rows) {  // n_rows % 4 == 0: all four rows exist
+          const size_t idx = size_t(f) * n_rows + row, sidx = size_t(f - src_f0) * n_rows + row;
+          const uint32_t b4 = *reinterpret_cast<const uint32_t*>(static_cast<const uint8_t*>(src) + sidx);
+          const uint32_t m4 = missing ? *reinterpret_cast<const uint32_t*>(missing + sidx) : 0u;
+          const uint32_t nb = bin_count[f];
+#pragma unroll
+          for (uint32_t q = 0; q < 4; ++q) {
+            const uint32_t b = (b4 >> (8 * q)) & 0xFFu;
+            uint32_t v;
+            if ((m4 >> (8 * q)) & 0xFFu) {
+              if (nb > 255) bad = 1;
+              v = kMissingSlot;
+            } else {
+              if (b >= nb) bad = 1;
+              v = b;
+            }
+            tile[c][r + q] = uint8_t(v);
+            word |= v << (8 * q);
+          }
+          *reinterpret_cast<uint32_t*>(out_fm + idx) = word;
+        } else {
+#pragma unroll
+          for (uint32_t q = 0; q < 4; ++q) tile[c][r + q] = 0;
+        }
+      }
+    } else {
+      for (uint32_t k = threadIdx.x; k < 32 * 128; k += blockDim.x) {
+        const uint32_t c = k / 128, r = k % 128;
+        const uint32_t f = fb * 32 + c, row = r0 + r;
+        uint8_t v = 0;
+        if (f < features && row < n_rows) {
+          const size_t sidx = size_t(f - src_f0) * n_rows + row;
+          const uint32_t b = width == 1 ? static_cast<const uint8_t*>(src)[sidx]
+                                        : static_cast<const uint16_t*>(src)[sidx];
+          const bool miss = missing != nullptr && missing[sidx] != 0;
+          if (miss) {
+            if (bin_count[f] > 255) bad = 1;
+            v = uint8_t(kMissingSlot);
+          } else {
+            if (b >= bin_count[f]) bad = 1;
+            v = uint8_t(b);
+          }
+        }
+        tile[c][r] = v;
+        if (f < features && row < n_rows) out_fm[size_t(f) * n_rows + row] = v;
+      }
     }
     __syncthreads();
     // store 128 rows x 32 bytes: row-major rows padded to nfb * 32 bytes
@@ -2154,6 +2232,16 @@ cudaError_t launch_partition_finish(const TrainerDev& a, int grid, cudaStream_t 
   partition_scatter_kernel<<<grid, kPartThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
+__global__ void fill_f64_kernel(double* dst, uint64_t n, double value) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    dst[i] = value;
+}
+cudaError_t launch_fill_f64(double* dst, uint64_t n, double value, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, 4096);
+  fill_f64_kernel<<<unsigned(blocks), 256, 0, s>>>(dst, n, value);
+  return cudaGetLastError();
+}
 cudaError_t launch_apply_leaves(const TrainerDev& a, int grid, cudaStream_t s) {
   apply_leaves_kernel<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
@@ -2175,7 +2263,17 @@ cudaError_t launch_pack_bins(const void* src, uint32_t width, const uint8_t* mis
   const uint32_t gx = std::min<uint32_t>((n_rows + 127) / 128, 4096u);
   pack_bins_kernel<<<dim3(gx > 0 ? gx : 1, nfb), 256, 0, s>>>(src, width, missing, bin_count,
                                                               n_rows, features, nfb, out_rows,
-                                                              out_blocked, out_fm, error);
+                                                              out_blocked, out_fm, error, 0u, 0u);
+  return cudaGetLastError();
+}
+cudaError_t launch_pack_bins_block(const void* src_block, uint32_t width, const uint8_t* missing_block,
+                                   const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
+                                   uint32_t nfb, uint32_t fb, uint8_t* out_rows, uint8_t* out_blocked,
+                                   uint8_t* out_fm, uint32_t* error, cudaStream_t s) {
+  const uint32_t gx = std::min<uint32_t>((n_rows + 127) / 128, 4096u);
+  pack_bins_kernel<<<dim3(gx > 0 ? gx : 1, 1), 256, 0, s>>>(src_block, width, missing_block, bin_count,
+                                                            n_rows, features, nfb, out_rows, out_blocked,
+                                                            out_fm, error, fb, fb * kBlockFeatures);
   return cudaGetLastError();
 }
 cudaError_t launch_predict(const uint8_t* bins_fm, uint32_t n_rows, uint32_t nfb,

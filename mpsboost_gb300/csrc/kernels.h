@@ -135,6 +135,7 @@ bool encode_bins_tmap(CUtensorMap* map, const uint8_t* bins, uint64_t row_stride
 
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,
                               cudaStream_t stream);
+cudaError_t launch_fill_f64(double* dst, uint64_t n, double value, cudaStream_t stream);
 cudaError_t launch_round_begin(const TrainerDev& a, cudaStream_t stream);
 cudaError_t launch_gradients(const TrainerDev& a, int grid, cudaStream_t stream);
 cudaError_t launch_round_setup(const TrainerDev& a, cudaStream_t stream);
@@ -166,6 +167,12 @@ cudaError_t launch_predict(const uint8_t* bins_fm, uint32_t n_rows, uint32_t nfb
                            const uint32_t* tree_offsets, uint32_t n_trees, double base,
                            double learning_rate, double* out, uint32_t* error,
                            cudaStream_t stream);
+// One feature block fb of the dataset from a staged copy of its source features
+// (src_block / missing_block start at feature 32 * fb).
+cudaError_t launch_pack_bins_block(const void* src_block, uint32_t width, const uint8_t* missing_block,
+                                   const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
+                                   uint32_t nfb, uint32_t fb, uint8_t* out_rows, uint8_t* out_blocked,
+                                   uint8_t* out_fm, uint32_t* error, cudaStream_t stream);
 cudaError_t launch_pack_bins(const void* src, uint32_t width, const uint8_t* missing,
                              const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
                              uint32_t nfb, uint8_t* out_rows, uint8_t* out_blocked,

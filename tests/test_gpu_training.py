@@ -241,6 +241,23 @@ def test_training_errors(backend):
         mb.train_regressor(backend, binned, y, learning_rate=0.0)
     with pytest.raises(mb.TrainingError, match="binary"):
         mb.train_regressor(backend, binned, y, objective="binary_logistic", n_estimators=1)
+    # The reference's check order: every weight check before any label check, each at its
+    # first failing row.
+    big_w = w.copy()
+    big_w[10:12] = 1.7e308
+    with pytest.raises(mb.TrainingError, match="sample weight sum overflowed"):
+        mb.train_regressor(backend, binned, y, big_w, n_estimators=1, max_depth=2)
+    with pytest.raises(mb.TrainingError, match="finite non-negative"):
+        mb.train_regressor(backend, binned, bad, -w, n_estimators=1, max_depth=2)
+    big_y = y.copy()
+    big_y[3:5] = 1.7e308
+    with pytest.raises(mb.TrainingError, match="Label accumulation overflowed"):
+        mb.train_regressor(backend, binned, big_y, n_estimators=1, max_depth=2)
+    big_y[200] = np.nan
+    with pytest.raises(mb.TrainingError, match="Label accumulation overflowed"):
+        mb.train_regressor(backend, binned, big_y, n_estimators=1, max_depth=2)
+    with pytest.raises(mb.TrainingError, match="poisson labels must be non-negative"):
+        mb.train_regressor(backend, binned, -np.abs(y) - 1, objective="poisson", n_estimators=1, max_depth=2)
 
 
 def test_scale_properties(backend):

@@ -230,17 +230,32 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
       y = (yb == class_bits || (t == 0 && (yb << 1) == 0)) ? 1.0 : 0.0;
     }
     double g = 0.0, h = 0.0;
-    if (a.n_classes) {
-      if (!softmax_pair(a, y, i, *a.round_counter % a.n_classes, &g, &h)) bad = 1;
-    } else {
+    if (a.objective == 0 && !a.n_classes) {
+      // Squared error (the objective_pair case 0 then the weight products): g = w (p - y),
+      // h = w; two FP64 operations per row on the narrow FP64 pipe.
       const double pred = a.preds[tree_off + i];
-      if (!objective_pair(a.objective, y, pred, a.params, &g, &h)) bad = 1;
-    }
-    if (a.weights != nullptr) {
-      const double w = a.weights_per_tree ? a.weights[tree_off + i] : a.weights[i];
-      g = __dmul_rn(g, w);
-      h = unit_h ? w : __dmul_rn(h, w);
-      if (!f64_finite(g) || !f64_finite(h) || f64_negative(h)) bad = 1;
+      g = __dsub_rn(pred, y);  // p + (-y): negation is exact
+      if (!f64_finite(y) || !f64_finite(pred) || !f64_finite(g)) bad = 1;
+      h = 1.0;
+      if (a.weights != nullptr) {
+        const double w = a.weights_per_tree ? a.weights[tree_off + i] : a.weights[i];
+        g = __dmul_rn(g, w);
+        h = w;
+        if (!f64_finite(g) || !f64_finite(h) || f64_negative(h)) bad = 1;
+      }
+    } else {
+      if (a.n_classes) {
+        if (!softmax_pair(a, y, i, *a.round_counter % a.n_classes, &g, &h)) bad = 1;
+      } else {
+        const double pred = a.preds[tree_off + i];
+        if (!objective_pair(a.objective, y, pred, a.params, &g, &h)) bad = 1;
+      }
+      if (a.weights != nullptr) {
+        const double w = a.weights_per_tree ? a.weights[tree_off + i] : a.weights[i];
+        g = __dmul_rn(g, w);
+        h = unit_h ? w : __dmul_rn(h, w);
+        if (!f64_finite(g) || !f64_finite(h) || f64_negative(h)) bad = 1;
+      }
     }
     const float g32 = f64_to_f32_rn(g), h32 = f64_to_f32_rn(h);
     if (!isfinite(g32) || !isfinite(h32)) bad = 1;
@@ -1881,7 +1896,7 @@ __global__ void leafwise_finish_kernel(TrainerDev a) {
 // ------------------------------------------------------------------------------------
 // Leaf application and round end
 // ------------------------------------------------------------------------------------
-__global__ void apply_leaves_kernel(TrainerDev a) {
+__global__ void __launch_bounds__(256, 4) apply_leaves_kernel(TrainerDev a) {
   if (a.skip_apply) return;  // forest trees: no training predictions
   const double lr = a.params.learning_rate;
   uint32_t err = 0;

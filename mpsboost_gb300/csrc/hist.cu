@@ -346,16 +346,22 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int nrows = int(min(32u, row_count - tile_pos));
         const uint8_t* sb = wbins + size_t(st) * 32 * 32;
         const uint2* sv = wval + st * 32;
-        for (int j = 0; j < nrows; j += 4) {
-          const int r = j + int(rot);
-          if (r < nrows) {
-            const uint32_t w = *reinterpret_cast<const uint32_t*>(sb + r * 32 + quad_byte);
-            const uint2 q = sv[r];
+        auto reduce_rows = [&](int r) {
+          const uint32_t w = *reinterpret_cast<const uint32_t*>(sb + r * 32 + quad_byte);
+          const uint2 q = sv[r];
 #pragma unroll
-            for (uint32_t i = 0; i < 4; ++i) {
-              const uint32_t sel = (i + rot) & 3u;
-              accumulate(quad_byte + sel, (w >> (8u * sel)) & 0xFFu, q);
-            }
+          for (uint32_t i = 0; i < 4; ++i) {
+            const uint32_t sel = (i + rot) & 3u;
+            accumulate(quad_byte + sel, __byte_perm(w, 0u, 0x4440u | sel), q);  // byte sel of w
+          }
+        };
+        if (nrows == 32) {  // full tile: no bounds tests, the eight groups unrolled
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) reduce_rows(j + int(rot));
+        } else {
+          for (int j = 0; j < nrows; j += 4) {
+            const int r = j + int(rot);
+            if (r < nrows) reduce_rows(r);
           }
         }
         __syncwarp();

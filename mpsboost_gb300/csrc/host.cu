@@ -549,7 +549,13 @@ struct mpsb_cuda_trainer {
     return bufs.back()->as<T>();
   }
 
+  cudaStream_t side = nullptr;                      // work beside the main stream
+  cudaEvent_t fork_ev = nullptr, zero_ev = nullptr;  // fork to / join from `side`
+
   ~mpsb_cuda_trainer() {
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (zero_ev) cudaEventDestroy(zero_ev);
+    if (side) cudaStreamDestroy(side);
     for (int i = 0; i < 2; ++i) {
       if (graph_exec[i]) cudaGraphExecDestroy(graph_exec[i]);
       if (graph[i]) cudaGraphDestroy(graph[i]);
@@ -576,7 +582,11 @@ struct mpsb_cuda_trainer {
     const uint32_t levels = std::max<uint32_t>(depth, 1);
     for (uint32_t d = 0; d < levels; ++d) {
       const int parity = int(d & 1);
-      CK(launch_zero_build_slots(dev, grid(8), s)); ++k;
+      if (d == 0) {
+        CK(launch_zero_build_slots(dev, grid(8), s)); ++k;
+      } else {
+        CK(cudaStreamWaitEvent(s, zero_ev, 0));  // this level's slots were cleared beside the partition
+      }
       if (record_events) CK(cudaEventRecord(events[2 * d], s));
       if (options & MPSB_OPT_PER_NODE) {
         k += enqueue_hist_per_node(d);
@@ -603,6 +613,12 @@ struct mpsb_cuda_trainer {
       }
       CK(launch_finalize(dev, parity, d, s)); ++k;
       if (d + 1 < depth) {
+        // The next level's build slots (named by the finalize) are cleared on the side
+        // stream while the partition moves the rows.
+        CK(cudaEventRecord(fork_ev, s));
+        CK(cudaStreamWaitEvent(side, fork_ev, 0));
+        CK(launch_zero_build_slots(dev, grid(8), side)); ++k;
+        CK(cudaEventRecord(zero_ev, side));
         CK(launch_partition(dev, grid(4), s)); k += kPartitionKernels;
       }
     }
@@ -781,6 +797,9 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   b->activate();
   t->b = b;
   t->ds = ds;
+  CK(cudaStreamCreateWithFlags(&t->side, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&t->fork_ev, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&t->zero_ev, cudaEventDisableTiming));
   t->params = *p;
   t->options = options;
   t->depth = p->max_depth;

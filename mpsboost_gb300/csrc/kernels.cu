@@ -362,6 +362,10 @@ __global__ void round_setup_kernel(TrainerDev a) {
 
 // Zero the histogram slots of the current build list.
 __global__ void zero_build_slots_kernel(TrainerDev a) {
+  // The level's split scan publishes node maxima into node_screen: clear them first.
+  if (a.node_screen)
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.max_level_nodes; i += gridDim.x * blockDim.x)
+      a.node_screen[i] = 0u;
   const uint64_t words_per_slot = uint64_t(a.features) * kSlots * 3;
   const uint64_t total = uint64_t(a.ctl->n_build) * (words_per_slot / 2);
   for (uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; idx < total;
@@ -2202,8 +2206,8 @@ cudaError_t launch_split_scan(const TrainerDev& a, int parity, int grid, cudaStr
   if (threads < 32 || threads > kScanThreadsMax || threads % 32) return cudaErrorInvalidValue;
   const bool fixed = a.mode == kModeFixed;
   if (split_scan_kernels(a) == 2) {
-    cudaError_t err = cudaMemsetAsync(a.node_screen, 0, size_t(a.max_level_nodes) * sizeof(uint32_t), s);
-    if (err != cudaSuccess) return err;
+    // node_screen was cleared by the level's zero_build_slots_kernel.
+    cudaError_t err;
     // The screen phase holds about half the registers: twice the CTAs.
     err = fixed ? launch_scan_variant<true, true>(a, parity, 2 * grid, threads, s)
                 : launch_scan_variant<false, true>(a, parity, 2 * grid, threads, s);

@@ -56,7 +56,8 @@ struct TrainerDev {
   SplitRec* partial;            // [max_level_nodes][n_fchunks]
   // Two-phase split scan (scan_two_phase: the FP32 screen applies): [max_level_nodes]
   // maximum FP32 screen score of each node's certainly admissible candidates (float
-  // bits; zeroed before every scan) and [max_level_nodes][n_fchunks] each chunk's maximum
+  // bits; zeroed by each level's zero_build_slots_kernel, which every scan of the trainer
+  // follows) and [max_level_nodes][n_fchunks] each chunk's maximum
   // and exact flag. Null node_screen: one launch, each feature screened on its own (the
   // per-feature entry point needs every feature's best split).
   uint32_t* node_screen;

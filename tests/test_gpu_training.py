@@ -176,6 +176,24 @@ def test_root_reuse_is_exact(backend, monkeypatch, objective):
     assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
 
 
+@pytest.mark.parametrize("rows", [20_000, 20_003])
+def test_dataset_upload_layouts(backend, rows):
+    """The per-block upload and pack gives the same trees from u8 and from u16 bins, with
+    and without missing values, on row counts that take the 16-byte and the byte load
+    paths of the pack (70 features: a partial last feature block)."""
+    import dataclasses
+
+    x, y, w = _data(47, rows, 70, 0.03, 2)
+    params = dict(n_estimators=2, learning_rate=0.3, max_depth=6, min_samples_leaf=2)
+    narrow = mb.quantize_dense(x, 200)
+    wide = dataclasses.replace(narrow, bins=narrow.bins.astype(np.uint16), _device={})
+    a = mb.train_regressor(backend, narrow, y, w, **params)
+    b = mb.train_regressor(backend, wide, y, w, **params)
+    for t1, t2 in zip(a.trees, b.trees):
+        assert t1.tobytes() == t2.tobytes()
+    assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
+
+
 @pytest.mark.parametrize("threads", ["768", "512"])
 def test_tma_staging_equals_cp_async(backend, monkeypatch, threads):
     """Row-major levels whose gathered rows arrive by TMA gather4 copies give the same

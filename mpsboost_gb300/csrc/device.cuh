@@ -20,7 +20,10 @@ constexpr uint32_t kApplyChunk = 4096;    // rows per leaf-application chunk
 
 // kModeFixedG: fixed point, gradient limbs only (a root build whose count and hessian
 // histograms are restored from the fit's first round).
-enum : int { kModeFixed = 0, kModeFloat = 1, kModeFixedG = 2 };
+// kModeFixedCG: fixed point, count and gradient limbs; every row's hessian is the same
+// quantized unit (unweighted squared error and quantile: h = 1), so a cell's hessian
+// sum is its count times that unit, exactly.
+enum : int { kModeFixed = 0, kModeFloat = 1, kModeFixedG = 2, kModeFixedCG = 3 };
 
 // Device status bits (ORed into TrainerState::error).
 enum : uint32_t {

@@ -111,6 +111,10 @@ struct HistSmem<kModeFixed> {  // count, g_lo, g_hi, h_lo, h_hi: five u32 words 
   static constexpr size_t kBytes = 5ull * kSlots * kBlockFeatures * sizeof(uint32_t);
 };
 template <>
+struct HistSmem<kModeFixedCG> {  // count, g_lo, g_hi
+  static constexpr size_t kBytes = 3ull * kSlots * kBlockFeatures * sizeof(uint32_t);
+};
+template <>
 struct HistSmem<kModeFixedG> {  // g_lo, g_hi
   static constexpr size_t kBytes = 2ull * kSlots * kBlockFeatures * sizeof(uint32_t);
 };
@@ -195,6 +199,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint8_t* bins = a.bins + size_t(fb) * a.bins_block_stride;
     const int kg = a.trees[e.tree].kg;
     const int kh = a.trees[e.tree].kh;
+    // Unit-hessian builds: the quantized hessian of every row, round_half_even(2^kh).
+    const long long q_unit_h = MODE == kModeFixedCG ? quantize_f32(1.0f, kh) : 0ll;
 
     // Zero the CTA histogram.
     {
@@ -246,6 +252,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       } else if constexpr (MODE == kModeFixedG) {
         red_shared_u32<0>(addr, q.x & 0xFFFFu);
         red_shared_u32<1u * CELLS * 4u>(addr, uint32_t(int32_t(q.x) >> 16));
+      } else if constexpr (MODE == kModeFixedCG) {
+        red_shared_u32<0>(addr, 1u);
+        red_shared_u32<1u * CELLS * 4u>(addr, q.x & 0xFFFFu);
+        red_shared_u32<2u * CELLS * 4u>(addr, uint32_t(int32_t(q.x) >> 16));
       } else {
         red_shared_u32<0>(addr, 1u);
         red_shared_f32<CELLS * 4u>(addr, __uint_as_float(q.x));
@@ -306,7 +316,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint32_t glo = uint32_t(qg) & 0xFFFFu, ghi = uint32_t(qg >> 16) & 0xFFFFu;
             const uint32_t hlo = uint32_t(qh) & 0xFFFFu, hhi = uint32_t(qh >> 16) & 0xFFFFu;
             v = make_uint2(glo | (hlo << 16), ghi | (hhi << 16));
-          } else if constexpr (MODE == kModeFixedG) {
+          } else if constexpr (MODE == kModeFixedG || MODE == kModeFixedCG) {
             // |q| <= 2^30: the low 32 bits hold q in two's complement; the reductions
             // take its unsigned low and signed high 16 bits.
             v = make_uint2(uint32_t(quantize_f32(p.x, kg)), 0u);
@@ -391,6 +401,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t* w = reinterpret_cast<const uint32_t*>(hist_smem);
         const long long g = (long long)int32_t(w[CELLS + idx]) * 65536 + (long long)w[idx];
         if (g != 0) atomicAdd(dst + 1, (unsigned long long)g);
+      } else if constexpr (MODE == kModeFixedCG) {
+        const uint32_t* w = reinterpret_cast<const uint32_t*>(hist_smem);
+        const uint32_t cnt = w[idx];
+        if (cnt == 0) continue;
+        const long long g = (long long)int32_t(w[2 * CELLS + idx]) * 65536 + (long long)w[CELLS + idx];
+        atomicAdd(dst + 0, (unsigned long long)cnt);
+        atomicAdd(dst + 1, (unsigned long long)g);
+        atomicAdd(dst + 2, (unsigned long long)((long long)cnt * q_unit_h));
       } else {
         const uint32_t* hc = reinterpret_cast<const uint32_t*>(hist_smem);
         const float* hgf = reinterpret_cast<const float*>(hc + CELLS);
@@ -443,6 +461,10 @@ cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int gr
   if (a.mode == kModeFixedG) {
     if (cfg.root_threads == 1024) return launch_variant<kModeFixedG, 1024, 2>(a, grid, stream);
     return launch_variant<kModeFixedG, 768, 2>(a, grid, stream);
+  }
+  if (a.mode == kModeFixedCG) {  // 96 KB histogram: room for 1024 threads
+    if (cfg.root_threads == 1024) return launch_variant<kModeFixedCG, 1024, 2>(a, grid, stream);
+    return launch_variant<kModeFixedCG, 768, 2>(a, grid, stream);
   }
   if (a.mode == kModeFixed) {
     // Row-major view of the matrix the tensor map describes: gather with TMA.

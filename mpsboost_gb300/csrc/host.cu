@@ -649,7 +649,7 @@ struct mpsb_cuda_trainer {
       CK(launch_leafwise_select(dev, s)); ++k;
       CK(launch_partition(dev, grid(4), s)); k += kPartitionKernels;
       CK(launch_zero_build_slots(dev, grid(8), s)); ++k;
-      CK(launch_hist_build(dev, hcfg, grid(1), s)); ++k;
+      CK(launch_hist_build(build_view(), hcfg, grid(1), s)); ++k;
       CK(launch_subtract(dev, grid(8), s)); ++k;
       CK(launch_split_scan(dev, 1, grid(4), s)); k += split_scan_kernels(dev);
       CK(launch_leafwise_merge(dev, s)); ++k;
@@ -658,11 +658,18 @@ struct mpsb_cuda_trainer {
     return k;
   }
 
+  // The histogram launch's view: unit-hessian fixed-point builds count and gradient limbs.
+  TrainerDev build_view() const {
+    TrainerDev v = dev;
+    if (v.mode == kModeFixed && v.unit_hess) v.mode = kModeFixedCG;
+    return v;
+  }
+
   // Dense levels (every row of a node close to the next) read the column-blocked copy of
   // the bins, whose 32-byte block rows are consecutive; sparse levels read the padded
   // row-major copy, whose 128-byte row line serves all feature blocks through L2.
   TrainerDev level_view(uint32_t d) const {
-    TrainerDev v = dev;
+    TrainerDev v = build_view();
     if (d < blocked_levels) {
       v.bins = ds->bins_blocked.as<uint8_t>();
       v.bins_row_stride = kBlockFeatures;
@@ -900,6 +907,11 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     CK(cudaMemcpyAsync(d_w, weights, n * sizeof(double), cudaMemcpyHostToDevice, s));
     a.weights = d_w;
   }
+  // Squared error and quantile have h = 1 per row; without weights every row's quantized
+  // hessian is the same unit (MPSB_UNIT_HESS=0 builds the hessian limbs anyway).
+  a.unit_hess = !weights && !softmax_classes && n_classes == 0 &&
+                (p->objective == MPSB_SQUARED_ERROR || p->objective == MPSB_QUANTILE);
+  if (const char* v = std::getenv("MPSB_UNIT_HESS")) a.unit_hess = a.unit_hess && std::atoi(v) != 0;
   if (softmax_classes) {
     // Margins [K][n] from the class priors (WeightedClassBaseScores,
     // multiclass_trainer.cpp:39-67); labels must be class ids (22-37).

@@ -372,6 +372,13 @@ __global__ void zero_build_slots_kernel(TrainerDev a) {
        idx += uint64_t(gridDim.x) * blockDim.x) {
     const uint32_t e = uint32_t(idx / (words_per_slot / 2));
     const uint64_t w = idx % (words_per_slot / 2);
+    if (a.tree_feature_masks) {
+      // A forest tree reads only its own features' histograms (and feature 0's, for the
+      // root statistics): the others are neither cleared nor subtracted nor scanned.
+      const uint32_t f = uint32_t(w * 2 / (kSlots * 3));
+      const uint32_t mask = a.tree_feature_masks[size_t(a.build[e].tree) * a.params.path_words + (f >> 5)];
+      if (f != 0 && !((mask >> (f & 31)) & 1u)) continue;
+    }
     reinterpret_cast<ulonglong2*>(a.hist + a.build[e].slot * words_per_slot)[w] =
         make_ulonglong2(0, 0);
   }
@@ -469,6 +476,12 @@ __global__ void subtract_kernel(TrainerDev a) {
        idx += uint64_t(gridDim.x) * blockDim.x) {
     const SubEntry e = a.sub[idx / bins_per_slot];
     const uint64_t b = idx % bins_per_slot;
+    if (a.tree_feature_masks) {  // a forest tree's own features only (sub[k] pairs build[k])
+      const uint32_t f = uint32_t(b / kSlots);
+      const uint32_t mask =
+          a.tree_feature_masks[size_t(a.build[idx / bins_per_slot].tree) * a.params.path_words + (f >> 5)];
+      if (!((mask >> (f & 31)) & 1u)) continue;
+    }
     unsigned long long* p = a.hist + (e.parent_slot * bins_per_slot + b) * 3;
     const unsigned long long* c = a.hist + (e.built_slot * bins_per_slot + b) * 3;
     const unsigned long long pc = p[0], cc = c[0];

@@ -39,6 +39,8 @@ struct TrainerDev {
   const uint32_t* feature_rank;   // [n_trees][features] or null (rank = feature)
   const uint32_t* tree_seeds;     // [n_trees] or null (params.random_seed)
   uint32_t skip_apply;            // 1: no prediction update (forest trees are single-round)
+  uint32_t unit_hess;             // every row's hessian is 1 (no weights; squared error or
+                                  // quantile): fixed-point builds take kModeFixedCG
   TreeState* trees;             // [n_trees]
   TreeParams params;
   const int8_t* monotonic;      // [features] or null

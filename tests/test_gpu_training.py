@@ -65,6 +65,13 @@ FIXED_CASES = {
                  params=dict(n_estimators=2, learning_rate=0.1, max_depth=10, min_samples_leaf=2)),
     "quantile": dict(seed=31, rows=2000, feats=4, nan=0.0, ints=0, max_bins=64, objective="quantile",
                      params=dict(n_estimators=3, learning_rate=0.3, max_depth=4, objective_alpha=0.7)),
+    # No sample weights: squared error and quantile have h = 1 on every row, so the
+    # histograms build count and gradient limbs only (the hessian is count x unit).
+    "unweighted": dict(seed=32, rows=20000, feats=40, nan=0.03, ints=2, max_bins=255, unweighted=True,
+                       params=dict(n_estimators=3, learning_rate=0.2, max_depth=8, min_samples_leaf=2)),
+    "unweighted_quantile": dict(seed=33, rows=6000, feats=12, nan=0.0, ints=1, max_bins=128, unweighted=True,
+                                objective="quantile",
+                                params=dict(n_estimators=3, learning_rate=0.3, max_depth=6, objective_alpha=0.3)),
 }
 
 
@@ -73,6 +80,8 @@ def test_fixed_point_bit_exact_to_replica(backend, port, name):
     c = FIXED_CASES[name]
     objective = c.get("objective", "squared_error")
     x, y, w = _data(c["seed"], c["rows"], c["feats"], c["nan"], c["ints"], objective)
+    if c.get("unweighted"):
+        w = None
     params = dict(c["params"], objective=objective)
     binned = mb.quantize_dense(x, c["max_bins"])
     model = mb.train_regressor(backend, binned, y, w, **params)
@@ -174,6 +183,28 @@ def test_root_reuse_is_exact(backend, monkeypatch, objective):
     for t1, t2 in zip(a.trees, b.trees):
         assert t1.tobytes() == t2.tobytes()
     assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
+
+
+def test_unit_hessian_builds_equal_full_builds(backend, monkeypatch):
+    """Count-and-gradient histograms (unweighted squared error and quantile) give the same
+    trees as five-limb histograms, depth-wise, leaf-wise and for a forest."""
+    x, y, _ = _data(48, 30000, 45, 0.02, 3)
+    binned = mb.quantize_dense(x, 255)
+    cases = [dict(n_estimators=3, learning_rate=0.2, max_depth=8, min_samples_leaf=3),
+             dict(n_estimators=3, learning_rate=0.3, max_depth=6, objective="quantile", objective_alpha=0.6),
+             dict(n_estimators=2, learning_rate=0.3, max_depth=8, growth_strategy="leaf_wise", max_leaves=40)]
+    fast = [mb.train_regressor(backend, binned, y, None, **p) for p in cases]
+    counts, subsets, seeds = mb.forest_samples(30000, 45, 4, random_state=5, max_features=0.5)
+    forest_fast = mb.train_forest(backend, binned, y, None, row_counts=counts, feature_subsets=subsets,
+                                  seeds=seeds, max_depth=9, min_samples_leaf=2)
+    monkeypatch.setenv("MPSB_UNIT_HESS", "0")
+    full = [mb.train_regressor(backend, binned, y, None, **p) for p in cases]
+    forest_full = mb.train_forest(backend, binned, y, None, row_counts=counts, feature_subsets=subsets,
+                                  seeds=seeds, max_depth=9, min_samples_leaf=2)
+    for a, b in zip(fast + forest_fast, full + forest_full):
+        assert a.base_score == b.base_score
+        for t1, t2 in zip(a.trees, b.trees):
+            assert t1.tobytes() == t2.tobytes()
 
 
 @pytest.mark.parametrize("rows", [20_000, 20_003])

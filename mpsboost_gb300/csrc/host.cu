@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <limits>
 #include <memory>
 #include <new>
@@ -291,6 +292,60 @@ double base_score(const mpsb_train_params& p, const double* y, const double* w, 
     default:  // squared error, poisson and tweedie take the row_sums path above
       throw TrainingError("unknown training objective");
   }
+}
+
+// Runs body(0..count-1) on worker threads (each index once); rethrows the first error.
+template <class F>
+void parallel_trees(uint32_t count, F&& body) {
+  const uint32_t workers = std::min<uint32_t>(count, std::max(1u, std::thread::hardware_concurrency()));
+  std::atomic<uint32_t> next{0};
+  std::vector<std::exception_ptr> errors(workers);
+  auto run = [&](uint32_t w) {
+    try {
+      for (uint32_t i = next.fetch_add(1); i < count; i = next.fetch_add(1)) body(i);
+    } catch (...) {
+      errors[w] = std::current_exception();
+    }
+  };
+  std::vector<std::thread> pool;
+  for (uint32_t w = 1; w < workers; ++w) pool.emplace_back(run, w);
+  if (workers > 0) run(0);
+  for (auto& t : pool) t.join();
+  for (auto& e : errors)
+    if (e) std::rethrow_exception(e);
+}
+
+// InitialBaseScore of a mean-type objective (label_mode 1 or 2) over a row multiset in
+// row order, row r taken m[r] times: the same sequence of additions as over the expanded
+// sample, without expanding it.
+double multiset_base_score(const mpsb_train_params& p, const double* y, const double* w,
+                           const uint8_t* m, uint64_t n, int mode) {
+  double total = 0.0, s = 0.0;
+  bool bad_w = false, bad_y = false;
+  for (uint64_t r = 0; r < n; ++r) {
+    for (uint32_t c = 0; c < m[r]; ++c) {
+      const double x = w ? w[r] : 1.0;
+      total += x;
+      s += y[r] * x;
+    }
+    if (m[r]) {
+      const double x = w ? w[r] : 1.0;
+      bad_w |= !std::isfinite(x) || x < 0.0;
+      bad_y |= !std::isfinite(y[r]) || (mode == 2 && y[r] < 0.0);
+    }
+  }
+  if (bad_w || bad_y || !std::isfinite(total) || !(total > 0.0) || !std::isfinite(s)) {
+    // The exact error of the reference's sequential checks, over the expanded sample.
+    std::vector<double> ys, ws;
+    for (uint64_t r = 0; r < n; ++r)
+      for (uint32_t c = 0; c < m[r]; ++c) {
+        ys.push_back(y[r]);
+        if (w) ws.push_back(w[r]);
+      }
+    return base_score(p, ys.data(), w ? ws.data() : nullptr, ys.size(), -1);
+  }
+  if (mode == 1) return s / total;
+  return std::log(std::max(1e-15, s / total));
 }
 
 uint32_t effective_max_leaves(const mpsb_train_params& p) {  // tree_structure.cpp:54-62
@@ -1255,10 +1310,17 @@ int mpsb_cuda_train_forest(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
     // memory, so batch as many trees as fit in half of the free memory.
     mpsb_train_params tp = *p;
     tp.n_estimators = 1;
+    // Sample sizes of every tree (independent trees: worker threads).
+    std::vector<uint64_t> sample_size(n_trees, 0);
+    parallel_trees(n_trees, [&](uint32_t t) {
+      uint64_t c = 0;
+      const uint8_t* m = row_counts + size_t(t) * n;
+      for (uint64_t r = 0; r < n; ++r) c += m[r];
+      sample_size[t] = c;
+    });
     uint64_t cap_all = 1;
     for (uint32_t t = 0; t < n_trees; ++t) {
-      uint64_t c = 0;
-      for (uint64_t r = 0; r < n; ++r) c += row_counts[size_t(t) * n + r];
+      const uint64_t c = sample_size[t];
       if (c == 0) throw TrainingError("a forest tree's row sample must not be empty");
       if (c >= 0x80000000ull) throw UnsupportedError("a forest tree's row sample exceeds 2^31 rows");
       cap_all = std::max(cap_all, c);
@@ -1287,38 +1349,42 @@ int mpsb_cuda_train_forest(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
       fs.n_trees = B;
       fs.count.resize(B);
       for (uint32_t k = 0; k < B; ++k) {
-        uint64_t c = 0;
-        for (uint64_t r = 0; r < n; ++r) c += row_counts[size_t(t0 + k) * n + r];
-        fs.count[k] = uint32_t(c);
-        fs.cap = std::max<uint32_t>(fs.cap, uint32_t(c));
+        fs.count[k] = uint32_t(sample_size[t0 + k]);
+        fs.cap = std::max<uint32_t>(fs.cap, fs.count[k]);
       }
       fs.sample.assign(size_t(B) * fs.cap, 0);
       fs.masks.assign(size_t(B) * W, 0);
       fs.ranks.assign(size_t(B) * F, 0);
       fs.base_scores.resize(B);
       if (seeds) fs.seeds.assign(seeds + t0, seeds + t0 + B);
-      std::vector<double> ys, ws;
-      for (uint32_t k = 0; k < B; ++k) {
+      const int mode = label_mode_of(tp.objective);
+      parallel_trees(B, [&](uint32_t k) {
         const uint8_t* m = row_counts + size_t(t0 + k) * n;
         uint32_t* dst = fs.sample.data() + size_t(k) * fs.cap;
-        ys.clear();
-        ws.clear();
         uint32_t pos = 0;
         for (uint64_t r = 0; r < n; ++r)
-          for (uint32_t c = 0; c < m[r]; ++c) {
-            dst[pos++] = uint32_t(r);
-            ys.push_back(labels[r]);
-            if (weights) ws.push_back(weights[r]);
+          for (uint32_t c = 0; c < m[r]; ++c) dst[pos++] = uint32_t(r);
+        // The reference fits the tree on its sample: base score over the sample's rows in
+        // order (each row as often as it was drawn).
+        if (mode) {
+          fs.base_scores[k] = multiset_base_score(tp, labels, weights, m, n, mode);
+        } else {
+          std::vector<double> ys, ws;
+          ys.reserve(pos);
+          if (weights) ws.reserve(pos);
+          for (uint32_t i = 0; i < pos; ++i) {
+            ys.push_back(labels[dst[i]]);
+            if (weights) ws.push_back(weights[dst[i]]);
           }
-        // The reference fits the tree on its sample: base score over the sample's rows.
-        fs.base_scores[k] = base_score(tp, ys.data(), weights ? ws.data() : nullptr, ys.size(), -1);
+          fs.base_scores[k] = base_score(tp, ys.data(), weights ? ws.data() : nullptr, ys.size(), -1);
+        }
         std::vector<uint32_t> sub(features + feature_offsets[t0 + k], features + feature_offsets[t0 + k + 1]);
         std::sort(sub.begin(), sub.end());
         for (uint32_t i = 0; i < sub.size(); ++i) {
           fs.masks[size_t(k) * W + sub[i] / 32] |= 1u << (sub[i] % 32);
           fs.ranks[size_t(k) * F + sub[i]] = i;  // position in the tree's ascending subset
         }
-      }
+      });
       std::unique_ptr<mpsb_cuda_trainer> t(new mpsb_cuda_trainer);
       setup_trainer(t.get(), b, ds, labels, weights, n, &tp, options | MPSB_OPT_NO_GRAPH, 0, &fs);
       t->run(1);

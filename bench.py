@@ -205,6 +205,9 @@ def run_ours(args, rank, world):
     t_dbin = time.perf_counter() - t0
     dbin_equal = bool(np.array_equal(dbin.bin_counts, binned.bin_counts))
     dbin.close()
+    # Launch shape for this fit shape: the autotuner times rounds under candidate shapes and
+    # every later session below (timed, roofline, end to end) uses the fastest.
+    tuning = backend.autotune(binned, y, w, rounds_per_trial=5, **PARAMS)
     n_rounds = args.warmup + args.steps
     trainer = mb.Trainer(backend, binned, y, w, n_estimators=2 * n_rounds + 4, **PARAMS)
     trainer.run(args.warmup)
@@ -282,7 +285,12 @@ def run_ours(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
         "config": dict(CONFIG, parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                        binning_seconds=round(t_bin, 2), device_binning_seconds=round(t_dbin, 3),
-                       device_binning_same_schema=dbin_equal),
+                       device_binning_same_schema=dbin_equal,
+                       launch_shape={k: tuning[k] for k in ("hist_threads", "hist_stages", "root_threads",
+                                                             "items_per_sm", "blocked_levels", "scan_threads")},
+                       autotune={"trials": tuning["trials"],
+                                 "ms_per_round": round(tuning["ms_per_round"], 4),
+                                 "built_in_ms_per_round": round(tuning["default_ms_per_round"], 4)}),
         "gpu_launches": int(st["kernel_launches"]),
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -178,6 +178,21 @@ typedef struct {
   uint64_t hist_timed_launches;
 } mpsb_cuda_stats;
 
+/* Launch shape of a training session: histogram CTA threads and pipeline stages,
+   gradient-only root CTA threads, histogram work items per SM, depth levels built from
+   the column-blocked bins copy, split-scan CTA threads. */
+typedef struct {
+  uint32_t hist_threads;
+  uint32_t hist_stages;
+  uint32_t root_threads;
+  uint32_t items_per_sm;
+  uint32_t blocked_levels;
+  uint32_t scan_threads;
+  double ms_per_round;          /* measured with this shape */
+  double default_ms_per_round;  /* measured with the built-in shape */
+  uint32_t trials;
+} mpsb_cuda_tuning;
+
 typedef struct mpsb_cuda_backend mpsb_cuda_backend;
 typedef struct mpsb_cuda_dataset mpsb_cuda_dataset;
 typedef struct mpsb_cuda_model mpsb_cuda_model;
@@ -422,6 +437,19 @@ int mpsb_cuda_trainer_reset_stats(mpsb_cuda_trainer* trainer);
 int mpsb_cuda_trainer_level_stats(const mpsb_cuda_trainer* trainer, uint32_t n_levels,
                                   double* milliseconds, uint64_t* cells);
 int mpsb_cuda_trainer_export(mpsb_cuda_trainer* trainer, mpsb_cuda_model** out);
+
+/* Autotuner: times boosting rounds of this fit's shape (rows, features, depth, histogram
+   arithmetic, weighted or not, growth strategy) under launch shapes chosen by coordinate
+   descent from the built-in one (rounds_per_trial timed rounds each, after one untimed),
+   and keeps the fastest in a process-wide table that every later session of the same
+   shape uses (the MPSB_* tile variables still override it). Results do not depend on
+   the shape: every launch shape gives the same trees. */
+int mpsb_cuda_autotune(mpsb_cuda_backend* backend, const mpsb_cuda_dataset* dataset,
+                       const double* labels, const double* weights, uint64_t n,
+                       const mpsb_train_params* params, uint32_t options,
+                       uint32_t rounds_per_trial, mpsb_cuda_tuning* out);
+/* Forget every tuned shape. */
+void mpsb_cuda_autotune_clear(void);
 void mpsb_cuda_trainer_destroy(mpsb_cuda_trainer* trainer);
 
 #ifdef __cplusplus

@@ -84,6 +84,20 @@ class Stats(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [
+        ("hist_threads", C.c_uint32),
+        ("hist_stages", C.c_uint32),
+        ("root_threads", C.c_uint32),
+        ("items_per_sm", C.c_uint32),
+        ("blocked_levels", C.c_uint32),
+        ("scan_threads", C.c_uint32),
+        ("ms_per_round", C.c_double),
+        ("default_ms_per_round", C.c_double),
+        ("trials", C.c_uint32),
+    ]
+
+
 NODE_DTYPE = np.dtype(
     [
         ("feature_index", "<u4"),
@@ -179,6 +193,8 @@ SIGNATURES = {
     "mpsb_cuda_trainer_reset_stats": (_I32, [_VP]),
     "mpsb_cuda_trainer_level_stats": (_I32, [_VP, _U32, _VP, _VP]),
     "mpsb_cuda_trainer_export": (_I32, [_VP, C.POINTER(_VP)]),
+    "mpsb_cuda_autotune": (_I32, [_VP, _VP, _VP, _VP, _U64, _VP, _U32, _U32, C.POINTER(Tuning)]),
+    "mpsb_cuda_autotune_clear": (None, []),
     "mpsb_cuda_trainer_destroy": (None, [_VP]),
 }
 

@@ -383,6 +383,26 @@ class CudaBackend:
         check(_lib.load().mpsb_cuda_squared_error(self.handle, ptr(y), ptr(p), y.size, ptr(out)))
         return out
 
+    def autotune(self, dataset, labels, weights=None, *, rounds_per_trial: int = 3,
+                 hist_mode: str = "fixed", **params) -> dict:
+        """Times boosting rounds of this fit's shape under candidate launch shapes and keeps
+        the fastest for every later fit of the same shape (mpsb_cuda_autotune)."""
+
+        dev = self.dataset(dataset)
+        y = np.ascontiguousarray(labels, dtype=np.float64)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        p, keep = make_params(**params)
+        out = _lib.Tuning()
+        check(_lib.load().mpsb_cuda_autotune(self.handle, dev.handle, ptr(y), ptr(w), y.size, C.byref(p),
+                                             _options(hist_mode, True, True), rounds_per_trial,
+                                             C.byref(out)))
+        del keep
+        return {name: getattr(out, name) for name, _ in _lib.Tuning._fields_}
+
+    @staticmethod
+    def autotune_clear() -> None:
+        _lib.load().mpsb_cuda_autotune_clear()
+
     def histograms_from_pairs(self, dataset: BinnedDataset, pairs, rows) -> list[np.ndarray]:
         """Per-feature HistogramBin arrays of one node (HistogramBuilder::BuildHistograms)."""
 

@@ -20,7 +20,9 @@
 #include <cstring>
 #include <exception>
 #include <limits>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <thread>
@@ -563,6 +565,48 @@ int mpsb_cuda_dataset_uses_tma(const mpsb_cuda_dataset* d) { return d && d->has_
 }  // extern "C"
 
 // ======================================================================================
+// Autotuned launch shapes, per fit shape
+// ======================================================================================
+namespace mpsb {
+
+struct TuneKey {
+  uint32_t rows, features, depth, mode, unit_hess, weighted, leafwise;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(rows, features, depth, mode, unit_hess, weighted, leafwise) <
+           std::tie(o.rows, o.features, o.depth, o.mode, o.unit_hess, o.weighted, o.leafwise);
+  }
+};
+
+std::mutex g_tune_mutex;
+std::map<TuneKey, mpsb_cuda_tuning> g_tune_table;
+
+// The shape of a single-model fit (forests, softmax and one-vs-rest keep the built-in
+// launch shape).
+bool unit_hessian_fit(const double* weights, const mpsb_train_params& p) {
+  bool unit = !weights && (p.objective == MPSB_SQUARED_ERROR || p.objective == MPSB_QUANTILE);
+  if (const char* v = std::getenv("MPSB_UNIT_HESS")) unit = unit && std::atoi(v) != 0;
+  return unit;
+}
+
+TuneKey tune_key_of(const mpsb_cuda_dataset* ds, const double* weights, const mpsb_train_params& p,
+                    uint32_t options) {
+  return TuneKey{ds->n_rows, ds->features, p.max_depth,
+                 uint32_t((options & MPSB_OPT_FLOAT_HIST) ? kModeFloat : kModeFixed),
+                 unit_hessian_fit(weights, p) ? 1u : 0u, weights ? 1u : 0u,
+                 p.growth_strategy == 1 ? 1u : 0u};
+}
+
+bool tuned_shape(const TuneKey& k, mpsb_cuda_tuning* out) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  const auto it = g_tune_table.find(k);
+  if (it == g_tune_table.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+}  // namespace mpsb
+
+// ======================================================================================
 // Training session
 // ======================================================================================
 struct mpsb_cuda_trainer {
@@ -619,6 +663,27 @@ struct mpsb_cuda_trainer {
   }
 
   int grid(int per_sm) const { return b->sm_count * per_sm; }
+
+  // Captured rounds bake in the launch shape: drop them after a change.
+  void reset_graphs() {
+    for (int i = 0; i < 2; ++i) {
+      if (graph_exec[i]) cudaGraphExecDestroy(graph_exec[i]);
+      if (graph[i]) cudaGraphDestroy(graph[i]);
+      graph_exec[i] = nullptr;
+      graph[i] = nullptr;
+    }
+  }
+
+  void apply_shape(const mpsb_cuda_tuning& s) {
+    hcfg.threads = int(s.hist_threads);
+    hcfg.stages = int(s.hist_stages);
+    hcfg.root_threads = int(s.root_threads);
+    dev.items_per_sm = s.items_per_sm;
+    blocked_levels = s.blocked_levels;
+    dev.scan_threads = s.scan_threads;
+    dev.n_fchunks = (dev.features + s.scan_threads / 32 - 1) / (s.scan_threads / 32);
+    reset_graphs();
+  }
 
   // Enqueue one boosting round. Returns the number of kernels enqueued. root_gradient_only:
   // the roots' count and hessian histograms come from the fit's first round.
@@ -904,15 +969,31 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   // Four features (warps) per split-scan CTA spread a shallow level's few nodes over many
   // SMs; MPSB_SCAN_THREADS overrides (a multiple of 32, at most 512).
   a.scan_threads = 128;
+  // rows per histogram work item: chosen per level on the device (about three items per
+  // SM, within the 2^16-row limb bound)
+  a.item_rows = 0;
+  // Squared error and quantile have h = 1 per row; without weights every row's quantized
+  // hessian is the same unit (MPSB_UNIT_HESS=0 builds the hessian limbs anyway).
+  a.unit_hess = !softmax_classes && n_classes == 0 && unit_hessian_fit(weights, *p);
+  {
+    // A shape the autotuner chose for this kind of fit.
+    mpsb_cuda_tuning tuned{};
+    if (!forest && !softmax_classes && n_classes == 0 &&
+        tuned_shape(tune_key_of(ds, weights, *p, options), &tuned)) {
+      t->hcfg.threads = int(tuned.hist_threads);
+      t->hcfg.stages = int(tuned.hist_stages);
+      t->hcfg.root_threads = int(tuned.root_threads);
+      a.items_per_sm = tuned.items_per_sm;
+      t->blocked_levels = tuned.blocked_levels;
+      a.scan_threads = tuned.scan_threads;
+    }
+  }
+  t->hcfg.bins_tmap = ds->has_bins_tmap ? &ds->bins_tmap : nullptr;
+  // Launch-shape overrides (tuning sweeps): threads per CTA, pipeline stages, rows per work
+  // item, split-scan CTA size.
   if (const char* v = std::getenv("MPSB_SCAN_THREADS"))
     a.scan_threads = uint32_t(std::min(512, std::max(32, std::atoi(v) / 32 * 32)));
   a.n_fchunks = (F + a.scan_threads / 32 - 1) / (a.scan_threads / 32);
-  // rows per histogram work item: chosen per level on the device (about four items per
-  // SM, within the 2^16-row limb bound)
-  a.item_rows = 0;
-  // Tile-shape overrides (used by the tuning sweeps): threads per CTA, pipeline stages,
-  // rows per work item.
-  t->hcfg.bins_tmap = ds->has_bins_tmap ? &ds->bins_tmap : nullptr;
   if (const char* v = std::getenv("MPSB_HIST_THREADS")) t->hcfg.threads = std::atoi(v);
   if (const char* v = std::getenv("MPSB_HIST_STAGES")) t->hcfg.stages = std::atoi(v);
   if (const char* v = std::getenv("MPSB_ROOT_THREADS")) t->hcfg.root_threads = std::atoi(v);
@@ -962,11 +1043,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     CK(cudaMemcpyAsync(d_w, weights, n * sizeof(double), cudaMemcpyHostToDevice, s));
     a.weights = d_w;
   }
-  // Squared error and quantile have h = 1 per row; without weights every row's quantized
-  // hessian is the same unit (MPSB_UNIT_HESS=0 builds the hessian limbs anyway).
-  a.unit_hess = !weights && !softmax_classes && n_classes == 0 &&
-                (p->objective == MPSB_SQUARED_ERROR || p->objective == MPSB_QUANTILE);
-  if (const char* v = std::getenv("MPSB_UNIT_HESS")) a.unit_hess = a.unit_hess && std::atoi(v) != 0;
+
   if (softmax_classes) {
     // Margins [K][n] from the class priors (WeightedClassBaseScores,
     // multiclass_trainer.cpp:39-67); labels must be class ids (22-37).
@@ -1241,6 +1318,143 @@ int mpsb_cuda_trainer_export(mpsb_cuda_trainer* t, mpsb_cuda_model** out) {
 }
 
 void mpsb_cuda_trainer_destroy(mpsb_cuda_trainer* t) { delete t; }
+
+int mpsb_cuda_autotune(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds, const double* labels,
+                       const double* weights, uint64_t n, const mpsb_train_params* p,
+                       uint32_t options, uint32_t rounds_per_trial, mpsb_cuda_tuning* out) {
+  return guard([&] {
+    if (!b || !ds || !labels || !p || !out) throw TrainingError("null argument");
+    if (options & (MPSB_OPT_PER_NODE | MPSB_OPT_TIMING | MPSB_OPT_NO_GRAPH))
+      throw UnsupportedError("the autotuner times the batched, graph-captured rounds");
+    const uint32_t R = std::max(1u, rounds_per_trial);
+    constexpr uint32_t kMaxTrials = 16, kConfirmTrials = 4;
+    mpsb_train_params tp = *p;
+    tp.n_estimators = (kMaxTrials + kConfirmTrials) * (R + 1) + 1;
+    std::unique_ptr<mpsb_cuda_trainer> t(new mpsb_cuda_trainer);
+    const TuneKey key = tune_key_of(ds, weights, *p, options);
+    {
+      // The session starts from the built-in shape, not from an earlier tuning.
+      std::lock_guard<std::mutex> lock(g_tune_mutex);
+      g_tune_table.erase(key);
+    }
+    setup_trainer(t.get(), b, ds, labels, weights, n, &tp, options, 0);
+    mpsb_cuda_tuning cur{};
+    cur.hist_threads = uint32_t(t->hcfg.threads);
+    cur.hist_stages = uint32_t(t->hcfg.stages);
+    cur.root_threads = uint32_t(t->hcfg.root_threads);
+    cur.items_per_sm = t->dev.items_per_sm ? t->dev.items_per_sm : 3u;
+    cur.blocked_levels = t->blocked_levels;
+    cur.scan_threads = t->dev.scan_threads;
+    const uint32_t min_scan = t->dev.scan_threads;  // the chunk tables are sized for it
+    const mpsb_cuda_tuning built_in_shape = cur;
+    auto same_shape = [](const mpsb_cuda_tuning& x, const mpsb_cuda_tuning& y) {
+      return x.hist_threads == y.hist_threads && x.hist_stages == y.hist_stages &&
+             x.root_threads == y.root_threads && x.items_per_sm == y.items_per_sm &&
+             x.blocked_levels == y.blocked_levels && x.scan_threads == y.scan_threads;
+    };
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    uint32_t trials = 0;
+    auto measure = [&](const mpsb_cuda_tuning& s) -> double {
+      t->apply_shape(s);
+      t->run(1);  // captures the round graphs of this shape (and the roots' reuse)
+      CK(cudaEventRecord(e0, b->stream));
+      t->run(R);
+      CK(cudaEventRecord(e1, b->stream));
+      t->synchronize();
+      float ms = 0.0f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      ++trials;
+      return double(ms) / R;
+    };
+    try {
+      double best = measure(cur);
+      const double built_in = best;
+      // Coordinate descent over the shape, one parameter at a time.
+      auto try_values = [&](auto set, std::initializer_list<uint32_t> values) {
+        for (uint32_t v : values) {
+          if (trials >= kMaxTrials) return;
+          mpsb_cuda_tuning cand = cur;
+          if (!set(cand, v)) continue;
+          const double ms = measure(cand);
+          if (ms < best) {
+            best = ms;
+            cur = cand;
+          }
+        }
+      };
+      try_values([&](mpsb_cuda_tuning& c, uint32_t v) {
+        if (v == c.hist_threads) return false;
+        c.hist_threads = v;
+        c.hist_stages = 2;
+        return true;
+      }, {768, 640, 512});
+      try_values([&](mpsb_cuda_tuning& c, uint32_t v) {
+        if (c.hist_threads != 512 || v == c.hist_stages) return false;
+        c.hist_stages = v;
+        return true;
+      }, {3});
+      try_values([&](mpsb_cuda_tuning& c, uint32_t v) {
+        if (v == c.items_per_sm) return false;
+        c.items_per_sm = v;
+        return true;
+      }, {2, 3, 4});
+      try_values([&](mpsb_cuda_tuning& c, uint32_t v) {
+        if (v == c.blocked_levels) return false;
+        c.blocked_levels = v;
+        return true;
+      }, {1, 2, 3});
+      try_values([&](mpsb_cuda_tuning& c, uint32_t v) {
+        if (v == c.scan_threads || v < min_scan) return false;
+        c.scan_threads = v;
+        return true;
+      }, {128, 256});
+      try_values([&](mpsb_cuda_tuning& c, uint32_t v) {
+        if (v == c.root_threads) return false;
+        c.root_threads = v;
+        return true;
+      }, {1024, 768});
+      // Rounds differ a little from tree to tree: confirm the winner against the built-in
+      // shape with alternating measurements before keeping it.
+      mpsb_cuda_tuning chosen = cur;
+      double chosen_ms = best, default_ms = built_in;
+      if (!same_shape(cur, built_in_shape)) {
+        double d = 0.0, c = 0.0;
+        for (uint32_t i = 0; i < kConfirmTrials / 2; ++i) {
+          d += measure(built_in_shape);
+          c += measure(cur);
+        }
+        default_ms = d / (kConfirmTrials / 2);
+        chosen_ms = c / (kConfirmTrials / 2);
+        if (!(chosen_ms < default_ms)) {
+          chosen = built_in_shape;
+          chosen_ms = default_ms;
+        }
+      }
+      cur = chosen;
+      cur.ms_per_round = chosen_ms;
+      cur.default_ms_per_round = default_ms;
+      cur.trials = trials;
+    } catch (...) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    {
+      std::lock_guard<std::mutex> lock(g_tune_mutex);
+      g_tune_table[key] = cur;
+    }
+    *out = cur;
+  });
+}
+
+void mpsb_cuda_autotune_clear(void) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tune_table.clear();
+}
 
 int mpsb_cuda_train_regressor(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
                               const double* labels, const double* weights, uint64_t n,

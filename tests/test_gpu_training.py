@@ -207,6 +207,24 @@ def test_unit_hessian_builds_equal_full_builds(backend, monkeypatch):
             assert t1.tobytes() == t2.tobytes()
 
 
+def test_autotuned_shape_gives_the_same_trees(backend):
+    """The autotuner's shape is used by later fits of the same shape and changes nothing
+    in the trees."""
+    x, y, w = _data(49, 60000, 40, 0.02, 2)
+    binned = mb.quantize_dense(x, 255)
+    params = dict(n_estimators=3, learning_rate=0.2, max_depth=7, min_samples_leaf=2)
+    backend.autotune_clear()
+    plain = mb.train_regressor(backend, binned, y, w, **params)
+    tuned = backend.autotune(binned, y, w, rounds_per_trial=2, **params)
+    assert tuned["trials"] >= 1 and tuned["ms_per_round"] <= tuned["default_ms_per_round"]
+    assert tuned["hist_threads"] in (512, 640, 768) and tuned["scan_threads"] in (128, 256)
+    again = mb.train_regressor(backend, binned, y, w, **params)
+    backend.autotune_clear()
+    for t1, t2 in zip(plain.trees, again.trees):
+        assert t1.tobytes() == t2.tobytes()
+    assert plain.train_predictions.tobytes() == again.train_predictions.tobytes()
+
+
 @pytest.mark.parametrize("rows", [20_000, 20_003])
 def test_dataset_upload_layouts(backend, rows):
     """The per-block upload and pack gives the same trees from u8 and from u16 bins, with

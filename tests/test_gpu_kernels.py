@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 import mpsboost_gb300 as mb
+import oracle
 from conftest import seeded_matrix
 
 pytestmark = pytest.mark.gpu
@@ -199,3 +200,80 @@ def test_integer_pipe_conversions_match_hardware(tmp_path):
                    check=True)
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert run.returncode == 0, run.stdout + run.stderr
+
+
+def test_error_report_against_fp64_oracle(backend, port, record_property):
+    """Max error of every histogram bin against the FP64 oracle's row-ordered sums, for the
+    fixed-point path (exact int64 sums of values quantized to 2^-k) and the plain FP32
+    path. Each bin's error stays within its a-priori bound: the FP64 -> FP32 rounding of
+    the pair (2^-24 of each |value|) plus, fixed point, half a quantization unit per row,
+    or, FP32 atomics, 2^-24 of the bin's absolute sum per added row. The figures are
+    recorded as test properties."""
+    x = seeded_matrix(13, 200_000, 24, 0.05, 3)
+    binned = mb.quantize_dense(x, 255)
+    ds = port.quantize_dense(x, 255)
+    rng = np.random.default_rng(14)
+    pairs = np.column_stack([rng.normal(size=200_000) * 2.0, rng.uniform(0.5, 1.5, 200_000)])
+    rows = np.sort(rng.choice(200_000, 150_000, replace=False))
+    want = port.histograms(ds, pairs, rows)
+    absolute = port.histograms(ds, np.abs(pairs), rows)  # per-bin sums of |g|, |h|
+    kg, kh = port.fixed_scales(pairs.astype(np.float32))
+    report = {}
+    for mode in ("fixed", "float"):
+        backend.set_hist_mode(mode)
+        try:
+            got = backend.histograms_from_pairs(binned, pairs, rows)
+        finally:
+            backend.set_hist_mode("fixed")
+        worst = {"g": 0.0, "h": 0.0, "g_rel_to_abs_sum": 0.0, "h_rel_to_abs_sum": 0.0}
+        for gf, wf, af in zip(got, want, absolute):
+            assert np.array_equal(gf["count"], wf["count"])
+            n = wf["count"].astype(np.float64)
+            for key, name, k in (("g", "gradient_sum", kg), ("h", "hessian_sum", kh)):
+                err = np.abs(gf[name] - wf[name])
+                s_abs = af[name]
+                slack = n * 2.0 ** -52 * s_abs  # the oracle's own FP64 rounding
+                if mode == "fixed":
+                    bound = s_abs * 2.0 ** -24 + n * 2.0 ** -(k + 1) + slack
+                else:
+                    bound = s_abs * 2.0 ** -24 + n * s_abs * 2.0 ** -24 + slack
+                assert np.all(err <= bound), (mode, key)
+                worst[key] = max(worst[key], float(err.max()))
+                nz = s_abs > 0
+                if nz.any():
+                    worst[key + "_rel_to_abs_sum"] = max(worst[key + "_rel_to_abs_sum"],
+                                                         float((err[nz] / s_abs[nz]).max()))
+        report[mode] = worst
+        record_property(f"hist_max_error_{mode}", worst)
+    print("histogram max errors vs FP64 oracle:", report)
+    # Fixed point: the quantization error dominates and is far below FP32 accumulation's.
+    assert report["fixed"]["g_rel_to_abs_sum"] < 1e-6
+
+
+def test_leaf_error_report_against_fp64_oracle(backend, port, record_property):
+    """Max relative error of the leaf values and training predictions against the FP64
+    oracle's trees (same structures on these inputs), for both histogram paths."""
+    x = seeded_matrix(15, 50_000, 16, 0.0, 0)
+    rng = np.random.default_rng(16)
+    y = np.sin(x[:, 0]) + 2.0 * x[:, 1] * (x[:, 2] > 0) + rng.normal(size=50_000) * 0.05
+    params = dict(n_estimators=3, learning_rate=0.3, max_depth=5, min_samples_leaf=50)
+    binned = mb.quantize_dense(x, 64)
+    ds = port.quantize_dense(x, 64)
+    want = port.train_regressor(ds, y, None, hist_mode=oracle.HIST_FP64, **params)
+    ref_pred = want.predict(ds)
+    report = {}
+    for mode in ("fixed", "float"):
+        model = mb.train_regressor(backend, binned, y, None, hist_mode=mode, **params)
+        leaf_err = 0.0
+        for got_t, exp_t in zip(model.trees, want.trees):
+            assert [(int(a["feature_index"]), int(a["threshold_bin"])) for a in got_t] == \
+                   [(int(b["feature_index"]), int(b["threshold_bin"])) for b in exp_t]
+            leaf = (exp_t["flags"] & 1) == 1
+            rel = np.abs(got_t["leaf_value"][leaf] - exp_t["leaf_value"][leaf]) / \
+                np.maximum(np.abs(exp_t["leaf_value"][leaf]), 1e-12)
+            leaf_err = max(leaf_err, float(rel.max()))
+        pred_err = float(np.max(np.abs(model.train_predictions - ref_pred) / np.maximum(np.abs(ref_pred), 1e-12)))
+        report[mode] = {"leaf_rel": leaf_err, "prediction_rel": pred_err}
+        record_property(f"leaf_max_error_{mode}", report[mode])
+        assert leaf_err <= 1e-5 and pred_err <= 1e-5
+    print("leaf / prediction max relative errors vs FP64 oracle:", report)

@@ -207,7 +207,10 @@ def run_ours(args, rank, world):
     dbin.close()
     # Launch shape for this fit shape: the autotuner times rounds under candidate shapes and
     # every later session below (timed, roofline, end to end) uses the fastest.
-    tuning = backend.autotune(binned, y, w, rounds_per_trial=5, **PARAMS)
+    tuning = (backend.autotune(binned, y, w, rounds_per_trial=5, **PARAMS) if not args.no_autotune
+              else {"hist_threads": 768, "hist_stages": 2, "root_threads": 1024, "items_per_sm": 3,
+                    "blocked_levels": 2, "scan_threads": 128, "trials": 0, "ms_per_round": 0.0,
+                    "default_ms_per_round": 0.0})
     n_rounds = args.warmup + args.steps
     trainer = mb.Trainer(backend, binned, y, w, n_estimators=2 * n_rounds + 4, **PARAMS)
     trainer.run(args.warmup)
@@ -402,6 +405,8 @@ def main():
     ap.add_argument("--workload", choices=["regression", "forest"], default="regression",
                     help="forest: the 256-tree random-forest configuration instead of the default")
     ap.add_argument("--forest-trees", type=int, default=256)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the built-in launch shape (profiling runs)")
     ap.add_argument("--only-train", action="store_true",
                     help="time the training rounds only (for launch lists and ncu captures)")
     args = ap.parse_args()

@@ -133,7 +133,7 @@ struct HistConfig {
 };
 
 // Encodes the tensor map of a row-major bins matrix (rows x row_stride bytes). Returns
-// false where the driver offers no tensor maps.
+// false where the CUDA driver offers no tensor maps.
 bool encode_bins_tmap(CUtensorMap* map, const uint8_t* bins, uint64_t row_stride, uint32_t n_rows);
 
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,

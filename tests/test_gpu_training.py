@@ -28,6 +28,8 @@ def _data(seed, rows, feats, nan=0.0, ints=0, objective="squared_error"):
     y = np.sin(xs[:, 0]) + xs[:, 1] * xs[:, 2 % feats] + 0.5 * xs[:, 3 % feats] ** 2 + rng.normal(size=rows) * 0.1
     if objective == "binary_logistic":
         y = (y > np.median(y)).astype(np.float64)
+    elif objective in ("poisson", "tweedie"):
+        y = np.floor(np.exp(np.clip(y, -3.0, 2.0)))  # non-negative counts
     w = rng.uniform(0.5, 1.5, rows)
     return x, y, w
 
@@ -276,6 +278,62 @@ def test_logistic_against_replica(backend, port):
     for got, exp in zip(model.trees, want.trees):
         np.testing.assert_allclose(got["leaf_value"], exp["leaf_value"], rtol=1e-9, atol=1e-12)
     np.testing.assert_allclose(model.train_predictions, want.predict(ds), rtol=1e-9, atol=1e-12)
+
+
+COUNT_OBJECTIVES = {
+    "poisson": dict(objective="poisson"),
+    "tweedie": dict(objective="tweedie", tweedie_variance_power=1.3),
+}
+
+
+@pytest.mark.parametrize("name", sorted(COUNT_OBJECTIVES))
+def test_count_objectives_against_replica(backend, port, name):
+    """Poisson and Tweedie (log link, objective.cpp:383-429): the device's FP64 exp may
+    differ from the host's by an ulp, so structures must match and leaf values and
+    predictions agree to 1e-9 relative, as for the logistic objective."""
+    x, y, w = _data(44, 6000, 8, 0.05, 2, name)
+    params = dict(n_estimators=3, learning_rate=0.2, max_depth=5, min_samples_leaf=4,
+                  **COUNT_OBJECTIVES[name])
+    binned = mb.quantize_dense(x, 255)
+    ds = port.quantize_dense(x, 255)
+    model = mb.train_regressor(backend, binned, y, w, **params)
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FIXED, **params)
+    assert float(model.base_score).hex() == float(want.base_score).hex()
+    assert _structure(model.trees) == _structure(want.trees)
+    for got, exp in zip(model.trees, want.trees):
+        np.testing.assert_allclose(got["leaf_value"], exp["leaf_value"], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(model.train_predictions, want.predict(ds), rtol=1e-9, atol=1e-12)
+
+
+def _loss(objective, margin, y, w, rho=1.5):
+    """Weighted mean training loss on the link scale's margins."""
+    if objective == "binary_logistic":
+        per_row = np.where(y > 0.5, np.logaddexp(0.0, -margin), np.logaddexp(0.0, margin))
+    elif objective == "poisson":
+        per_row = np.exp(margin) - y * margin
+    else:  # tweedie negative log-likelihood up to a label-only term
+        per_row = -y * np.exp((1.0 - rho) * margin) / (1.0 - rho) + np.exp((2.0 - rho) * margin) / (2.0 - rho)
+    return float(np.sum(w * per_row) / np.sum(w))
+
+
+@pytest.mark.parametrize("name", ["binary_logistic", "poisson", "tweedie"])
+def test_loss_against_fp64_reference(backend, port, name):
+    """Fixed-point training against the FP64 reference restatement: the same trees on
+    these inputs and the final training loss (logloss, Poisson or Tweedie deviance)
+    within 1e-4."""
+    x, y, w = _data(45, 20000, 10, 0.02, 2, name)
+    extra = COUNT_OBJECTIVES.get(name, dict(objective=name))
+    params = dict(n_estimators=5, learning_rate=0.2, max_depth=6, min_samples_leaf=5, **extra)
+    binned = mb.quantize_dense(x, 255)
+    ds = port.quantize_dense(x, 255)
+    model = mb.train_regressor(backend, binned, y, w, **params)
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FP64, **params)
+    assert first_divergence(model.trees, want.trees) is None
+    rho = params.get("tweedie_variance_power", 1.5)
+    got_loss = _loss(name, model.train_predictions, y, w, rho)
+    want_loss = _loss(name, want.predict(ds), y, w, rho)
+    assert abs(got_loss - want_loss) <= 1e-4
+    np.testing.assert_allclose(model.train_predictions, want.predict(ds), rtol=1e-5, atol=1e-9)
 
 
 def test_ovr_equals_independent_binary_fits(backend, port):

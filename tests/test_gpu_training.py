@@ -11,6 +11,8 @@
 
 from __future__ import annotations
 
+import math
+
 import numpy as np
 import pytest
 
@@ -409,6 +411,55 @@ def test_scale_properties(backend):
         assert t1.tobytes() == t2.tobytes()
     stats = t.stats()
     assert stats["rounds"] == 2 and stats["kernel_launches"] > 0 and stats["hist_cells"] >= n * f
+
+
+def _random_bins(seed, rows, feats, nb=255):
+    """A binned dataset of uniform random bins (no missing values) with an identity schema."""
+    rng = np.random.default_rng(seed)
+    bins = rng.integers(0, nb, size=(feats, rows), dtype=np.uint8)
+    cnt = np.full(feats, nb - 1, np.uint32)
+    bounds = np.tile(np.arange(nb - 1, dtype=np.float32) + 0.5, feats)
+    return mb.BinnedDataset(rows, feats, nb, bins, np.zeros((feats, rows), bool), bounds,
+                            (np.arange(feats, dtype=np.uint64) * (nb - 1)), cnt,
+                            np.full(feats, nb, np.uint32), np.zeros(feats, np.uint64))
+
+
+def test_full_size_properties(backend):
+    """10M rows x 128 features, 255 bins, depth 8 (the benchmark's shape), through
+    size-independent properties: two fits are bit-identical; the training predictions,
+    applied from the final row segments, equal a traversal of every row through the trees
+    bit for bit (so no row was misrouted by any partition); and in one layer launch over a
+    root and its two children, every feature's parent histogram is exactly the sum of the
+    children's (count, gradient and hessian), with the same gradient total in every
+    feature."""
+    n, f = 10_000_000, 128
+    binned = _random_bins(46, n, f)
+    rng = np.random.default_rng(47)
+    b = binned.bins
+    y = ((b[0].astype(np.float64) - 127.0) / 64.0) * ((b[1].astype(np.float64) - 127.0) / 64.0)
+    y += np.sin(b[2] / 40.0) + 0.25 * (b[3] > 200) + rng.normal(size=n) * 0.1
+    w = rng.uniform(0.5, 1.5, n)
+    params = dict(n_estimators=2, learning_rate=0.1, max_depth=8, min_samples_leaf=20)
+    a = mb.train_regressor(backend, binned, y, w, **params)
+    a2 = mb.train_regressor(backend, binned, y, w, **params)
+    assert [t.tobytes() for t in a.trees] == [t.tobytes() for t in a2.trees]
+    assert a.train_predictions.tobytes() == a2.train_predictions.tobytes()
+    assert a.predict(backend, binned).tobytes() == a.train_predictions.tobytes()
+    assert sum(int(((t["flags"] & 1) == 1).sum()) for t in a.trees) > 2 * 100  # deep trees
+
+    pairs = np.column_stack([y - y.mean(), w])
+    rows = np.arange(n, dtype=np.uint64)
+    go_left = b[5] <= 100
+    parent, left, right = backend.layer_histograms(binned, pairs, [rows, rows[go_left], rows[~go_left]])
+    totals = set()
+    for feat in range(f):
+        p_, l_, r_ = parent[feat], left[feat], right[feat]
+        assert int(p_["count"].sum()) == n
+        assert np.array_equal(p_["count"], l_["count"] + r_["count"])
+        assert np.array_equal(p_["gradient_sum"], l_["gradient_sum"] + r_["gradient_sum"])
+        assert np.array_equal(p_["hessian_sum"], l_["hessian_sum"] + r_["hessian_sum"])
+        totals.add(math.fsum(p_["gradient_sum"]))
+    assert len(totals) == 1
 
 
 def test_softmax_against_replica(backend, port):

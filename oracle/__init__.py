@@ -361,6 +361,23 @@ class Oracle:
                                                 _ptr(f), C.c_uint32(f.size), C.byref(out)))
         return self._wrap_dataset(out.value)
 
+    def dataset_from_bins(self, binned) -> Dataset:
+        """The oracle's dataset over bins computed elsewhere (fields of a binned dataset:
+        feature-major ``bins``, ``missing``, ``max_bins``, the packed schema)."""
+
+        self._port_only()
+        b = np.ascontiguousarray(binned.bins)
+        m = np.ascontiguousarray(binned.missing, dtype=np.uint8)
+        bnd = np.ascontiguousarray(binned.boundaries_flat, dtype=np.float32)
+        off = np.ascontiguousarray(binned.boundary_offsets, dtype=np.uint64)
+        cnt = np.ascontiguousarray(binned.boundary_counts, dtype=np.uint32)
+        nb = np.ascontiguousarray(binned.bin_counts, dtype=np.uint32)
+        out = C.c_void_p()
+        self._check(self.lib.orc_dataset_from_bins(
+            _ptr(b), C.c_uint32(b.itemsize), _ptr(m), C.c_uint64(b.shape[1]), C.c_uint32(b.shape[0]),
+            C.c_uint32(binned.max_bins), _ptr(bnd), _ptr(off), _ptr(cnt), _ptr(nb), C.byref(out)))
+        return self._wrap_dataset(out.value)
+
     # -- objectives / histograms -------------------------------------------------------
     def gradients(self, objective, labels, predictions, alpha=0.5, variance_power=1.5) -> np.ndarray:
         y = np.ascontiguousarray(labels, dtype=np.float64)

@@ -297,6 +297,56 @@ int orc_dataset_subset(const void* src, const uint64_t* rows, uint64_t n_rows,
   return ORC_OK;
 }
 
+/* A dataset from bins computed elsewhere under a known schema: the fields QuantizeDense
+ * produces (binned_dataset.hpp:81-126), feature-major. Every non-missing bin must lie
+ * below its feature's bin count; missing counts are recomputed. */
+int orc_dataset_from_bins(const void* bins, uint32_t width, const uint8_t* missing,
+                          uint64_t rows, uint32_t features, uint32_t max_bins,
+                          const float* boundaries, const uint64_t* boundary_offset,
+                          const uint32_t* boundary_count, const uint32_t* bin_count, void** out) {
+  if (bins == NULL || boundary_offset == NULL || boundary_count == NULL || bin_count == NULL || out == NULL)
+    return fail(ORC_DATA_ERROR, "null argument");
+  if (width != 1 && width != 2) return fail(ORC_DATA_ERROR, "bin width must be 1 or 2 bytes");
+  if (rows == 0 || features == 0) return fail(ORC_DATA_ERROR, "empty dataset");
+  if (max_bins < 2 || max_bins > 65536) return fail(ORC_DATA_ERROR, "max_bins must be in [2, 65536]");
+  uint64_t total = 0;
+  for (uint32_t f = 0; f < features; ++f) {
+    if (bin_count[f] == 0 || bin_count[f] > max_bins || boundary_count[f] + 1 != bin_count[f])
+      return fail(ORC_DATA_ERROR, "bin counts do not match the boundaries");
+    if (boundary_offset[f] != total) return fail(ORC_DATA_ERROR, "boundary offsets are not packed");
+    total += boundary_count[f];
+  }
+  if (total > 0 && boundaries == NULL) return fail(ORC_DATA_ERROR, "null boundaries");
+  dataset_t* d = alloc_dataset(rows, features);
+  if (!d) return fail(ORC_OTHER_ERROR, "out of host memory");
+  d->max_bins = max_bins;
+  d->n_boundaries = total;
+  d->boundaries = (float*)malloc((total > 0 ? total : 1) * sizeof(float));
+  if (!d->boundaries) { orc_dataset_free(d); return fail(ORC_OTHER_ERROR, "out of host memory"); }
+  if (total > 0) memcpy(d->boundaries, boundaries, total * sizeof(float));
+  for (uint32_t f = 0; f < features; ++f) {
+    d->boundary_offset[f] = boundary_offset[f];
+    d->boundary_count[f] = boundary_count[f];
+    d->bin_count[f] = bin_count[f];
+    uint64_t miss = 0;
+    for (uint64_t r = 0; r < rows; ++r) {
+      const uint64_t i = (uint64_t)f * rows + r;
+      const uint32_t b = width == 1 ? ((const uint8_t*)bins)[i] : ((const uint16_t*)bins)[i];
+      const uint8_t m = missing ? (missing[i] != 0) : 0;
+      if (!m && b >= bin_count[f]) {
+        orc_dataset_free(d);
+        return fail(ORC_DATA_ERROR, "Binned value exceeds the feature histogram range");
+      }
+      d->bins[i] = (uint16_t)(m ? 0 : b);
+      d->missing[i] = m;
+      miss += m;
+    }
+    d->missing_count[f] = miss;
+  }
+  *out = d;
+  return ORC_OK;
+}
+
 int orc_dataset_info(const void* p, uint64_t* rows, uint32_t* features, uint32_t* max_bins,
                      uint64_t* boundary_total) {
   const dataset_t* d = (const dataset_t*)p;

@@ -198,6 +198,12 @@ int orc_partition_rows(const void* dataset, const uint64_t* rows, uint64_t n_row
    (forest_sampling.py:56-60) when the sample keeps the full data's bin boundaries. */
 int orc_dataset_subset(const void* dataset, const uint64_t* rows, uint64_t n_rows,
                        const uint32_t* features, uint32_t n_features, void** out);
+/* A dataset from feature-major bins (u8 or u16) and a missing mask computed elsewhere
+   under the given schema; missing cells hold bin 0, as QuantizeDense leaves them. */
+int orc_dataset_from_bins(const void* bins, uint32_t width, const uint8_t* missing,
+                          uint64_t rows, uint32_t features, uint32_t max_bins,
+                          const float* boundaries, const uint64_t* boundary_offset,
+                          const uint32_t* boundary_count, const uint32_t* bin_count, void** out);
 /* Weighted FP64 gradients of one boosting round rounded to FP32, the input of the
    fixed-point replica (trainer.cpp:178-216 followed by a round-to-nearest cast). */
 int orc_weighted_pairs32(uint32_t objective, double alpha, double variance_power,

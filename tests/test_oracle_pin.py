@@ -131,3 +131,36 @@ def test_leafwise_port_matches_reference(port, reference, case):
     for t1, t2 in zip(a.trees, b.trees):
         assert t1.tobytes() == t2.tobytes()
     assert a.predict(port.quantize_dense(x, 32)).tobytes() == b.predict(ds).tobytes()
+
+
+def test_dataset_from_bins_equals_quantized(port):
+    """The oracle's dataset over given bins (how tests hand it the device's bins) trains
+    exactly as the dataset of its own quantile binning, and rejects a bin past its
+    feature's count."""
+    x = seeded_matrix(61, 3000, 5, 0.1, 1)
+    y = np.nan_to_num(x[:, 0]) + np.nan_to_num(x[:, 1]) ** 2
+    own = port.quantize_dense(x, 64)
+
+    class Given:  # the fields of a binned dataset, as the package lays them out
+        bins = own.bins.astype(np.uint8)
+        missing = own.missing
+        max_bins = own.max_bins
+        boundaries_flat = own.boundaries_flat
+        boundary_offsets = own.boundary_offsets
+        boundary_counts = own.boundary_counts
+        bin_counts = own.bin_counts
+
+    given = port.dataset_from_bins(Given)
+    assert np.array_equal(given.bins, own.bins) and np.array_equal(given.missing, own.missing)
+    assert list(given.missing_counts) == list(own.missing_counts)
+    params = dict(n_estimators=2, max_depth=4, learning_rate=0.3)
+    for mode in (oracle.HIST_FP64, oracle.HIST_FIXED):
+        a = port.train_regressor(own, y, None, hist_mode=mode, **params)
+        b = port.train_regressor(given, y, None, hist_mode=mode, **params)
+        assert [t.tobytes() for t in a.trees] == [t.tobytes() for t in b.trees]
+    Given.bins = Given.bins.copy()
+    f = 2
+    row = int(np.flatnonzero(~Given.missing[f])[0])
+    Given.bins[f, row] = Given.bin_counts[f]
+    with pytest.raises(oracle.OracleError, match="exceeds"):
+        port.dataset_from_bins(Given)

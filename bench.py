@@ -260,6 +260,13 @@ def run_ours(args, rank, world):
     per_launch_bytes = alg_bytes / max(ts["hist_timed_launches"], 1)
     achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
+    # Whole tree: the histogram bytes above plus gradients (labels, predictions, weights in,
+    # g/h pairs out: 32 B per row), the partitions (row id in, split feature's bin, row id
+    # out: 9 B per routed row, rows counted on the device) and the prediction update (row
+    # id, bin, prediction read and written: 21 B per row).
+    part_rows = st["part_rows"] / args.steps
+    tree_bytes = alg_bytes / args.steps + 32 * args.rows + 9 * part_rows + 21 * args.rows
+    tree_achieved = tree_bytes / (ms_max / args.steps / 1e3) / 1e9
 
     # Plain path: FP32 atomics, one histogram launch per node, host round trip per level.
     plain_steps = max(2, args.steps // 4)
@@ -281,7 +288,7 @@ def run_ours(args, rank, world):
 
     if rank != 0:
         return
-    cpu = cpu_baseline(xf, y, w, args.cpu_rows, 1) if world == 1 and not args.no_cpu else None
+    cpu = cpu_baseline(xf, y, w, args.cpu_rows, args.cpu_trees) if world == 1 and not args.no_cpu else None
     line = {
         "metric": METRIC, "value": value, "unit": "trees/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -302,6 +309,11 @@ def run_ours(args, rank, world):
                      "kernel": "hist_build_kernel<fixed>",
                      "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
                      "cells_per_s": ts["hist_cells"] / (ts["hist_ms"] / 1e3), "levels": levels},
+        "tree_roofline": {"bound": "hbm", "bytes_per_tree": tree_bytes, "ms_per_tree": ms_max / args.steps,
+                          "achieved": tree_achieved, "peak": peak, "unit": "GB/s", "frac": tree_achieved / peak,
+                          "roofline_trees_per_s": peak * 1e9 / tree_bytes,
+                          "bytes": {"histogram": alg_bytes / args.steps, "gradients": 32 * args.rows,
+                                    "partition": 9 * part_rows, "prediction_update": 21 * args.rows}},
         "plain_fp32_per_node": {"value": plain_steps / (plain_ms / 1e3), "unit": "trees/s",
                                 "speedup_of_fixed_batched": value / world / (plain_steps / (plain_ms / 1e3))},
         "cpu_baseline": cpu,
@@ -398,6 +410,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-rows", type=int, default=500_000)
+    ap.add_argument("--cpu-trees", type=int, default=5,
+                    help="trees of the CPU baseline sample (about 10 s of single-core training)")
     ap.add_argument("--ref-rows", type=int, default=500_000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--rows", type=int, default=ROWS,

@@ -63,7 +63,7 @@
 extern "C" {
 #endif
 
-#define MPSB_CUDA_ABI_VERSION 1
+#define MPSB_CUDA_ABI_VERSION 2
 
 enum {
   MPSB_OK = 0,
@@ -176,6 +176,8 @@ typedef struct {
   double hist_ms;              /* summed CUDA-event time of histogram builds
                                   (MPSB_OPT_TIMING only) */
   uint64_t hist_timed_launches;
+  uint64_t part_rows;          /* rows routed by row partitions (every split level but the
+                                  last, whose rows go straight to the leaves) */
 } mpsb_cuda_stats;
 
 /* Launch shape of a training session: histogram CTA threads and pipeline stages,

@@ -81,6 +81,7 @@ class Stats(C.Structure):
         ("hist_rows", C.c_uint64),
         ("hist_ms", C.c_double),
         ("hist_timed_launches", C.c_uint64),
+        ("part_rows", C.c_uint64),
     ]
 
 

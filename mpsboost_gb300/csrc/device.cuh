@@ -159,6 +159,7 @@ struct Control {
   uint32_t item_rows;      // rows per histogram work item of the current level
   unsigned long long cells;       // cumulative row x feature cells built (accounting)
   unsigned long long rows_built;
+  unsigned long long rows_partitioned;  // rows routed by partitions (accounting)
 };
 
 // ---------------------------------------------------------------------------------

@@ -638,7 +638,7 @@ struct mpsb_cuda_trainer {
   uint32_t blocked_levels = 2;  // levels built from the column-blocked bins
   mpsb_cuda_stats stats{};
   uint64_t kernels_per_round[2] = {0, 0};
-  uint64_t cells_base = 0, rows_base = 0;
+  uint64_t cells_base = 0, rows_base = 0, part_base = 0;
   unsigned long long cells_before_round = 0;
 
   template <class T>
@@ -887,6 +887,7 @@ struct mpsb_cuda_trainer {
     CK(cudaMemcpy(&c, dev.ctl, sizeof c, cudaMemcpyDeviceToHost));
     stats.hist_cells = c.cells - cells_base;
     stats.hist_rows = c.rows_built - rows_base;
+    stats.part_rows = c.rows_partitioned - part_base;
     if (c.error) throw TrainingError(describe_device_error(c.error));
   }
 };
@@ -1293,6 +1294,7 @@ int mpsb_cuda_trainer_reset_stats(mpsb_cuda_trainer* t) {
     CK(cudaMemcpy(&c, t->dev.ctl, sizeof c, cudaMemcpyDeviceToHost));
     t->cells_base = c.cells;
     t->rows_base = c.rows_built;
+    t->part_base = c.rows_partitioned;
     t->cells_before_round = c.cells;
     t->stats = mpsb_cuda_stats{};
     t->level_ms.assign(t->level_ms.size(), 0.0);

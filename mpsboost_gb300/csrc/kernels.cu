@@ -1507,6 +1507,7 @@ __global__ void __launch_bounds__(kPartThreads) partition_count_kernel(TrainerDe
       uint32_t s = 0;
       for (int w = 0; w < kPartThreads / 32; ++w) s += warp_counts[w];
       a.part_counts[c] = s;
+      atomicAdd(&a.ctl->rows_partitioned, (unsigned long long)count);
     }
     __syncthreads();
   }

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     for name in names:
         assert hasattr(lib, name), name
     assert names == set(_lib.SIGNATURES), sorted(names ^ set(_lib.SIGNATURES))
-    assert lib.mpsb_cuda_abi_version() == 1
+    assert lib.mpsb_cuda_abi_version() == 2
 
 
 def test_struct_layouts():

@@ -411,6 +411,8 @@ def test_scale_properties(backend):
         assert t1.tobytes() == t2.tobytes()
     stats = t.stats()
     assert stats["rounds"] == 2 and stats["kernel_launches"] > 0 and stats["hist_cells"] >= n * f
+    # Every round partitions the root's n rows, and at most n rows at each of depths 0-6.
+    assert 2 * n <= stats["part_rows"] <= 2 * 7 * n
 
 
 def _random_bins(seed, rows, feats, nb=255):

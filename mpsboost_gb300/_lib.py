@@ -72,6 +72,9 @@ class Info(C.Structure):
     ]
 
 
+ABI_VERSION = 2  # MPSB_CUDA_ABI_VERSION of the structs below
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("rounds", C.c_uint64),
@@ -241,6 +244,9 @@ def load() -> C.CDLL:
                 fn = getattr(lib, name)
                 fn.restype = res
                 fn.argtypes = args
+            if lib.mpsb_cuda_abi_version() != ABI_VERSION:
+                raise BackendError(f"CUDA backend library {path} has ABI version "
+                                   f"{lib.mpsb_cuda_abi_version()}, these bindings need {ABI_VERSION}")
             _lib = lib
     return _lib
 

@@ -21,6 +21,8 @@
  *   mpsb_cuda_dataset_create           the per-node NewBuffer(dataset.bin_data())
  *                                      upload of src/mps/mps_histogram.mm:149, made
  *                                      once per dataset and kept resident
+ *   mpsb_cuda_dataset_create_async     the same upload left in flight, so the caller's
+ *   mpsb_cuda_dataset_wait             host work (label and weight checks) overlaps it
  *   mpsb_cuda_squared_error            GradientComputer::ComputeSquaredError
  *                                      (backend.hpp:52-58)
  *   mpsb_cuda_build_histograms         HistogramBuilder::BuildHistograms
@@ -244,6 +246,16 @@ int mpsb_cuda_dataset_create(mpsb_cuda_backend* backend, const void* bins,
                              uint32_t bin_width_bytes, const uint8_t* missing,
                              uint64_t rows, uint32_t features, const uint32_t* bin_count,
                              mpsb_cuda_dataset** out);
+/* As mpsb_cuda_dataset_create, but returns once the upload is enqueued. bins and missing
+   must stay valid and unchanged until mpsb_cuda_dataset_wait, or the first entry that
+   reads the dataset (training, prediction, histograms, export), has returned; a bin past
+   its feature's count is reported there (MPSB_ERR_DATA) rather than here. */
+int mpsb_cuda_dataset_create_async(mpsb_cuda_backend* backend, const void* bins,
+                                   uint32_t bin_width_bytes, const uint8_t* missing,
+                                   uint64_t rows, uint32_t features, const uint32_t* bin_count,
+                                   mpsb_cuda_dataset** out);
+/* Waits for an asynchronous upload to complete (returns at once for a complete one). */
+int mpsb_cuda_dataset_wait(const mpsb_cuda_dataset* dataset);
 void mpsb_cuda_dataset_destroy(mpsb_cuda_dataset* dataset);
 /* 1 when the dataset's row-major bins carry a TMA tensor map (row-major histogram levels
    stage their gathered rows with tile::gather4 copies), else 0 (cp.async staging); set at

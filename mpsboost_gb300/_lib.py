@@ -150,6 +150,8 @@ SIGNATURES = {
     "mpsb_quantize_dense": (_I32, [_VP, _I32, _U64, _U32, _U64, _U64, _U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "mpsb_transform_dense": (_I32, [_VP, _I32, _U64, _U32, _U64, _U64, _U32, _VP, _VP, _VP, _U32, _VP, _VP]),
     "mpsb_cuda_dataset_create": (_I32, [_VP, _VP, _U32, _VP, _U64, _U32, _VP, C.POINTER(_VP)]),
+    "mpsb_cuda_dataset_create_async": (_I32, [_VP, _VP, _U32, _VP, _U64, _U32, _VP, C.POINTER(_VP)]),
+    "mpsb_cuda_dataset_wait": (_I32, [_VP]),
     "mpsb_cuda_dataset_destroy": (None, [_VP]),
     "mpsb_cuda_dataset_uses_tma": (_I32, [_VP]),
     "mpsb_cuda_squared_error": (_I32, [_VP, _VP, _VP, _U64, _VP]),

@@ -473,6 +473,7 @@ int mpsb_cuda_dataset_transform(mpsb_cuda_backend* b, const mpsb_cuda_dataset* s
                                 mpsb_cuda_dataset** out) {
   return guard([&] {
     if (!b || !schema || !out) throw TrainingError("null argument");
+    dataset_ready(schema);
     if (!schema->has_schema) throw TrainingError("the schema dataset holds no bin boundaries");
     if (features != schema->features)
       throw DataError("Prediction input feature count does not match the binned schema");
@@ -531,6 +532,7 @@ int mpsb_cuda_dataset_schema(const mpsb_cuda_dataset* d, float* boundaries,
 int mpsb_cuda_dataset_export(const mpsb_cuda_dataset* d, uint8_t* bins, uint8_t* missing) {
   return guard([&] {
     if (!d || !bins) throw TrainingError("null argument");
+    dataset_ready(d);
     d->backend->activate();
     cudaStream_t s = d->backend->stream;
     const size_t cells = size_t(d->n_rows) * d->features;

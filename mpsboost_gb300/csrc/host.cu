@@ -473,12 +473,37 @@ int mpsb_transform_dense(const void* data, int scalar_type, uint64_t rows, uint3
   });
 }
 
+}  // extern "C"
+
 // ---- dataset ---------------------------------------------------------------------------
-int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t width,
-                             const uint8_t* missing, uint64_t rows, uint32_t features,
-                             const uint32_t* bin_count, mpsb_cuda_dataset** out) {
-  return guard([&] {
-    if (!b || !bins || !bin_count || !out) throw TrainingError("null argument");
+namespace mpsb {
+
+void dataset_ready(const mpsb_cuda_dataset* d) {
+  if (d == nullptr) return;
+  if (d->pending) {
+    d->backend->activate();
+    CK(cudaEventSynchronize(d->ready));
+    uint32_t e = 0;
+    CK(cudaMemcpy(&e, d->pack_error.p, sizeof e, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 2; ++k) {
+      d->stage[k].reset();
+      d->mstage[k].reset();
+    }
+    d->pending = false;
+    d->invalid = e != 0;
+  }
+  if (d->invalid) throw DataError("Binned value exceeds the feature histogram range");
+}
+
+namespace {
+
+// Allocates the dataset and enqueues its upload and pack; returns before they complete
+// (the dataset is pending).
+std::unique_ptr<mpsb_cuda_dataset> start_dataset(mpsb_cuda_backend* b, const void* bins,
+                                                 uint32_t width, const uint8_t* missing,
+                                                 uint64_t rows, uint32_t features,
+                                                 const uint32_t* bin_count) {
+    if (!b || !bins || !bin_count) throw TrainingError("null argument");
     if (width != 1 && width != 2) throw DataError("bin width must be 1 or 2 bytes");
     if (rows == 0 || features == 0) throw DataError("dataset must contain at least one row and one feature");
     if (rows >= 0xFFFFFFFFull) throw UnsupportedError("the CUDA backend indexes rows with uint32");
@@ -513,13 +538,17 @@ int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t wi
     d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
     d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
     d->bins_fm.alloc(size_t(features) * rows);
+    d->pack_error.alloc(sizeof(uint32_t));
+    CK(cudaMemsetAsync(d->pack_error.p, 0, sizeof(uint32_t), b->stream));
+    CK(cudaEventCreateWithFlags(&d->ready, cudaEventDisableTiming));
     trace.mark("allocs");
     // Feature block by feature block (32 feature columns, contiguous in the feature-major
     // source): the copy stream uploads block fb + 1 into one staging buffer while the
     // compute stream packs block fb from the other.
     if (!b->copy_stream) CK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
     const size_t block_cells = size_t(kBlockFeatures) * rows;
-    DevBuf stage[2], mstage[2];
+    DevBuf* stage = d->stage;
+    DevBuf* mstage = d->mstage;
     const int nstage = d->nfb > 1 ? 2 : 1;
     for (int k = 0; k < nstage; ++k) {
       stage[k].alloc(block_cells * width);
@@ -548,13 +577,47 @@ int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t wi
       CK(launch_pack_bins_block(stage[k].p, width, missing ? mstage[k].as<uint8_t>() : nullptr,
                                 d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb, fb,
                                 d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(),
-                                d->bins_fm.as<uint8_t>(), b->error.as<uint32_t>(), b->stream));
+                                d->bins_fm.as<uint8_t>(), d->pack_error.as<uint32_t>(), b->stream));
       CK(cudaEventRecord(ev.e[2 + k], b->stream));
     }
-    if (b->take_error()) throw DataError("Binned value exceeds the feature histogram range");
-    trace.mark("upload + pack (synchronized)");
+    CK(cudaEventRecord(d->ready, b->stream));
+    d->pending = true;
+    trace.mark("upload + pack (enqueued)");
     attach_bins_tmap(d.get());
+    return d;
+}
+
+}  // namespace
+}  // namespace mpsb
+
+extern "C" {
+
+int mpsb_cuda_dataset_create(mpsb_cuda_backend* b, const void* bins, uint32_t width,
+                             const uint8_t* missing, uint64_t rows, uint32_t features,
+                             const uint32_t* bin_count, mpsb_cuda_dataset** out) {
+  return guard([&] {
+    if (!out) throw TrainingError("null argument");
+    std::unique_ptr<mpsb_cuda_dataset> d = start_dataset(b, bins, width, missing, rows, features, bin_count);
+    PhaseTrace trace("dataset");
+    dataset_ready(d.get());
+    trace.mark("upload + pack (synchronized)");
     *out = d.release();
+  });
+}
+
+int mpsb_cuda_dataset_create_async(mpsb_cuda_backend* b, const void* bins, uint32_t width,
+                                   const uint8_t* missing, uint64_t rows, uint32_t features,
+                                   const uint32_t* bin_count, mpsb_cuda_dataset** out) {
+  return guard([&] {
+    if (!out) throw TrainingError("null argument");
+    *out = start_dataset(b, bins, width, missing, rows, features, bin_count).release();
+  });
+}
+
+int mpsb_cuda_dataset_wait(const mpsb_cuda_dataset* d) {
+  return guard([&] {
+    if (!d) throw TrainingError("null argument");
+    dataset_ready(d);
   });
 }
 
@@ -922,6 +985,9 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   const RowSums sums = row_sums(weights, single_mean ? labels : nullptr, n, label_mode_of(p->objective),
                                 count_objective_name(p->objective));
   trace.mark("validate weights, label sum");
+  // An asynchronous dataset upload ran beside the host passes above.
+  dataset_ready(ds);
+  trace.mark("dataset upload complete");
   b->activate();
   t->b = b;
   t->ds = ds;
@@ -1326,6 +1392,7 @@ int mpsb_cuda_autotune(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds, const 
                        uint32_t options, uint32_t rounds_per_trial, mpsb_cuda_tuning* out) {
   return guard([&] {
     if (!b || !ds || !labels || !p || !out) throw TrainingError("null argument");
+    dataset_ready(ds);
     if (options & (MPSB_OPT_PER_NODE | MPSB_OPT_TIMING | MPSB_OPT_NO_GRAPH))
       throw UnsupportedError("the autotuner times the batched, graph-captured rounds");
     const uint32_t R = std::max(1u, rounds_per_trial);
@@ -1663,6 +1730,7 @@ namespace {
 // base + lr * sum of the given trees' leaves for every row, on the device.
 void predict_trees(mpsb_cuda_backend* b, const std::vector<const std::vector<mpsb_tree_node>*>& trees,
                    double base, double lr, const mpsb_cuda_dataset* ds, double* out) {
+  dataset_ready(ds);
   std::vector<uint32_t> offsets(trees.size() + 1, 0);
   for (size_t t = 0; t < trees.size(); ++t) {
     offsets[t + 1] = offsets[t] + uint32_t(trees[t]->size());

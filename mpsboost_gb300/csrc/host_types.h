@@ -138,7 +138,32 @@ struct mpsb_cuda_dataset {
   std::vector<uint64_t> boundary_offset;
   std::vector<uint32_t> boundary_count;
   std::vector<uint64_t> missing_count;
+  // Upload state. An asynchronous upload (mpsb_cuda_dataset_create_async) is pending until
+  // mpsb::dataset_ready has waited for `ready`: until then the staging buffers stay alive
+  // and the pack kernels' range error (`pack_error`) is unread. Work on the backend's
+  // stream is ordered after the packs, so only the host needs to wait.
+  mutable bool pending = false;
+  mutable bool invalid = false;
+  cudaEvent_t ready = nullptr;
+  mpsb::DevBuf pack_error;
+  mutable mpsb::DevBuf stage[2], mstage[2];
+  mpsb_cuda_dataset() = default;
+  mpsb_cuda_dataset(const mpsb_cuda_dataset&) = delete;
+  mpsb_cuda_dataset& operator=(const mpsb_cuda_dataset&) = delete;
+  ~mpsb_cuda_dataset() {
+    if (ready) {
+      cudaEventSynchronize(ready);  // copies in flight read the staging buffers
+      cudaEventDestroy(ready);
+    }
+  }
 };
+
+namespace mpsb {
+// Completes a pending upload: waits for the packs, releases the staging buffers and throws
+// DataError for a bin past its feature's count. Every entry that reads a dataset's device
+// arrays calls it first; it returns at once for a complete upload.
+void dataset_ready(const mpsb_cuda_dataset* d);
+}  // namespace mpsb
 
 struct mpsb_cuda_model {
   uint32_t n_trees = 0;

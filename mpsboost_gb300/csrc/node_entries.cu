@@ -39,6 +39,7 @@ struct Session {
 };
 
 void base_session(Session& ss, mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds) {
+  dataset_ready(ds);
   TrainerDev& a = ss.a;
   a.bins = ds->bins.as<uint8_t>();
   a.bins_row_stride = uint64_t(ds->nfb) * kBlockFeatures;

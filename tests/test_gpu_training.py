@@ -247,6 +247,92 @@ def test_dataset_upload_layouts(backend, rows):
     assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
 
 
+def _c_dataset(lib, backend, binned, create):
+    import ctypes as C
+
+    from mpsboost_gb300 import _lib
+
+    ds = C.c_void_p()
+    bins = np.ascontiguousarray(binned.bins)
+    miss = np.ascontiguousarray(binned.missing, dtype=np.uint8)
+    counts = np.ascontiguousarray(binned.bin_counts, np.uint32)
+    rc = create(backend.handle, _lib.ptr(bins), bins.itemsize, _lib.ptr(miss), binned.rows, binned.features,
+                _lib.ptr(counts), C.byref(ds))
+    return rc, ds, (bins, miss, counts)
+
+
+def _c_fit(lib, backend, ds, y, w, **params):
+    import ctypes as C
+
+    from mpsboost_gb300 import _lib
+
+    p, keep = mb.make_params(**params)
+    model = C.c_void_p()
+    rc = lib.mpsb_cuda_train_regressor(backend.handle, ds, _lib.ptr(y), _lib.ptr(w), y.size, C.byref(p), 0,
+                                       C.byref(model))
+    del keep
+    if rc:
+        return rc, None
+    trees = []
+    for t in range(lib.mpsb_cuda_model_tree_count(model)):
+        out = np.empty(lib.mpsb_cuda_model_tree_node_count(model, t), _lib.NODE_DTYPE)
+        _lib.check(lib.mpsb_cuda_model_tree_nodes(model, t, _lib.ptr(out)))
+        trees.append(out)
+    preds = np.empty(y.size)
+    _lib.check(lib.mpsb_cuda_model_train_predictions(model, _lib.ptr(preds)))
+    lib.mpsb_cuda_model_destroy(model)
+    return 0, (trees, preds)
+
+
+def test_async_dataset_upload(backend):
+    """mpsb_cuda_dataset_create_async: training on a dataset whose upload is still in
+    flight (the host checks labels and weights meanwhile) gives the trees and predictions
+    of the synchronous upload; a bin past its feature's count is reported by the wait
+    and by every later entry, not by the create."""
+    from mpsboost_gb300 import _lib
+
+    lib = _lib.load()
+    x, y, w = _data(48, 300_000, 70, 0.03, 2)
+    binned = mb.quantize_dense(x, 255)
+    params = dict(n_estimators=3, learning_rate=0.3, max_depth=6, min_samples_leaf=2)
+    results = []
+    bins = np.ascontiguousarray(binned.bins)
+    pinned = mb.BinnedDataset(**{**{f: getattr(binned, f) for f in (
+        "rows", "features", "max_bins", "missing", "boundaries_flat", "boundary_offsets",
+        "boundary_counts", "bin_counts", "missing_counts")}, "bins": bins})
+    _lib.check(lib.mpsb_cuda_host_register(_lib.ptr(bins), bins.nbytes))  # copies run async
+    try:
+        for create in (lib.mpsb_cuda_dataset_create, lib.mpsb_cuda_dataset_create_async):
+            rc, ds, keep = _c_dataset(lib, backend, pinned, create)
+            assert rc == 0
+            rc, res = _c_fit(lib, backend, ds, y, w, **params)
+            assert rc == 0
+            assert lib.mpsb_cuda_dataset_wait(ds) == 0
+            lib.mpsb_cuda_dataset_destroy(ds)
+            del keep
+            results.append(res)
+    finally:
+        lib.mpsb_cuda_host_unregister(_lib.ptr(bins))
+    (ta, pa), (tb, pb) = results
+    assert [t.tobytes() for t in ta] == [t.tobytes() for t in tb]
+    assert pa.tobytes() == pb.tobytes()
+
+    import dataclasses
+
+    bad = dataclasses.replace(binned, bins=binned.bins.copy(), _device={})
+    row = int(np.flatnonzero(~bad.missing[5])[0])
+    bad.bins[5, row] = bad.bin_counts[5]  # one past the feature's last bin
+    rc, ds, keep = _c_dataset(lib, backend, bad, lib.mpsb_cuda_dataset_create_async)
+    assert rc == 0
+    assert lib.mpsb_cuda_dataset_wait(ds) == _lib.MPSB_ERR_DATA
+    assert b"exceeds" in lib.mpsb_cuda_last_error()
+    rc, _ = _c_fit(lib, backend, ds, y, w, **params)
+    assert rc == _lib.MPSB_ERR_DATA
+    lib.mpsb_cuda_dataset_destroy(ds)
+    rc, ds, keep = _c_dataset(lib, backend, bad, lib.mpsb_cuda_dataset_create)
+    assert rc == _lib.MPSB_ERR_DATA and not ds.value
+
+
 @pytest.mark.parametrize("threads", ["768", "512"])
 def test_tma_staging_equals_cp_async(backend, monkeypatch, threads):
     """Row-major levels whose gathered rows arrive by TMA gather4 copies give the same

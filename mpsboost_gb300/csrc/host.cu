@@ -480,6 +480,7 @@ namespace mpsb {
 
 void dataset_ready(const mpsb_cuda_dataset* d) {
   if (d == nullptr) return;
+  std::lock_guard<std::mutex> lock(d->ready_mutex);
   if (d->pending) {
     d->backend->activate();
     CK(cudaEventSynchronize(d->ready));

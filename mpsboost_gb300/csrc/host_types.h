@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <utility>
@@ -142,6 +143,7 @@ struct mpsb_cuda_dataset {
   // mpsb::dataset_ready has waited for `ready`: until then the staging buffers stay alive
   // and the pack kernels' range error (`pack_error`) is unread. Work on the backend's
   // stream is ordered after the packs, so only the host needs to wait.
+  mutable std::mutex ready_mutex;  // threads sharing a pending dataset complete it once
   mutable bool pending = false;
   mutable bool invalid = false;
   cudaEvent_t ready = nullptr;

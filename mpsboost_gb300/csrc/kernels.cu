@@ -1507,7 +1507,6 @@ __global__ void __launch_bounds__(kPartThreads) partition_count_kernel(TrainerDe
       uint32_t s = 0;
       for (int w = 0; w < kPartThreads / 32; ++w) s += warp_counts[w];
       a.part_counts[c] = s;
-      atomicAdd(&a.ctl->rows_partitioned, (unsigned long long)count);
     }
     __syncthreads();
   }
@@ -1529,6 +1528,7 @@ __global__ void __launch_bounds__(1024) partition_scan_kernel(TrainerDev a) {
       carry += tot[0];
     }
     if (carry != a.part[e].lcount) err |= kErrPartition;
+    if (threadIdx.x == 0) atomicAdd(&a.ctl->rows_partitioned, (unsigned long long)a.part[e].seg_cnt);
     __syncthreads();
   }
   if (err && threadIdx.x == 0) raise(a.ctl, err);

@@ -759,7 +759,7 @@ struct mpsb_cuda_trainer {
     CK(launch_round_setup(dev, s)); ++k;
     if (leafwise) {
       k += enqueue_leafwise(root_gradient_only);
-      CK(launch_apply_leaves(dev, grid(8), s)); ++k;
+      CK(launch_apply_leaves(dev, grid(8), s)); k += 2;
       CK(launch_round_end(dev, s)); ++k;
       return k;
     }
@@ -806,7 +806,7 @@ struct mpsb_cuda_trainer {
         CK(launch_partition(dev, grid(4), s)); k += kPartitionKernels;
       }
     }
-    CK(launch_apply_leaves(dev, grid(8), s)); ++k;
+    CK(launch_apply_leaves(dev, grid(8), s)); k += 2;
     CK(launch_round_end(dev, s)); ++k;
     return k;
   }
@@ -1233,6 +1233,11 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.max_leafsegs = uint32_t(T * (leaves + 1));
   a.leafseg = t->alloc<LeafSeg>(a.max_leafsegs);
   a.leaf_prefix = t->alloc<uint32_t>(a.max_leafsegs + 1);
+  if (!a.skip_apply) {
+    a.leaf_of = t->alloc<uint32_t>(size_t(T) * n);
+    CK(cudaMemsetAsync(a.leaf_of, 0xff, size_t(T) * n * sizeof(uint32_t), s));  // no leaf yet
+    a.leaf_steps = t->alloc<double>(2 * size_t(a.max_leafsegs));
+  }
   a.max_tree_nodes = uint32_t(tree_nodes);
   a.tree_nodes = t->alloc<TreeNodeOut>(size_t(T) * tree_nodes);
   a.ctl = t->alloc<Control>(1);

@@ -1914,6 +1914,14 @@ __global__ void leafwise_finish_kernel(TrainerDev a) {
 // ------------------------------------------------------------------------------------
 // Leaf application and round end
 // ------------------------------------------------------------------------------------
+// The prediction update runs in two passes. The first walks the leaf segments (a
+// segment's rows ascend but are spread over the whole row range), routes the rows of
+// last-level splits, and records per row which of its segment's steps applies (a 4-byte
+// scattered write into an array that stays in L2); the second walks the rows in order and
+// adds that step to the row's prediction, so the FP64 predictions are read and written as
+// streams instead of one 32-byte sector each way per row.
+constexpr uint32_t kNoLeaf = 0xffffffffu;
+
 __global__ void __launch_bounds__(256, 4) apply_leaves_kernel(TrainerDev a) {
   if (a.skip_apply) return;  // forest trees: no training predictions
   const double lr = a.params.learning_rate;
@@ -1926,34 +1934,27 @@ __global__ void __launch_bounds__(256, 4) apply_leaves_kernel(TrainerDev a) {
     const uint32_t start = (c - a.leaf_prefix[s]) * kApplyChunk;
     const uint32_t count = min(kApplyChunk, ls.seg_cnt - start);
     const uint32_t* rows = a.rows + (size_t(ls.tree) * 2 + ls.parity) * a.seg_stride + ls.seg_off + start;
-    // Softmax trees update the margins of the current round's class.
-    const size_t pred_row = a.n_classes ? *a.round_counter % a.n_classes : ls.tree;
-    double* pred = a.preds + pred_row * a.n_rows;
-    // lr * leaf is the same product for every row of a leaf.
-    const double step = __dmul_rn(lr, ls.value);
-    const double step_l = ls.split ? __dmul_rn(lr, ls.left_value) : step;
-    const double step_r = ls.split ? __dmul_rn(lr, ls.right_value) : step;
-    // Eight rows per thread at a time: row ids, then routing gathers and predictions,
-    // then the stores (a segment's rows are distinct, so the updates do not collide).
+    uint32_t* leaf_of = a.leaf_of + size_t(ls.tree) * a.n_rows;
+    if (start == 0 && threadIdx.x == 0) {
+      // lr * leaf is the same product for every row of a leaf.
+      const double step = __dmul_rn(lr, ls.value);
+      a.leaf_steps[2 * s] = ls.split ? __dmul_rn(lr, ls.left_value) : step;
+      a.leaf_steps[2 * s + 1] = ls.split ? __dmul_rn(lr, ls.right_value) : step;
+    }
+    // Eight rows per thread at a time: row ids, then the routing gathers, then the stores.
     constexpr int B = 8;
     for (uint32_t p0 = 0; p0 < count; p0 += B * blockDim.x) {
       uint32_t r[B];
 #pragma unroll
       for (int k = 0; k < B; ++k) {
         const uint32_t p = p0 + k * blockDim.x + threadIdx.x;
-        r[k] = p < count ? __ldg(rows + p) : 0xffffffffu;
+        r[k] = p < count ? __ldg(rows + p) : kNoLeaf;
       }
-      double v[B], old[B];
+      uint32_t side[B];
 #pragma unroll
-      for (int k = 0; k < B; ++k) {
-        v[k] = step;
-        old[k] = 0.0;
-        if (r[k] < a.n_rows) {
-          if (ls.split)
-            v[k] = row_goes_left(a, r[k], ls.feature, ls.threshold, ls.default_left) ? step_l : step_r;
-          old[k] = pred[r[k]];
-        }
-      }
+      for (int k = 0; k < B; ++k)
+        side[k] = (ls.split && r[k] < a.n_rows &&
+                   !row_goes_left(a, r[k], ls.feature, ls.threshold, ls.default_left)) ? 1u : 0u;
 #pragma unroll
       for (int k = 0; k < B; ++k) {
         const uint32_t p = p0 + k * blockDim.x + threadIdx.x;
@@ -1962,11 +1963,36 @@ __global__ void __launch_bounds__(256, 4) apply_leaves_kernel(TrainerDev a) {
           err = kErrCapacity;
           continue;
         }
-        const double out = __dadd_rn(old[k], v[k]);
-        if (!f64_finite(out)) err = kErrNonFinite;
-        pred[r[k]] = out;
+        leaf_of[r[k]] = 2 * s + side[k];
       }
     }
+  }
+  if (err) raise(a.ctl, err);
+}
+
+// Row order: prediction += the step recorded for the row, then the record is cleared, so
+// a row that no leaf segment covered in a round is caught in the next.
+__global__ void __launch_bounds__(256) apply_steps_kernel(TrainerDev a) {
+  if (a.skip_apply) return;
+  uint32_t err = 0;
+  const uint32_t steps = 2 * a.ctl->n_leafseg;
+  // Softmax trees update the margins of the current round's class.
+  const uint32_t klass = a.n_classes ? *a.round_counter % a.n_classes : 0u;
+  const size_t total = size_t(a.n_trees) * a.n_rows;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const uint32_t t = uint32_t(i / a.n_rows);
+    const uint32_t r = uint32_t(i - size_t(t) * a.n_rows);
+    const uint32_t idx = a.leaf_of[i];
+    if (idx >= steps) {
+      err = kErrPartition;
+      continue;
+    }
+    a.leaf_of[i] = kNoLeaf;
+    double* pred = a.preds + size_t(a.n_classes ? klass : t) * a.n_rows;
+    const double out = __dadd_rn(pred[r], a.leaf_steps[idx]);
+    if (!f64_finite(out)) err = kErrNonFinite;
+    pred[r] = out;
   }
   if (err) raise(a.ctl, err);
 }
@@ -2277,6 +2303,7 @@ cudaError_t launch_fill_f64(double* dst, uint64_t n, double value, cudaStream_t 
 }
 cudaError_t launch_apply_leaves(const TrainerDev& a, int grid, cudaStream_t s) {
   apply_leaves_kernel<<<grid, 256, 0, s>>>(a);
+  apply_steps_kernel<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 cudaError_t launch_round_end(const TrainerDev& a, cudaStream_t s) {

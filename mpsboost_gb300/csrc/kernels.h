@@ -76,6 +76,9 @@ struct TrainerDev {
   uint32_t* part_flags;         // [max_part_chunks][kPartChunk / 32]
   uint32_t max_part_chunks;
   LeafSeg* leafseg;             // [max_leafsegs]
+  uint32_t* leaf_of;            // [n_trees][n_rows]: 2 x leaf segment + side, per row of the
+                                // round (kNoLeaf between rounds)
+  double* leaf_steps;           // [2 * max_leafsegs]: lr x leaf value per (segment, side)
   uint32_t* leaf_prefix;        // [max_leafsegs + 1]
   uint32_t max_leafsegs;
   TreeNodeOut* tree_nodes;      // [n_trees][max_tree_nodes]

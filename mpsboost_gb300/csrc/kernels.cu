@@ -206,6 +206,9 @@ __device__ __forceinline__ bool f64_negative(double x) {
 }
 
 // grid = (x, n_trees): blockIdx.y is the tree, so a block's maxima belong to one tree.
+// SQ: squared error without softmax classes only; the instantiation leaves out the other
+// objectives' code, so it needs fewer registers and more rows are in flight per SM.
+template <bool SQ>
 __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
   __shared__ uint32_t sg[8], shh[8];
   const uint32_t t = blockIdx.y;
@@ -230,7 +233,7 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
       y = (yb == class_bits || (t == 0 && (yb << 1) == 0)) ? 1.0 : 0.0;
     }
     double g = 0.0, h = 0.0;
-    if (a.objective == 0 && !a.n_classes) {
+    if (SQ || (a.objective == 0 && !a.n_classes)) {
       // Squared error (the objective_pair case 0 then the weight products): g = w (p - y),
       // h = w; two FP64 operations per row on the narrow FP64 pipe.
       const double pred = a.preds[tree_off + i];
@@ -243,7 +246,7 @@ __global__ void __launch_bounds__(256) gradients_kernel(TrainerDev a) {
         h = w;
         if (!f64_finite(g) || !f64_finite(h) || f64_negative(h)) bad = 1;
       }
-    } else {
+    } else if constexpr (!SQ) {
       if (a.n_classes) {
         if (!softmax_pair(a, y, i, *a.round_counter % a.n_classes, &g, &h)) bad = 1;
       } else {
@@ -2199,7 +2202,10 @@ cudaError_t launch_round_begin(const TrainerDev& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 cudaError_t launch_gradients(const TrainerDev& a, int grid, cudaStream_t s) {
-  gradients_kernel<<<dim3(grid, a.n_trees), 256, 0, s>>>(a);
+  if (a.objective == 0 && !a.n_classes)  // twice the CTAs: twice as many fit on an SM
+    gradients_kernel<true><<<dim3(2 * grid, a.n_trees), 256, 0, s>>>(a);
+  else
+    gradients_kernel<false><<<dim3(grid, a.n_trees), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 cudaError_t launch_round_setup(const TrainerDev& a, cudaStream_t s) {

@@ -504,88 +504,88 @@ std::unique_ptr<mpsb_cuda_dataset> start_dataset(mpsb_cuda_backend* b, const voi
                                                  uint32_t width, const uint8_t* missing,
                                                  uint64_t rows, uint32_t features,
                                                  const uint32_t* bin_count) {
-    if (!b || !bins || !bin_count) throw TrainingError("null argument");
-    if (width != 1 && width != 2) throw DataError("bin width must be 1 or 2 bytes");
-    if (rows == 0 || features == 0) throw DataError("dataset must contain at least one row and one feature");
-    if (rows >= 0xFFFFFFFFull) throw UnsupportedError("the CUDA backend indexes rows with uint32");
-    b->activate();
-    PhaseTrace trace("dataset");
-    std::unique_ptr<mpsb_cuda_dataset> d(new mpsb_cuda_dataset);
-    d->backend = b;
-    d->n_rows = uint32_t(rows);
-    d->features = features;
-    d->nfb = (features + kBlockFeatures - 1) / kBlockFeatures;
-    d->h_bin_count.assign(bin_count, bin_count + features);
-    d->h_has_missing.assign(features, 0);
+  if (!b || !bins || !bin_count) throw TrainingError("null argument");
+  if (width != 1 && width != 2) throw DataError("bin width must be 1 or 2 bytes");
+  if (rows == 0 || features == 0) throw DataError("dataset must contain at least one row and one feature");
+  if (rows >= 0xFFFFFFFFull) throw UnsupportedError("the CUDA backend indexes rows with uint32");
+  b->activate();
+  PhaseTrace trace("dataset");
+  std::unique_ptr<mpsb_cuda_dataset> d(new mpsb_cuda_dataset);
+  d->backend = b;
+  d->n_rows = uint32_t(rows);
+  d->features = features;
+  d->nfb = (features + kBlockFeatures - 1) / kBlockFeatures;
+  d->h_bin_count.assign(bin_count, bin_count + features);
+  d->h_has_missing.assign(features, 0);
+  for (uint32_t f = 0; f < features; ++f) {
+    if (bin_count[f] == 0) throw DataError("every feature needs at least one bin");
+    if (bin_count[f] > 256)
+      throw UnsupportedError("the CUDA backend supports at most 256 bins per feature");
+  }
+  if (missing) {
     for (uint32_t f = 0; f < features; ++f) {
-      if (bin_count[f] == 0) throw DataError("every feature needs at least one bin");
-      if (bin_count[f] > 256)
-        throw UnsupportedError("the CUDA backend supports at most 256 bins per feature");
+      const uint8_t* m = missing + uint64_t(f) * rows;
+      for (uint64_t r = 0; r < rows; ++r)
+        if (m[r]) { d->h_has_missing[f] = 1; break; }
+      if (d->h_has_missing[f] && bin_count[f] > 255)
+        throw UnsupportedError("a feature with missing values may have at most 255 bins on the CUDA backend");
     }
-    if (missing) {
-      for (uint32_t f = 0; f < features; ++f) {
-        const uint8_t* m = missing + uint64_t(f) * rows;
-        for (uint64_t r = 0; r < rows; ++r)
-          if (m[r]) { d->h_has_missing[f] = 1; break; }
-        if (d->h_has_missing[f] && bin_count[f] > 255)
-          throw UnsupportedError("a feature with missing values may have at most 255 bins on the CUDA backend");
-      }
+  }
+  trace.mark("bin counts, missing scan");
+  d->bin_count.alloc(features * sizeof(uint32_t));
+  d->has_missing.alloc(features);
+  CK(cudaMemcpyAsync(d->bin_count.p, bin_count, features * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(d->has_missing.p, d->h_has_missing.data(), features, cudaMemcpyHostToDevice, b->stream));
+  d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+  d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+  d->bins_fm.alloc(size_t(features) * rows);
+  d->pack_error.alloc(sizeof(uint32_t));
+  CK(cudaMemsetAsync(d->pack_error.p, 0, sizeof(uint32_t), b->stream));
+  CK(cudaEventCreateWithFlags(&d->ready, cudaEventDisableTiming));
+  trace.mark("allocs");
+  // Feature block by feature block (32 feature columns, contiguous in the feature-major
+  // source): the copy stream uploads block fb + 1 into one staging buffer while the
+  // compute stream packs block fb from the other.
+  if (!b->copy_stream) CK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+  const size_t block_cells = size_t(kBlockFeatures) * rows;
+  DevBuf* stage = d->stage;
+  DevBuf* mstage = d->mstage;
+  const int nstage = d->nfb > 1 ? 2 : 1;
+  for (int k = 0; k < nstage; ++k) {
+    stage[k].alloc(block_cells * width);
+    if (missing) mstage[k].alloc(block_cells);
+  }
+  struct Events {
+    cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+    ~Events() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
     }
-    trace.mark("bin counts, missing scan");
-    d->bin_count.alloc(features * sizeof(uint32_t));
-    d->has_missing.alloc(features);
-    CK(cudaMemcpyAsync(d->bin_count.p, bin_count, features * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
-    CK(cudaMemcpyAsync(d->has_missing.p, d->h_has_missing.data(), features, cudaMemcpyHostToDevice, b->stream));
-    d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
-    d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
-    d->bins_fm.alloc(size_t(features) * rows);
-    d->pack_error.alloc(sizeof(uint32_t));
-    CK(cudaMemsetAsync(d->pack_error.p, 0, sizeof(uint32_t), b->stream));
-    CK(cudaEventCreateWithFlags(&d->ready, cudaEventDisableTiming));
-    trace.mark("allocs");
-    // Feature block by feature block (32 feature columns, contiguous in the feature-major
-    // source): the copy stream uploads block fb + 1 into one staging buffer while the
-    // compute stream packs block fb from the other.
-    if (!b->copy_stream) CK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
-    const size_t block_cells = size_t(kBlockFeatures) * rows;
-    DevBuf* stage = d->stage;
-    DevBuf* mstage = d->mstage;
-    const int nstage = d->nfb > 1 ? 2 : 1;
-    for (int k = 0; k < nstage; ++k) {
-      stage[k].alloc(block_cells * width);
-      if (missing) mstage[k].alloc(block_cells);
-    }
-    struct Events {
-      cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
-      ~Events() {
-        for (cudaEvent_t x : e)
-          if (x) cudaEventDestroy(x);
-      }
-    } ev;  // copied[2], packed[2]
-    for (cudaEvent_t& x : ev.e) CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
-    for (uint32_t fb = 0; fb < d->nfb; ++fb) {
-      const int k = int(fb & 1);
-      const uint32_t nf = std::min<uint32_t>(kBlockFeatures, features - fb * kBlockFeatures);
-      const size_t first = size_t(fb) * block_cells;
-      if (fb >= 2) CK(cudaStreamWaitEvent(b->copy_stream, ev.e[2 + k], 0));  // block fb-2 packed
-      CK(cudaMemcpyAsync(stage[k].p, static_cast<const uint8_t*>(bins) + first * width,
-                         size_t(nf) * rows * width, cudaMemcpyHostToDevice, b->copy_stream));
-      if (missing)
-        CK(cudaMemcpyAsync(mstage[k].p, missing + first, size_t(nf) * rows, cudaMemcpyHostToDevice,
-                           b->copy_stream));
-      CK(cudaEventRecord(ev.e[k], b->copy_stream));
-      CK(cudaStreamWaitEvent(b->stream, ev.e[k], 0));
-      CK(launch_pack_bins_block(stage[k].p, width, missing ? mstage[k].as<uint8_t>() : nullptr,
-                                d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb, fb,
-                                d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(),
-                                d->bins_fm.as<uint8_t>(), d->pack_error.as<uint32_t>(), b->stream));
-      CK(cudaEventRecord(ev.e[2 + k], b->stream));
-    }
-    CK(cudaEventRecord(d->ready, b->stream));
-    d->pending = true;
-    trace.mark("upload + pack (enqueued)");
-    attach_bins_tmap(d.get());
-    return d;
+  } ev;  // copied[2], packed[2]
+  for (cudaEvent_t& x : ev.e) CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+  for (uint32_t fb = 0; fb < d->nfb; ++fb) {
+    const int k = int(fb & 1);
+    const uint32_t nf = std::min<uint32_t>(kBlockFeatures, features - fb * kBlockFeatures);
+    const size_t first = size_t(fb) * block_cells;
+    if (fb >= 2) CK(cudaStreamWaitEvent(b->copy_stream, ev.e[2 + k], 0));  // block fb-2 packed
+    CK(cudaMemcpyAsync(stage[k].p, static_cast<const uint8_t*>(bins) + first * width,
+                       size_t(nf) * rows * width, cudaMemcpyHostToDevice, b->copy_stream));
+    if (missing)
+      CK(cudaMemcpyAsync(mstage[k].p, missing + first, size_t(nf) * rows, cudaMemcpyHostToDevice,
+                         b->copy_stream));
+    CK(cudaEventRecord(ev.e[k], b->copy_stream));
+    CK(cudaStreamWaitEvent(b->stream, ev.e[k], 0));
+    CK(launch_pack_bins_block(stage[k].p, width, missing ? mstage[k].as<uint8_t>() : nullptr,
+                              d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb, fb,
+                              d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(),
+                              d->bins_fm.as<uint8_t>(), d->pack_error.as<uint32_t>(), b->stream));
+    CK(cudaEventRecord(ev.e[2 + k], b->stream));
+  }
+  CK(cudaEventRecord(d->ready, b->stream));
+  d->pending = true;
+  trace.mark("upload + pack (enqueued)");
+  attach_bins_tmap(d.get());
+  return d;
 }
 
 }  // namespace

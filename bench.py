@@ -40,8 +40,10 @@ PARAMS = dict(max_depth=DEPTH, learning_rate=LR, min_samples_leaf=20, min_child_
 METRIC = "trees/s @10Mx128x255bins d8 (fixed-point batched)"
 # DRAM bytes per histogram launch on this workload: one ncu capture of
 # dram__bytes_read.sum + dram__bytes_write.sum over the 24 histogram launches of three
-# steady-state rounds (610.6 MB read + 6.9 MB written per launch on average).
+# steady-state rounds (610.6 MB read + 6.9 MB written per launch on average), recorded
+# with its command in the profile named below.
 HIST_TRAFFIC_BYTES_PER_LAUNCH = 617.5e6
+HIST_TRAFFIC_PROFILE = "profiles/hist_build_dram_traffic_10Mx128_d8.md"
 CONFIG = {
     "workload": "regression 10,000,000 rows x 128 features (64 normal, 32 lognormal, 32 int[0,1000)), "
                 "255 bins, depth 8, lr 0.05, weighted squared error",
@@ -70,6 +72,51 @@ def make_data(rows: int, seed: int = SEED):
         y += (xf[a] * scale[a]).astype(np.float64) * (xf[b] * scale[b])
     w = rng.uniform(0.5, 1.5, rows)
     return xf, y, w
+
+
+def make_logistic_data(rows: int = 4_000_000):
+    """Binary logistic configuration: rows x 256 float32 (200 N(0,1) features and 56
+    integer features with 2-16 distinct values), 10 % of all cells NaN; labels ~
+    Bernoulli(sigmoid(w . x[:32] + 0.5 x0 x1)), w ~ N(0, 1/32), missing cells read as 0
+    in the label model. Row-major [rows, 256]."""
+    f_cont, f_int = 200, 56
+    rng = np.random.default_rng(20260719 + 3)
+    x = np.empty((rows, f_cont + f_int), np.float32)
+    x[:, :f_cont] = rng.standard_normal((rows, f_cont), dtype=np.float32)
+    card = rng.integers(2, 17, f_int)
+    for j in range(f_int):
+        x[:, f_cont + j] = rng.integers(0, card[j], rows)
+    for lo in range(0, f_cont + f_int, 32):  # 10 % NaN, a column block at a time
+        blk = x[:, lo:lo + 32]
+        blk[rng.random(blk.shape, dtype=np.float32) < 0.1] = np.nan
+    xs = np.nan_to_num(x[:, :32]).astype(np.float64)
+    logit = xs @ rng.normal(0.0, np.sqrt(1.0 / 32), 32) + 0.5 * xs[:, 0] * xs[:, 1]
+    y = (rng.random(rows) < 1.0 / (1.0 + np.exp(-logit))).astype(np.float64)
+    return x, y
+
+
+def make_ovr_data(rows: int = 2_000_000, features: int = 64, classes: int = 10):
+    """One-vs-rest configuration: rows x 64 N(0,1) float32; class = argmax of 10 random
+    linear scores plus Gumbel noise."""
+    rng = np.random.default_rng(20260719 + 4)
+    x = rng.standard_normal((rows, features), dtype=np.float32)
+    scores = x @ rng.standard_normal((features, classes), dtype=np.float32)
+    scores += rng.gumbel(size=(rows, classes)).astype(np.float32)
+    return x, scores.argmax(axis=1).astype(np.float64)
+
+
+def make_forest_data(rows: int = 1_000_000, features: int = 100, trees: int = 256):
+    """Random-forest configuration: rows x 100 N(0,1) float32, Friedman-1 target on
+    x0..x4 (scaled to [0, 1]) + N(0,1); per tree Poisson(1) row counts and a sorted
+    subset of 10 = sqrt(100) features."""
+    rng = np.random.default_rng(20260719 + 5)
+    x = rng.standard_normal((rows, features), dtype=np.float32)
+    u = (x[:, :5] - x[:, :5].min(0)) / (x[:, :5].max(0) - x[:, :5].min(0))
+    y = (10 * np.sin(np.pi * u[:, 0] * u[:, 1]) + 20 * (u[:, 2] - 0.5) ** 2 + 10 * u[:, 3] + 5 * u[:, 4]
+         + rng.normal(size=rows))
+    counts = rng.poisson(1.0, size=(trees, rows)).astype(np.uint8)
+    subsets = [np.sort(rng.choice(features, size=10, replace=False)) for _ in range(trees)]
+    return x, y, counts, subsets
 
 
 def sample_clocks(stop: threading.Event, out: list):
@@ -108,11 +155,13 @@ def measured_peak_hbm():
 
 
 def cpu_baseline(xf, y, w, sample_rows: int, trees: int):
-    """The oracle's FP64 restatement of the reference trainer on a leading row sample."""
+    """The oracle's FP64 restatement of the reference trainer on a leading row sample,
+    on one core as the reference trainer runs."""
     import oracle
 
     oracle.build(reference=False)
     orc = oracle.Oracle("port")
+    orc.set_threads(1)
     x = xf[:, :sample_rows].T  # strided view, columns contiguous
     t0 = time.perf_counter()
     ds = orc.quantize_dense(x, BINS)
@@ -165,6 +214,7 @@ def run_reference(args, rank, world):
 
     oracle.build(reference=False)
     orc = oracle.Oracle("port")
+    orc.set_threads(1)  # the reference trainer is single-threaded
     ds = orc.quantize_dense(xf.T, BINS)
     warm = max(1, min(args.warmup, 3))
     orc.train_regressor(ds, y, w, hist_mode=oracle.HIST_FP64, n_estimators=warm, **PARAMS)
@@ -268,23 +318,31 @@ def run_ours(args, rank, world):
     tree_bytes = alg_bytes / args.steps + 32 * args.rows + 9 * part_rows + 21 * args.rows
     tree_achieved = tree_bytes / (ms_max / args.steps / 1e3) / 1e9
 
-    # Plain path: FP32 atomics, one histogram launch per node, host round trip per level.
-    plain_steps = max(2, args.steps // 4)
-    plain = mb.Trainer(backend, binned, y, w, n_estimators=plain_steps + 2,
-                       options=_lib.OPT_FLOAT_HIST | _lib.OPT_PER_NODE, **PARAMS)
-    plain.run(1)
-    plain.synchronize()
-    backend.timer_begin()
-    plain.run(plain_steps)
-    plain_ms = backend.timer_end()
-    plain.synchronize()
-    plain.close()
+    # Plain paths. FP32 atomics in the same batched, graph-per-round trainer (the price of
+    # exact fixed point alone), and FP32 atomics with one histogram launch per node and a
+    # host round trip per level (the reference's MPS loop, mps_histogram.mm:62-80).
+    def plain_rate(options, steps):
+        t = mb.Trainer(backend, binned, y, w, n_estimators=steps + 2, options=options, **PARAMS)
+        t.run(1)
+        t.synchronize()
+        backend.timer_begin()
+        t.run(steps)
+        ms = backend.timer_end()
+        t.synchronize()
+        t.close()
+        return steps / (ms / 1e3)
 
-    # End to end through the C ABI: pinned host buffers in, model out, K trees.
-    e2e = None
+    batched_fp32 = plain_rate(_lib.OPT_FLOAT_HIST, args.steps)
+    per_node_fp32 = plain_rate(_lib.OPT_FLOAT_HIST | _lib.OPT_PER_NODE, max(2, args.steps // 4))
+
+    # End to end through the C ABI: pinned host buffers in, model out, K trees; and the
+    # same fit from ordinary (pageable) numpy arrays.
+    e2e = e2e_pageable = None
     if rank == 0 or world > 1:
-        e2e = run_e2e(mb, backend, binned, y, w, args.steps)
+        e2e = run_e2e(mb, backend, binned, y, w, args.steps, pinned=True)
+        e2e_pageable = run_e2e(mb, backend, binned, y, w, args.steps, pinned=False)
     trainer.close()
+    secondary = run_secondary(mb, backend) if world == 1 and not args.no_secondary else None
 
     if rank != 0:
         return
@@ -305,7 +363,8 @@ def run_ours(args, rank, world):
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": HIST_TRAFFIC_BYTES_PER_LAUNCH,
-                     "traffic_unit": "bytes per launch (ncu)", "peak_kind": peak_kind,
+                     "traffic_unit": "bytes per launch (ncu)", "traffic_source": HIST_TRAFFIC_PROFILE,
+                     "peak_kind": peak_kind,
                      "kernel": "hist_build_kernel<fixed>",
                      "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
                      "cells_per_s": ts["hist_cells"] / (ts["hist_ms"] / 1e3), "levels": levels},
@@ -314,16 +373,24 @@ def run_ours(args, rank, world):
                           "roofline_trees_per_s": peak * 1e9 / tree_bytes,
                           "bytes": {"histogram": alg_bytes / args.steps, "gradients": 32 * args.rows,
                                     "partition": 9 * part_rows, "prediction_update": 21 * args.rows}},
-        "plain_fp32_per_node": {"value": plain_steps / (plain_ms / 1e3), "unit": "trees/s",
-                                "speedup_of_fixed_batched": value / world / (plain_steps / (plain_ms / 1e3))},
+        "plain_fp32_batched": {"value": batched_fp32, "unit": "trees/s",
+                               "speedup_of_fixed_batched": value / world / batched_fp32,
+                               "note": "FP32 shared atomics, FP64 node sums, same batched graph-per-round trainer"},
+        "plain_fp32_per_node": {"value": per_node_fp32, "unit": "trees/s",
+                                "speedup_of_fixed_batched": value / world / per_node_fp32,
+                                "note": "FP32 atomics, one histogram launch per node, host round trip per level"},
+        "e2e_pageable": e2e_pageable,
+        "secondary": secondary,
         "cpu_baseline": cpu,
         "clocks": clocks_summary(samples),
     }
     print(json.dumps(line), flush=True)
 
 
-def run_e2e(mb, backend, binned, y, w, trees):
-    """One fit through mpsb_cuda_train_regressor from pinned host buffers."""
+def run_e2e(mb, backend, binned, y, w, trees, pinned=True):
+    """One fit through mpsb_cuda_train_regressor: from page-locked host buffers (pinned;
+    registered before the clock starts) or from ordinary numpy arrays (every cost inside
+    the clock)."""
     import ctypes as C
 
     from mpsboost_gb300 import _lib
@@ -333,8 +400,8 @@ def run_e2e(mb, backend, binned, y, w, trees):
     counts = np.ascontiguousarray(binned.bin_counts, np.uint32)
     yy = np.ascontiguousarray(y)
     ww = np.ascontiguousarray(w)
-    pinned = [bins, yy, ww]
-    for a in pinned:
+    registered = [bins, yy, ww] if pinned else []
+    for a in registered:
         _lib.check(lib.mpsb_cuda_host_register(_lib.ptr(a), a.nbytes))
     try:
         p, keep = mb.make_params(n_estimators=trees, **PARAMS)
@@ -357,14 +424,75 @@ def run_e2e(mb, backend, binned, y, w, trees):
         lib.mpsb_cuda_dataset_destroy(ds)
         del keep
     finally:
-        for a in pinned:
+        for a in registered:
             lib.mpsb_cuda_host_unregister(_lib.ptr(a))
     h2d = bins.nbytes + yy.nbytes + ww.nbytes + counts.nbytes
     d2h = nodes * _lib.NODE_DTYPE.itemsize  # the trees (training predictions stay on the device)
     return {"value": trees / dt, "unit": "trees/s", "h2d_bytes_per_step": h2d // trees,
             "d2h_bytes_per_step": d2h // trees, "seconds": dt,
+            "host_memory": "page-locked (registered before timing)" if pinned else "pageable numpy arrays",
             "note": "one fit of K trees: dataset upload (asynchronous, beside the host's label and "
                     "weight checks), training, tree readback"}
+
+
+def run_secondary(mb, backend):
+    """Bounded measurements of the other benchmark configurations on the same GPU.
+
+    binary logistic 4M x 256 (10 % missing, depth 10, lr 0.1): trees/s over 8 graph-
+    replayed rounds, CUDA events on the backend stream, device-binned data resident.
+    one-vs-rest K = 10, 2M x 64, depth 6: per round from two one-shot fits through the
+    public API (12 and 4 rounds; the difference removes setup), 10 trees per round.
+    random forest 1M x 100, 256 trees, depth 12, sqrt features, Poisson(1) rows: one
+    host-timed fit of the whole forest through the public API (sample expansion, upload,
+    training, model readback) after a 16-tree warm-up."""
+    out = {}
+    x, y = make_logistic_data()
+    dset = mb.quantize_device(backend, x, 255)
+    del x
+    params = dict(max_depth=10, learning_rate=0.1, objective="binary_logistic", min_samples_leaf=20,
+                  min_child_weight=1.0, reg_lambda=1.0, max_bins=255)
+    t = mb.Trainer(backend, dset, y, None, n_estimators=12, **params)
+    t.run(3)
+    t.synchronize()
+    backend.timer_begin()
+    t.run(8)
+    ms = backend.timer_end()
+    t.synchronize()
+    t.close()
+    dset.close()
+    out["logistic_4Mx256_d10"] = {"value": 8 / (ms / 1e3), "unit": "trees/s", "ms_per_tree": ms / 8,
+                                  "rounds": 8, "timing": "CUDA events, graph per round"}
+    del y
+
+    x, labels = make_ovr_data()
+    dset = mb.quantize_device(backend, x, 255)
+    del x
+    params = dict(max_depth=6, learning_rate=0.1, min_samples_leaf=20, min_child_weight=1.0, reg_lambda=1.0)
+    mb.train_ovr(backend, dset, labels, 10, n_estimators=2, **params)  # warm
+    times = {}
+    for rounds in (4, 12):
+        backend.synchronize()
+        t0 = time.perf_counter()
+        mb.train_ovr(backend, dset, labels, 10, n_estimators=rounds, **params)
+        times[rounds] = time.perf_counter() - t0
+    dset.close()
+    per_round = (times[12] - times[4]) / 8
+    out["ovr_k10_2Mx64_d6"] = {"value": 10 / per_round, "unit": "trees/s", "ms_per_round": per_round * 1e3,
+                               "fit_seconds_12_rounds": times[12], "timing": "host, (t(12) - t(4)) / 8"}
+    del labels
+
+    x, y, counts, subsets = make_forest_data()
+    binned = mb.quantize_dense(x, 255)
+    del x
+    params = dict(max_depth=12, min_samples_leaf=20, max_bins=255)
+    mb.train_forest(backend, binned, y, row_counts=counts[:16], feature_subsets=subsets[:16], **params)
+    backend.synchronize()
+    t0 = time.perf_counter()
+    models = mb.train_forest(backend, binned, y, row_counts=counts, feature_subsets=subsets, **params)
+    dt = time.perf_counter() - t0
+    out["forest_256_1Mx100_d12"] = {"value": len(models) / dt, "unit": "trees/s", "seconds_per_forest": dt,
+                                    "timing": "host, whole forest through the public API"}
+    return out
 
 
 def run_forest(args, rank, world):
@@ -374,14 +502,8 @@ def run_forest(args, rank, world):
     A step is one forest of ``--forest-trees`` trees."""
     import mpsboost_gb300 as mb
 
-    n, f, trees = 1_000_000, 100, args.forest_trees
-    rng = np.random.default_rng(20260719 + 5)
-    x = rng.standard_normal((n, f), dtype=np.float32)
-    u = (x[:, :5] - x[:, :5].min(0)) / (x[:, :5].max(0) - x[:, :5].min(0))  # to [0, 1]
-    y = (10 * np.sin(np.pi * u[:, 0] * u[:, 1]) + 20 * (u[:, 2] - 0.5) ** 2 + 10 * u[:, 3] + 5 * u[:, 4]
-         + rng.normal(size=n))
-    counts = rng.poisson(1.0, size=(trees, n)).astype(np.uint8)
-    subsets = [rng.choice(f, size=10, replace=False) for _ in range(trees)]
+    trees = args.forest_trees
+    x, y, counts, subsets = make_forest_data(trees=trees)
     binned = mb.quantize_dense(x, 255)
     backend = mb.CudaBackend(int(os.environ.get("LOCAL_RANK", "0")))
     params = dict(max_depth=12, min_samples_leaf=20, max_bins=255)
@@ -416,6 +538,8 @@ def main():
                     help="trees of the CPU baseline sample (about 10 s of single-core training)")
     ap.add_argument("--ref-rows", type=int, default=500_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the bounded logistic / one-vs-rest / forest measurements")
     ap.add_argument("--rows", type=int, default=ROWS,
                     help="rows of the synthetic workload (profiling runs use fewer)")
     ap.add_argument("--workload", choices=["regression", "forest"], default="regression",

@@ -294,7 +294,10 @@ int mpsb_cuda_partition_rows(mpsb_cuda_backend* backend, const mpsb_cuda_dataset
             ((f/32)*dataset_rows + r)*32 + f%32; padding features 0; a missing value may
             use bin 255 and then lands in slot 255),
      rows   u32 [n_rows] row ids of the node (< dataset_rows),
-     pairs  FP32 [dataset_rows][2] gradient/hessian pairs (hessian >= 0),
+     pairs  FP32 [dataset_rows][2] gradient/hessian pairs, all finite, hessians >= 0 (the
+            scale comes from every row's pair, not only the node's); if any pair breaks
+            this, no histogram is built and every bin of `out` gets count 0 and NaN sums,
+            since the entry cannot report an error without waiting for the GPU,
      out    [features][256] bins: exact fixed-point count/G/H as FP64 (same scale rule and
             kernel as mpsb_cuda_build_histograms).
    Work is enqueued on `stream` (a cudaStream_t; NULL = default stream) and not waited for.

@@ -439,14 +439,9 @@ cudaError_t launch_variant(const TrainerDev& a, int grid, cudaStream_t stream,
                            const CUtensorMap* tmap = nullptr) {
   static_assert(HistSmem<MODE>::kBytes % 128 == 0, "stage slots must stay 128-byte aligned");
   const size_t smem = hist_smem_bytes<MODE, THREADS, NSTAGE, TMA>();
-  static bool configured = false;  // per variant; the attribute is per function
-  if (!configured) {
-    const cudaError_t err = cudaFuncSetAttribute(hist_build_kernel<MODE, THREADS, NSTAGE, TMA>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 int(smem));
-    if (err != cudaSuccess) return err;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};  // per variant, one bit per device
+  const cudaError_t err = opt_in_dynamic_smem(configured, hist_build_kernel<MODE, THREADS, NSTAGE, TMA>, smem);
+  if (err != cudaSuccess) return err;
   static const CUtensorMap kNoMap{};
   hist_build_kernel<MODE, THREADS, NSTAGE, TMA><<<grid, THREADS, smem, stream>>>(a, tmap ? *tmap : kNoMap);
   return cudaGetLastError();

@@ -2231,14 +2231,10 @@ cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t s) {
 template <bool FIXED, bool SCREEN>
 cudaError_t launch_scan_variant(const TrainerDev& a, int parity, int grid, int threads, cudaStream_t s) {
   const size_t smem = scan_smem_per_warp<FIXED, SCREEN>() * size_t(threads / 32);
-  static bool configured = false;
-  if (!configured) {
-    const cudaError_t err = cudaFuncSetAttribute(
-        split_scan_kernel<FIXED, SCREEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        int(scan_smem_per_warp<FIXED, SCREEN>() * (kScanThreadsMax / 32)));
-    if (err != cudaSuccess) return err;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};  // one bit per device
+  const cudaError_t err = opt_in_dynamic_smem(configured, split_scan_kernel<FIXED, SCREEN>,
+                                              scan_smem_per_warp<FIXED, SCREEN>() * (kScanThreadsMax / 32));
+  if (err != cudaSuccess) return err;
   split_scan_kernel<FIXED, SCREEN><<<grid, threads, smem, s>>>(a, parity);
   return cudaGetLastError();
 }

@@ -1,6 +1,7 @@
 // Launch interface of the sm_103a kernels (host and device code include this).
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -183,6 +184,24 @@ cudaError_t launch_pack_bins(const void* src, uint32_t width, const uint8_t* mis
                              const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
                              uint32_t nfb, uint8_t* out_rows, uint8_t* out_blocked,
                              uint8_t* out_fm, uint32_t* error, cudaStream_t stream);
+// Raises `kernel`'s dynamic shared memory limit to `bytes` on the current device before
+// its first launch there. The limit is an attribute of the function in that device's
+// context, so it is set once per device: bit d of `devices` records device d (devices
+// past 63 set it before every launch). Two host threads that race past the check both set
+// the same value, which is harmless.
+template <typename Kernel>
+inline cudaError_t opt_in_dynamic_smem(std::atomic<unsigned long long>& devices, Kernel kernel,
+                                       size_t bytes) {
+  int device = 0;
+  cudaError_t err = cudaGetDevice(&device);
+  if (err != cudaSuccess) return err;
+  const unsigned long long bit = device >= 0 && device < 64 ? 1ull << device : 0ull;
+  if (bit && (devices.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (err == cudaSuccess && bit) devices.fetch_or(bit, std::memory_order_acq_rel);
+  return err;
+}
+
 // Number of kernels each launch_* helper enqueues (launch accounting).
 constexpr int kPartitionKernels = 3;
 

@@ -71,10 +71,15 @@ DeviceScratch scratch_for_current_device() {
 }
 
 // max |g| and max h over all dataset rows (the same scale rule as every other entry).
-__global__ void noalloc_maxima_kernel(const float2* pairs, uint32_t n, TreeState* st) {
+// A pair that is not finite, or a negative hessian, sets ctl->error: the entry cannot
+// raise an error without synchronising, so the histogram is then skipped and every bin
+// comes back with NaN sums.
+__global__ void noalloc_maxima_kernel(const float2* pairs, uint32_t n, TreeState* st, Control* ctl) {
   uint32_t mg = 0, mh = 0;
+  bool bad = false;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float2 p = pairs[i];
+    bad |= !isfinite(p.x) || !isfinite(p.y) || p.y < 0.0f;
     mg = max(mg, __float_as_uint(fabsf(p.x)));
     mh = max(mh, __float_as_uint(fmaxf(p.y, 0.0f)));
   }
@@ -82,9 +87,11 @@ __global__ void noalloc_maxima_kernel(const float2* pairs, uint32_t n, TreeState
     mg = max(mg, __shfl_xor_sync(0xffffffffu, mg, off));
     mh = max(mh, __shfl_xor_sync(0xffffffffu, mh, off));
   }
+  bad = __any_sync(0xffffffffu, bad);
   if ((threadIdx.x & 31) == 0) {
     atomicMax(&st->max_abs_g_bits, mg);
     atomicMax(&st->max_h_bits, mh);
+    if (bad) atomicOr(&ctl->error, 1u);
   }
 }
 
@@ -111,18 +118,22 @@ __global__ void noalloc_setup_kernel(TreeState* st, BuildEntry* build, uint32_t*
   prefix[0] = 0;
   prefix[1] = chunks;
   ctl->n_build = 1;
-  ctl->hist_items = chunks * nfb;
+  ctl->hist_items = ctl->error ? 0u : chunks * nfb;  // invalid pairs: no histogram work
   ctl->hist_counter = 0;
 }
 
 // Slot (int64 fixed point) -> [features][256] {count, FP64 G, FP64 H}.
+// Invalid pairs (ctl->error): count 0 and NaN sums in every bin.
 __global__ void noalloc_decode_kernel(const unsigned long long* slot, const TreeState* st,
-                                      uint32_t cells, mpsb_histogram_bin* out) {
+                                      const Control* ctl, uint32_t cells, mpsb_histogram_bin* out) {
+  const bool bad = ctl->error != 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cells; i += gridDim.x * blockDim.x) {
     mpsb_histogram_bin o;
-    o.count = slot[3 * size_t(i)];
-    o.gradient_sum = q_image((long long)slot[3 * size_t(i) + 1], st->inv_g);
-    o.hessian_sum = q_image((long long)slot[3 * size_t(i) + 2], st->inv_h);
+    o.count = bad ? 0ull : slot[3 * size_t(i)];
+    o.gradient_sum = bad ? __longlong_as_double(0x7FF8000000000000ll)
+                         : q_image((long long)slot[3 * size_t(i) + 1], st->inv_g);
+    o.hessian_sum = bad ? __longlong_as_double(0x7FF8000000000000ll)
+                        : q_image((long long)slot[3 * size_t(i) + 2], st->inv_h);
     out[i] = o;
   }
 }
@@ -155,7 +166,7 @@ extern "C" int mpsb_cuda_build_histogram_noalloc(const uint8_t* bins, uint32_t d
     CK(cudaMemsetAsync(slot, 0, slot_bytes, s));
     const float2* gh = reinterpret_cast<const float2*>(pairs);
     const int grid = sc.sm_count * 4;
-    noalloc_maxima_kernel<<<grid, 256, 0, s>>>(gh, dataset_rows, st);
+    noalloc_maxima_kernel<<<grid, 256, 0, s>>>(gh, dataset_rows, st, ctl);
     CK(cudaGetLastError());
     const uint64_t target = uint64_t(sc.sm_count) * 4;
     uint64_t per = (uint64_t(n_rows) * nfb + target - 1) / target;
@@ -185,7 +196,7 @@ extern "C" int mpsb_cuda_build_histogram_noalloc(const uint8_t* bins, uint32_t d
     CK(launch_hist_build(a, HistConfig{}, sc.sm_count, s));
     const uint32_t cells = features * kSlots;
     noalloc_decode_kernel<<<std::max(1u, std::min(4096u, (cells + 255) / 256)), 256, 0, s>>>(
-        slot, st, cells, out);
+        slot, st, ctl, cells, out);
     CK(cudaGetLastError());
   });
 }

@@ -23,7 +23,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liborc.so")
 REF_LIB = os.path.join(HERE, "_ref", "libmpsb_ref.so")
-REFERENCE_ROOT = os.environ.get("MPSB_REFERENCE_ROOT", "/root/reference")
+# The reference project's checkout: MPSB_REFERENCE_ROOT, else a directory named
+# ``reference`` beside this repository.
+REFERENCE_ROOT = os.environ.get(
+    "MPSB_REFERENCE_ROOT", os.path.normpath(os.path.join(HERE, "..", "..", "reference")))
 
 SQUARED_ERROR, BINARY_LOGISTIC, QUANTILE, POISSON, TWEEDIE = range(5)
 HIST_FP64, HIST_FIXED = 0, 1
@@ -546,6 +549,12 @@ class Oracle:
     def _port_only(self):
         if self.kind != "port":
             raise ValueError("only available in the port")
+
+    def set_threads(self, threads: int) -> None:
+        """Threads of the port's feature-parallel loops (0 = all cores; 1 = the
+        reference's single-threaded timing). Results do not depend on it."""
+        self._port_only()
+        self.lib.orc_set_threads(C.c_int(threads))
 
     def fixed_scales(self, pairs32) -> tuple[int, int]:
         self._port_only()

@@ -18,12 +18,23 @@
 
 #include <float.h>
 #include <math.h>
+#include <omp.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 static __thread char g_err[512];
+
+/* Threads of the feature-parallel loops (histograms, missing statistics). Every bin is
+ * owned by one feature and summed in row order whatever the thread count, so results do
+ * not depend on it; 1 reproduces the reference's single-threaded timing. */
+static int g_threads = 0; /* 0: OpenMP's default (all cores) */
+void orc_set_threads(int threads) { g_threads = threads > 0 ? threads : 0; }
+static int n_threads(uint64_t work) {
+  if (work < (1u << 20)) return 1; /* small nodes: not worth a parallel region */
+  return g_threads > 0 ? g_threads : omp_get_max_threads();
+}
 
 static int fail(int code, const char* fmt, ...) {
   va_list ap;
@@ -599,10 +610,10 @@ static uint64_t total_bins(const dataset_t* d) {
 }
 
 /* CpuReferenceBackend::BuildHistograms, reference_backend.cpp:22-71: rows outer so the
-   FP64 accumulation order inside every bin is the row order. */
-static int fp64_histograms(const dataset_t* d, const double* pairs, const uint64_t* rows,
-                           uint64_t n_rows, orc_hist_bin* out) {
-  if (n_rows == 0) return fail(ORC_TRAINING_ERROR, "Node row set must not be empty");
+   FP64 accumulation order inside every bin is the row order. This loop also decides which
+   error is reported first; fp64_histograms below runs it only when an input is invalid. */
+static int fp64_histograms_rows_outer(const dataset_t* d, const double* pairs, const uint64_t* rows,
+                                      uint64_t n_rows, orc_hist_bin* out) {
   uint64_t* offset = (uint64_t*)malloc(d->features * sizeof(uint64_t));
   uint64_t t = 0;
   for (uint32_t f = 0; f < d->features; ++f) { offset[f] = t; t += d->bin_count[f]; }
@@ -629,6 +640,47 @@ static int fp64_histograms(const dataset_t* d, const double* pairs, const uint64
     }
   }
   free(offset);
+  return ORC_OK;
+}
+
+/* The same sums with features outer, one feature per thread at a time: every bin belongs
+   to one feature and still adds its rows in row order, so each bin's FP64 value equals the
+   rows-outer loop's bit for bit. Any invalid input (row index, pair, bin, overflow) reruns
+   the rows-outer loop, which reports the error the reference reports first. */
+static int fp64_histograms(const dataset_t* d, const double* pairs, const uint64_t* rows,
+                           uint64_t n_rows, orc_hist_bin* out) {
+  if (n_rows == 0) return fail(ORC_TRAINING_ERROR, "Node row set must not be empty");
+  int bad = 0;
+  for (uint64_t i = 0; i < n_rows && !bad; ++i) {
+    const uint64_t row = rows[i];
+    if (row >= d->rows) { bad = 1; break; }
+    const double g = pairs[2 * row], h = pairs[2 * row + 1];
+    bad = !isfinite(g) || !isfinite(h) || h < 0.0;
+  }
+  if (bad) return fp64_histograms_rows_outer(d, pairs, rows, n_rows, out);
+  uint64_t* offset = (uint64_t*)malloc(d->features * sizeof(uint64_t));
+  uint64_t t = 0;
+  for (uint32_t f = 0; f < d->features; ++f) { offset[f] = t; t += d->bin_count[f]; }
+  memset(out, 0, t * sizeof(orc_hist_bin));
+  const int64_t nf = (int64_t)d->features;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads(n_rows * d->features)) reduction(|| : bad)
+  for (int64_t f = 0; f < nf; ++f) {
+    const uint16_t* fb = d->bins + (uint64_t)f * d->rows;
+    const uint32_t cnt = d->bin_count[f];
+    orc_hist_bin* o = out + offset[f];
+    for (uint64_t i = 0; i < n_rows; ++i) {
+      const uint64_t row = rows[i];
+      const uint32_t bin = fb[row];
+      if (bin >= cnt) { bad = 1; break; }
+      orc_hist_bin* b = &o[bin];
+      ++b->count;
+      b->gradient_sum += pairs[2 * row];
+      b->hessian_sum += pairs[2 * row + 1];
+      if (!isfinite(b->gradient_sum) || !isfinite(b->hessian_sum)) { bad = 1; break; }
+    }
+  }
+  free(offset);
+  if (bad) return fp64_histograms_rows_outer(d, pairs, rows, n_rows, out);
   return ORC_OK;
 }
 
@@ -675,19 +727,34 @@ static int fixed_histograms(const dataset_t* d, const float* pairs32, int32_t kg
                             orc_fixed_bin* out_bins, orc_fixed_bin* out_missing) {
   memset(out_bins, 0, total_bins(d) * sizeof(orc_fixed_bin));
   memset(out_missing, 0, d->features * sizeof(orc_fixed_bin));
-  for (uint64_t i = 0; i < n_rows; ++i) {
-    const uint64_t row = rows[i];
-    if (row >= d->rows) return fail(ORC_TRAINING_ERROR, "Histogram row index is out of bounds");
-    const int64_t qg = quantize(pairs32[2 * row], kg);
-    const int64_t qh = quantize(pairs32[2 * row + 1], kh);
-    for (uint32_t f = 0; f < d->features; ++f) {
-      const uint64_t cell = (uint64_t)f * d->rows + row;
-      orc_fixed_bin* b = d->missing[cell] ? &out_missing[f] : &out_bins[offset[f] + d->bins[cell]];
-      ++b->count;
-      b->gradient_q += qg;
-      b->hessian_q += qh;
-    }
+  for (uint64_t i = 0; i < n_rows; ++i)
+    if (rows[i] >= d->rows) return fail(ORC_TRAINING_ERROR, "Histogram row index is out of bounds");
+  /* Integer sums do not depend on order: quantize each row once, then one feature per
+     thread at a time. */
+  int64_t* q = (int64_t*)malloc(2 * (n_rows ? n_rows : 1) * sizeof(int64_t));
+  const int64_t nr = (int64_t)n_rows;
+#pragma omp parallel for schedule(static) num_threads(n_threads(n_rows * 16))
+  for (int64_t i = 0; i < nr; ++i) {
+    q[2 * i] = quantize(pairs32[2 * rows[i]], kg);
+    q[2 * i + 1] = quantize(pairs32[2 * rows[i] + 1], kh);
   }
+  const int64_t nf = (int64_t)d->features;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads(n_rows * d->features))
+  for (int64_t f = 0; f < nf; ++f) {
+    const uint16_t* fb = d->bins + (uint64_t)f * d->rows;
+    const uint8_t* fm = d->missing + (uint64_t)f * d->rows;
+    orc_fixed_bin* o = out_bins + offset[f];
+    orc_fixed_bin m = {0, 0, 0};
+    for (int64_t i = 0; i < nr; ++i) {
+      const uint64_t row = rows[i];
+      orc_fixed_bin* b = fm[row] ? &m : &o[fb[row]];
+      ++b->count;
+      b->gradient_q += q[2 * i];
+      b->hessian_q += q[2 * i + 1];
+    }
+    out_missing[f] = m;
+  }
+  free(q);
   return ORC_OK;
 }
 
@@ -1131,7 +1198,10 @@ static int subtract_hist(const ctx_t* x, const node_hist_t* parent, const node_h
 static void node_missing(const ctx_t* x, const active_t* a, const node_hist_t* h, stats_t* miss) {
   const dataset_t* d = x->d;
   memset(miss, 0, d->features * sizeof(stats_t));
-  for (uint32_t f = 0; f < d->features; ++f) {
+  const int64_t nf = (int64_t)d->features;
+  /* Each feature's statistics add its missing rows in row order, whatever the thread. */
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads(x->mode.fixed ? 0 : a->n_rows * d->features))
+  for (int64_t f = 0; f < nf; ++f) {
     if (x->mode.fixed) {
       miss[f].count = h->fx_missing[f].count;
       miss[f].qg = h->fx_missing[f].gradient_q;
@@ -1153,11 +1223,34 @@ static void node_missing(const ctx_t* x, const active_t* a, const node_hist_t* h
 static int find_best_split(const ctx_t* x, const active_t* a, const node_hist_t* h,
                            const stats_t* miss, candidate_t* best) {
   memset(best, 0, sizeof *best);
-  for (uint32_t f = 0; f < x->d->features; ++f) {
-    if (!interaction_allows(x->p, a->path, a->n_path, f)) continue;
-    TRY(scan_feature(x, h, miss, &a->stats, a->lo, a->hi, a->node_index, a->depth, f, best));
+  /* Features are scanned in parallel, each to its own best candidate, and merged in
+     feature order with the same IsBetterSplit test. Two candidates of different features
+     never tie under that test, so the merge picks the candidate the sequential scan
+     picks; the first failing feature's error is reported, as the sequential scan stops
+     there (its message is set again on this thread by scanning that feature once more). */
+  const int64_t nf = (int64_t)x->d->features;
+  candidate_t* per = (candidate_t*)calloc((size_t)(nf ? nf : 1), sizeof(candidate_t));
+  int* rcs = (int*)calloc((size_t)(nf ? nf : 1), sizeof(int));
+#pragma omp parallel for schedule(dynamic, 2) num_threads(n_threads((uint64_t)nf << 16))
+  for (int64_t f = 0; f < nf; ++f) {
+    if (!interaction_allows(x->p, a->path, a->n_path, (uint32_t)f)) continue;
+    rcs[f] = scan_feature(x, h, miss, &a->stats, a->lo, a->hi, a->node_index, a->depth, (uint32_t)f,
+                          &per[f]);
   }
-  return ORC_OK;
+  int rc = ORC_OK;
+  for (int64_t f = 0; f < nf; ++f) {
+    if (rcs[f] != ORC_OK) {
+      candidate_t scratch;
+      memset(&scratch, 0, sizeof scratch);
+      rc = scan_feature(x, h, miss, &a->stats, a->lo, a->hi, a->node_index, a->depth, (uint32_t)f,
+                        &scratch);
+      break;
+    }
+    if (per[f].valid && is_better(&per[f], best)) *best = per[f];
+  }
+  free(per);
+  free(rcs);
+  return rc;
 }
 
 static int goes_left(const dataset_t* d, uint64_t row, uint32_t f, uint32_t thr, int dl) {

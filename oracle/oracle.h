@@ -156,6 +156,9 @@ int ref_softmax_deserialize(const uint8_t* data, uint64_t size, void** model_out
 
 /* Power-of-two scale exponents of one round: q_g = rne(g * 2^kg), q_h = rne(h * 2^kh). */
 int orc_fixed_scales(const float* pairs32, uint64_t n, int32_t* kg, int32_t* kh);
+/* Port only: threads of the feature-parallel loops (0 = all cores). Results do not
+   depend on it. */
+void orc_set_threads(int threads);
 /* Exact int64 histograms of FP32 pairs. Output: features x bin_count bins (bin 0 holds
    the non-missing rows of bin 0 only) followed by one missing-statistics bin per feature. */
 int orc_fixed_histograms(const void* dataset, const float* pairs32, int32_t kg,

@@ -68,6 +68,52 @@ def test_port_matches_reference(port, reference, case):
     assert mp.predict(dp).tobytes() == mr.predict(dr).tobytes()
 
 
+@pytest.mark.parametrize("objective", ["squared_error", "binary_logistic"])
+def test_port_matches_reference_at_scale(port, reference, objective):
+    """The pin at the sizes the GPU parity tests rely on: 120,000 rows x 32 features (the
+    small benchmark configuration's shape, with 2 % missing cells and integer columns),
+    depth 8, U(0.5, 1.5) weights, three rounds; bins, every tree node and the predictions
+    bit for bit. The port runs its feature-parallel loops on every core."""
+    n, f = 120_000, 32
+    x = seeded_matrix(4242, n, f, 0.02, 4)
+    rng = np.random.default_rng(4243)
+    x0, x1, x2, x3 = (np.nan_to_num(x[:, i]).astype(np.float64) for i in range(4))
+    y = np.sin(x0) + x1 * x2 + 0.5 * x3 ** 2 + rng.normal(0.0, 0.1, n)
+    if objective == "binary_logistic":
+        y = (y > np.median(y)).astype(np.float64)
+    w = rng.uniform(0.5, 1.5, n)
+    dp, dr = port.quantize_dense(x, 255), reference.quantize_dense(x, 255)
+    assert np.array_equal(dp.bins, dr.bins) and np.array_equal(dp.missing, dr.missing)
+    assert dp.boundaries_flat.tobytes() == dr.boundaries_flat.tobytes()
+    kw = dict(n_estimators=3, learning_rate=0.1, objective=objective, max_depth=8,
+              min_samples_leaf=20, min_child_weight=1.0, reg_lambda=1.0)
+    port.set_threads(0)
+    mp = port.train_regressor(dp, y, w, hist_mode=oracle.HIST_FP64, **kw)
+    mr = reference.train_regressor(dr, y, w, **kw)
+    assert float(mp.base_score).hex() == float(mr.base_score).hex()
+    assert [t.tobytes() for t in mp.trees] == [t.tobytes() for t in mr.trees]
+    assert int((mp.trees[0]["flags"] & 1).sum()) > 32  # deep trees
+    assert mp.predict(dp).tobytes() == mr.predict(dr).tobytes()
+
+
+def test_port_threads_do_not_change_results(port):
+    """The port's feature-parallel loops give the same trees on one thread and on all."""
+    x = seeded_matrix(4244, 40_000, 24, 0.05, 3)
+    rng = np.random.default_rng(4245)
+    y = np.nan_to_num(x[:, 0]) * np.nan_to_num(x[:, 1]) + rng.normal(0.0, 0.1, len(x))
+    w = rng.uniform(0.5, 1.5, len(x))
+    ds = port.quantize_dense(x, 255)
+    kw = dict(n_estimators=2, learning_rate=0.1, max_depth=7, min_samples_leaf=5)
+    out = []
+    for threads in (1, 0):
+        port.set_threads(threads)
+        for mode in (oracle.HIST_FP64, oracle.HIST_FIXED):
+            m = port.train_regressor(ds, y, w, hist_mode=mode, **kw)
+            out.append(b"".join(t.tobytes() for t in m.trees) + m.predict(ds).tobytes())
+    port.set_threads(0)
+    assert out[0] == out[2] and out[1] == out[3]
+
+
 def test_histograms_and_transform_match_reference(port, reference):
     x = seeded_matrix(77, 3000, 7, 0.1, 3)
     dp, dr = port.quantize_dense(x, 255), reference.quantize_dense(x, 255)

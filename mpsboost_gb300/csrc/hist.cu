@@ -434,6 +434,307 @@ size_t hist_smem_bytes() {
          (TMA ? size_t(THREADS / 32) * NSTAGE * 8 : 0);
 }
 
+// ---- Register-direct variant (fixed-point modes) ---------------------------------------
+//
+// Measured on GB300 (ncu, 4M x 128): the staged kernels keep the L1 data pipe (one
+// wavefront per clock per SM, shared by shared-memory reductions and global-load data)
+// 75-85 % busy, spending per gathered 32-byte row block 5 wavefronts on reductions, about 1
+// on the staged bins and values and about 2 on the two 16-byte cp.async copies; and each
+// work item's flush (3 x 8192 single-word red.global, each warp instruction touching 32
+// lines) made small items expensive. This variant loads each row's block with one
+// 256-bit load into registers, reduces straight from registers, and flushes through TMA
+// bulk reductions.
+
+struct Bins32 {
+  uint32_t w[8];
+};
+// One 32-byte load (a row's feature block) into registers, without L1 allocation.
+__device__ __forceinline__ Bins32 ld_nc_na_v8(const void* p) {
+  Bins32 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+               : "=r"(v.w[0]), "=r"(v.w[1]), "=r"(v.w[2]), "=r"(v.w[3]), "=r"(v.w[4]), "=r"(v.w[5]),
+                 "=r"(v.w[6]), "=r"(v.w[7])
+               : "l"(p));
+  return v;
+}
+
+// Flush through TMA bulk reductions, for kernels with kFlushBytes of free shared memory at
+// `staging`. The CTA histogram is bin-major ([bin][feature], so that the reductions of a
+// warp hit 32 banks) and the node's slot feature-major ([feature][bin] {count, g, h}).
+// Each of kFlushWarps warps takes tiles of 32 features x 8 bins: lane f reads its
+// feature's 8 cells (conflict-free), writes their 24 words into its row of the warp's
+// staging tile in the slot's order, and hands the row to one 192-byte
+// `cp.reduce.async.bulk ... .add.u64`, which L2 applies a sector at a time instead of as
+// 24 single-word atomics. All-zero rows are skipped. Every thread of the CTA calls it.
+constexpr int kFlushWarps = 8;
+constexpr int kFlushBins = 8;
+constexpr int kFlushRowWords = kFlushBins * 3 + 2;  // a feature's 24 words, padded to 16 bytes
+constexpr size_t kFlushBytes = size_t(kFlushWarps) * kBlockFeatures * kFlushRowWords * 8;
+
+__device__ __forceinline__ void bulk_reduce_add_u64(void* gdst, uint32_t ssrc, uint32_t bytes) {
+  asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.u64 [%0], [%1], %2;\n" ::"l"(gdst),
+               "r"(ssrc), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// The shared source of this thread's bulk operations may be written again.
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+// This thread's bulk operations are complete (their global writes performed).
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
+template <int MODE, int THREADS>
+__device__ __forceinline__ void flush_cta_histogram_bulk(const TrainerDev& a, const BuildEntry& e, uint32_t fb,
+                                                         const unsigned char* hist_smem,
+                                                         unsigned long long* staging, long long q_unit_h,
+                                                         uint32_t row_count) {
+  static_assert(THREADS / 32 > kFlushWarps, "flush warps and a spare warp");
+  constexpr int CELLS = kSlots * kBlockFeatures;
+  const int tid = threadIdx.x;
+  const uint32_t lane = uint32_t(tid & 31);
+  const int warp = tid >> 5;
+  const uint32_t width = min(uint32_t(kBlockFeatures), a.features - fb * kBlockFeatures);
+  if (warp < kFlushWarps) {
+    unsigned long long* dst_base =
+        a.hist + (size_t(e.slot) * a.features + size_t(fb) * kBlockFeatures) * kSlots * 3;
+    unsigned long long* row = staging + (size_t(warp) * kBlockFeatures + lane) * kFlushRowWords;
+    const uint32_t row_addr = static_cast<uint32_t>(__cvta_generic_to_shared(row));
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(hist_smem);
+    for (uint32_t grp = uint32_t(warp); grp < kSlots / kFlushBins; grp += kFlushWarps) {
+      const uint32_t b0 = grp * kFlushBins;
+      bulk_wait_read();  // the row's previous bulk reduction has read it
+      unsigned long long any = 0;
+#pragma unroll
+      for (uint32_t j = 0; j < kFlushBins; ++j) {
+        const uint32_t idx = (b0 + j) * kBlockFeatures + lane;
+        unsigned long long c, g, h;
+        if constexpr (MODE == kModeFixed) {
+          c = w[idx];
+          g = (unsigned long long)((long long)int32_t(w[2 * CELLS + idx]) * 65536 + (long long)w[CELLS + idx]);
+          h = (unsigned long long)((long long)w[4 * CELLS + idx] * 65536 + (long long)w[3 * CELLS + idx]);
+        } else if constexpr (MODE == kModeFixedG) {
+          c = 0;  // the gradient-only root's count and hessian words are restored afterwards
+          g = (unsigned long long)((long long)int32_t(w[CELLS + idx]) * 65536 + (long long)w[idx]);
+          h = 0;
+        } else {
+          c = w[idx];
+          g = (unsigned long long)((long long)int32_t(w[2 * CELLS + idx]) * 65536 + (long long)w[CELLS + idx]);
+          h = (unsigned long long)((long long)c * q_unit_h);
+        }
+        row[3 * j + 0] = c;
+        row[3 * j + 1] = g;
+        row[3 * j + 2] = h;
+        any |= c | g | h;
+      }
+      if (lane < width && any != 0ull) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the row's stores before the bulk read
+        bulk_reduce_add_u64(dst_base + (size_t(lane) * kSlots + b0) * 3, row_addr, kFlushBins * 3 * 8);
+        bulk_commit();
+      }
+    }
+    bulk_wait_read();  // the staging rows are free for the next item
+  }
+  if (tid == 0) {
+    atomicAdd(&a.ctl->cells, (unsigned long long)row_count * width);
+    if (fb == 0) atomicAdd(&a.ctl->rows_built, (unsigned long long)row_count);
+  }
+}
+
+// A work item's description, prepared one item ahead by one warp.
+struct ItemDesc {
+  uint32_t item, limit, fb, row_begin, row_count;
+  int kg, kh;
+  BuildEntry e;
+};
+
+// Takes the next work item from the device counter and describes it (one warp; lane 0
+// writes *out). The build entry holding the item's row chunk is the last one whose chunk
+// prefix is <= the chunk, found by a 32-way search of the prefix table.
+__device__ __forceinline__ void fetch_item_warp(const TrainerDev& a, uint32_t lane, ItemDesc* out) {
+  uint32_t item = 0;
+  if (lane == 0) item = a.item_begin + atomicAdd(&a.ctl->hist_counter, 1u);
+  item = __shfl_sync(0xffffffffu, item, 0);
+  const uint32_t limit = a.item_end ? a.item_end : a.ctl->hist_items;
+  ItemDesc d{};
+  d.item = item;
+  d.limit = limit;
+  if (item < limit) {
+    const uint32_t chunk = item / a.nfb;
+    uint32_t lo = 0, hi = a.ctl->n_build;  // build_prefix[lo] <= chunk < build_prefix[hi]
+    while (hi - lo > 1) {
+      const uint32_t step = (hi - lo + 31) / 32;
+      const uint32_t pos = lo + lane * step;
+      const bool ok = pos < hi && a.build_prefix[pos] <= chunk;  // true on lane 0
+      const uint32_t last = 31u - uint32_t(__clz(__ballot_sync(0xffffffffu, ok)));
+      lo += last * step;
+      hi = min(hi, lo + step);
+    }
+    d.e = a.build[lo];
+    const uint32_t item_rows = a.item_rows ? a.item_rows : a.ctl->item_rows;
+    d.fb = item % a.nfb;
+    d.row_begin = (chunk - a.build_prefix[lo]) * item_rows;
+    d.row_count = d.row_begin < d.e.seg_cnt ? min(item_rows, d.e.seg_cnt - d.row_begin) : 0u;
+    d.kg = a.trees[d.e.tree].kg;
+    d.kh = a.trees[d.e.tree].kh;
+  }
+  if (lane == 0) *out = d;
+}
+
+// The kernel. A warp takes its rows 32 at a time: lane l owns row l of the group, loads the
+// row's whole 32-byte feature block with one 256-bit load and the row's g/h, which it
+// quantizes once. In reduction round i (0..31) lane l updates feature i ^ l: for each i
+// the 32 lanes touch 32 different features, hence 32 different banks. The row's 32 bytes
+// are permuted once (words by l >> 2, bytes within a word by l & 3) so that round i reads
+// the fixed byte i. Row ids are loaded three groups ahead, bins and g/h two ahead; the
+// warps meet only at work-item boundaries (zero, flush), while warp kFlushWarps fetches the
+// next item's description during the flush.
+template <int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDev a) {
+  static_assert(MODE == kModeFixed || MODE == kModeFixedCG || MODE == kModeFixedG, "fixed-point modes");
+  static_assert(THREADS / 32 > kFlushWarps, "a warp besides the flush warps fetches the next item");
+  constexpr int WARPS = THREADS / 32;
+  constexpr int CELLS = kSlots * kBlockFeatures;
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char* hist_smem = smem;
+  __shared__ ItemDesc s_desc;
+
+  const int tid = threadIdx.x;
+  const uint32_t lane = uint32_t(tid & 31);
+  const int warp = tid >> 5;
+  const uint32_t n = a.n_rows;
+  const uint32_t hist_base = static_cast<uint32_t>(__cvta_generic_to_shared(hist_smem));
+  const uint32_t lw = lane >> 2;
+  const uint32_t lb = lane & 3u;
+  const uint32_t byte_sel = (0u ^ lb) | ((1u ^ lb) << 4) | ((2u ^ lb) << 8) | ((3u ^ lb) << 12);
+
+  if (warp == kFlushWarps) fetch_item_warp(a, lane, &s_desc);
+  __syncthreads();
+  for (;;) {
+    const ItemDesc d = s_desc;
+    if (d.item >= d.limit) break;
+    const uint32_t fb = d.fb;
+    const BuildEntry e = d.e;
+    const uint32_t row_count = d.row_count;
+    const size_t seg = (size_t(e.tree) * 2 + e.parity) * a.seg_stride + e.seg_off + d.row_begin;
+    const uint32_t* rows = a.rows + seg;
+    const float2* gh_seg = a.gh_ordered ? a.gh + seg : nullptr;
+    const float2* gh_row = a.gh_ordered ? nullptr : a.gh + size_t(e.tree) * n;
+    const uint8_t* bins = a.bins + size_t(fb) * a.bins_block_stride;
+    const uint64_t row_stride = a.bins_row_stride;
+    const int kg = d.kg;
+    const int kh = d.kh;
+    const long long q_unit_h = MODE == kModeFixedCG ? quantize_f32(1.0f, kh) : 0ll;
+    {
+      uint4* z = reinterpret_cast<uint4*>(hist_smem);
+      const int words = int(HistSmem<MODE>::kBytes / 16);
+      for (int i = tid; i < words; i += THREADS) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();  // also: every thread holds this item's description
+
+    const uint32_t ngroups = (row_count + 31u) / 32u;
+    const uint32_t my = uint32_t(warp) < ngroups ? (ngroups - uint32_t(warp) + WARPS - 1) / WARPS : 0u;
+    auto pos_of = [&](uint32_t k) -> uint32_t { return (uint32_t(warp) + k * WARPS) * 32u + lane; };
+    auto row_at = [&](uint32_t k) -> uint32_t {
+      const uint32_t pos = pos_of(k);
+      if (k >= my || pos >= row_count) return 0u;
+      const uint32_t r = __ldg(rows + pos);
+      return r < n ? r : 0u;  // row ids are < n by construction
+    };
+    auto bins_at = [&](uint32_t k, uint32_t r) -> Bins32 {
+      if (k >= my) return Bins32{};
+      return ld_nc_na_v8(bins + size_t(r) * row_stride);
+    };
+    auto gh_at = [&](uint32_t k, uint32_t r) -> float2 {
+      const uint32_t pos = pos_of(k);
+      if (k >= my || pos >= row_count) return make_float2(0.f, 0.f);
+      return gh_seg ? __ldg(gh_seg + pos) : __ldg(gh_row + r);
+    };
+    const uint32_t r0 = row_at(0), r1 = row_at(1);
+    uint32_t r2 = row_at(2);
+    Bins32 b0 = bins_at(0, r0), b1 = bins_at(1, r1);
+    float2 g0 = gh_at(0, r0), g1 = gh_at(1, r1);
+    for (uint32_t k = 0; k < my; ++k) {
+      const uint32_t r3 = row_at(k + 3);
+      const Bins32 b2 = bins_at(k + 2, r2);
+      const float2 g2 = gh_at(k + 2, r2);
+      if (pos_of(k) < row_count) {
+        // Limbs of the row's quantized values (|q| <= 2^30): unsigned low 16 bits and the
+        // signed high part.
+        uint32_t glo, ghi, hlo = 0, hhi = 0;
+        {
+          const long long qg = quantize_f32(g0.x, kg);
+          glo = uint32_t(qg) & 0xFFFFu;
+          ghi = uint32_t(int32_t(qg >> 16));
+          if constexpr (MODE == kModeFixed) {
+            const long long qh = quantize_f32(g0.y, kh);
+            hlo = uint32_t(qh) & 0xFFFFu;
+            hhi = uint32_t(qh >> 16);
+          }
+        }
+        // w[k] = word k ^ lw of the row's block with its bytes permuted by lb: byte i of w
+        // is byte i ^ lane of the block (feature i ^ lane).
+        uint32_t w[8];
+#pragma unroll
+        for (uint32_t k8 = 0; k8 < 8; ++k8) w[k8] = b0.w[k8];
+#pragma unroll
+        for (uint32_t bit = 1; bit < 8; bit <<= 1) {
+          const bool swap = (lw & bit) != 0;  // per lane: selects, no divergence
+#pragma unroll
+          for (uint32_t k8 = 0; k8 < 8; ++k8)
+            if ((k8 & bit) == 0) {
+              const uint32_t x = w[k8], y = w[k8 | bit];
+              w[k8] = swap ? y : x;
+              w[k8 | bit] = swap ? x : y;
+            }
+        }
+#pragma unroll
+        for (uint32_t k8 = 0; k8 < 8; ++k8) w[k8] = __byte_perm(w[k8], 0u, byte_sel);
+#pragma unroll
+        for (uint32_t i = 0; i < 32; ++i) {
+          const uint32_t bin = (w[i >> 2] >> (8u * (i & 3u))) & 0xFFu;
+          const uint32_t addr = hist_base + (lane ^ i) * 4u + bin * (kBlockFeatures * 4u);
+          if constexpr (MODE == kModeFixed) {
+            red_shared_u32<0>(addr, 1u);
+            red_shared_u32<1u * CELLS * 4u>(addr, glo);
+            red_shared_u32<2u * CELLS * 4u>(addr, ghi);
+            red_shared_u32<3u * CELLS * 4u>(addr, hlo);
+            red_shared_u32<4u * CELLS * 4u>(addr, hhi);
+          } else if constexpr (MODE == kModeFixedG) {
+            red_shared_u32<0>(addr, glo);
+            red_shared_u32<1u * CELLS * 4u>(addr, ghi);
+          } else {
+            red_shared_u32<0>(addr, 1u);
+            red_shared_u32<1u * CELLS * 4u>(addr, glo);
+            red_shared_u32<2u * CELLS * 4u>(addr, ghi);
+          }
+        }
+      }
+      b0 = b1;
+      g0 = g1;
+      b1 = b2;
+      g1 = g2;
+      r2 = r3;
+    }
+    __syncthreads();
+    // The next item's description is fetched while the flush warps work.
+    if (warp == kFlushWarps) fetch_item_warp(a, lane, &s_desc);
+    flush_cta_histogram_bulk<MODE, THREADS>(
+        a, e, fb, hist_smem, reinterpret_cast<unsigned long long*>(hist_smem + HistSmem<MODE>::kBytes),
+        q_unit_h, row_count);
+    __syncthreads();
+  }
+  bulk_wait_all();  // this thread's bulk reductions have reached the slots
+}
+
+template <int MODE, int THREADS>
+cudaError_t launch_direct(const TrainerDev& a, int grid, cudaStream_t stream) {
+  const size_t smem = HistSmem<MODE>::kBytes + kFlushBytes;
+  static std::atomic<unsigned long long> configured{0};  // one bit per device
+  const cudaError_t err = opt_in_dynamic_smem(configured, hist_build_direct_kernel<MODE, THREADS>, smem);
+  if (err != cudaSuccess) return err;
+  hist_build_direct_kernel<MODE, THREADS><<<grid, THREADS, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
 template <int MODE, int THREADS, int NSTAGE, bool TMA = false>
 cudaError_t launch_variant(const TrainerDev& a, int grid, cudaStream_t stream,
                            const CUtensorMap* tmap = nullptr) {
@@ -451,6 +752,19 @@ cudaError_t launch_variant(const TrainerDev& a, int grid, cudaStream_t stream,
 
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,
                               cudaStream_t stream) {
+  const bool row_major_tma = cfg.bins_tmap && a.mode == kModeFixed && a.bins_block_stride == kBlockFeatures &&
+                             a.bins_row_stride == uint64_t(a.nfb) * kBlockFeatures;
+  if (cfg.direct && a.mode != kModeFloat && !row_major_tma) {
+    const int t = a.mode == kModeFixedG ? cfg.root_threads : cfg.threads;
+    if (a.mode == kModeFixedG)
+      return t == 512 ? launch_direct<kModeFixedG, 512>(a, grid, stream)
+                      : launch_direct<kModeFixedG, 768>(a, grid, stream);
+    if (a.mode == kModeFixedCG)
+      return t == 512 ? launch_direct<kModeFixedCG, 512>(a, grid, stream)
+                      : launch_direct<kModeFixedCG, 768>(a, grid, stream);
+    return t == 512 ? launch_direct<kModeFixed, 512>(a, grid, stream)
+                    : launch_direct<kModeFixed, 768>(a, grid, stream);
+  }
   // Shared memory: 160 KB (fixed) / 64 KB (gradient only) / 96 KB (float) histogram +
   // stages x threads x 40 B.
   if (a.mode == kModeFixedG) {

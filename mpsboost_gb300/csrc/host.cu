@@ -1064,6 +1064,8 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.n_fchunks = (F + a.scan_threads / 32 - 1) / (a.scan_threads / 32);
   if (const char* v = std::getenv("MPSB_HIST_THREADS")) t->hcfg.threads = std::atoi(v);
   if (const char* v = std::getenv("MPSB_HIST_STAGES")) t->hcfg.stages = std::atoi(v);
+  t->hcfg.direct = true;
+  if (const char* v = std::getenv("MPSB_HIST_DIRECT")) t->hcfg.direct = std::atoi(v) != 0;
   if (const char* v = std::getenv("MPSB_ROOT_THREADS")) t->hcfg.root_threads = std::atoi(v);
   if (const char* v = std::getenv("MPSB_BLOCKED_LEVELS")) t->blocked_levels = uint32_t(std::atoi(v));
   if (const char* v = std::getenv("MPSB_ITEMS_PER_SM")) a.items_per_sm = uint32_t(std::max(1, std::atoi(v)));

@@ -35,10 +35,15 @@ __device__ __forceinline__ void raise(Control* ctl, uint32_t bits) { atomicOr(&c
 __device__ __forceinline__ uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
 // Rows per histogram work item for a level that builds `rows` rows: about per_sm (default
-// three) items per SM, a multiple of 512, within [4096, kItemRowsMax].
+// three) items per SM, a multiple of 512, within [4096, kItemRowsMax]. Where the
+// kItemRowsMax cap forces more items, their number is raised to the next multiple of the
+// SM count, so that the persistent CTAs end the level together.
 __device__ __forceinline__ uint32_t adaptive_item_rows(uint64_t rows, uint32_t nfb, uint32_t sms,
                                                       uint32_t per_sm) {
-  const uint64_t target = uint64_t(sms ? sms : 152) * (per_sm ? per_sm : 3);
+  const uint64_t n_sm = sms ? sms : 152;
+  uint64_t target = n_sm * (per_sm ? per_sm : 3);
+  const uint64_t min_items = (rows * nfb + kItemRowsMax - 1) / kItemRowsMax;
+  if (target < min_items) target = (min_items + n_sm - 1) / n_sm * n_sm;
   uint64_t per = (rows * nfb + target - 1) / target;
   per = (per + 511) / 512 * 512;
   if (per < 4096) per = 4096;

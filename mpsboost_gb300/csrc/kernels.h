@@ -131,6 +131,11 @@ struct HistConfig {
   int threads = 768;        // fixed and float builds
   int stages = 2;
   int root_threads = 1024;  // gradient-only root builds (64 KB histogram)
+  // Register-direct fixed-point builds (hist_build_direct_kernel: each lane loads a whole
+  // row's 32-byte feature block, no shared-memory staging; flush by TMA bulk reductions);
+  // threads 512 or 768. The opt-in TMA staging (bins_tmap) takes precedence. The trainer
+  // turns it on; the node-level entries keep the staged kernel.
+  bool direct = false;
   // Tensor map of the row-major bins ({row stride, n_rows} u8, box 32 x 1): row-major
   // fixed-point builds stage gathered rows with TMA gather4 copies (opt-in). Null: cp.async.
   const CUtensorMap* bins_tmap = nullptr;

@@ -354,6 +354,33 @@ def test_tma_staging_equals_cp_async(backend, monkeypatch, threads):
     assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
 
 
+@pytest.mark.parametrize("threads", ["768", "512"])
+@pytest.mark.parametrize("weighted", [True, False])
+def test_direct_loads_equal_staged_builds(backend, port, monkeypatch, threads, weighted):
+    """Register-direct histogram builds (the trainer's default: each lane loads its row's
+    32 bin bytes with one 256-bit load, no shared-memory staging, flush by TMA bulk
+    reductions) give the staged kernel's trees bit for bit (MPSB_HIST_DIRECT=0), and the
+    replica's. Weighted squared error builds five limbs and, from round 2, gradient-only
+    roots; unweighted builds count and gradient limbs (unit hessian). Depth 9 with 70
+    features (a partial feature block), 40,000 rows (dense and sparse nodes, partial row
+    groups) and missing values."""
+    x, y, w = _data(47, 40000, 70, 0.05, 3)
+    w = w if weighted else None
+    params = dict(n_estimators=3, learning_rate=0.2, max_depth=9, min_samples_leaf=1)
+    monkeypatch.setenv("MPSB_HIST_THREADS", threads)
+    monkeypatch.setenv("MPSB_ROOT_THREADS", threads)
+    monkeypatch.setenv("MPSB_HIST_DIRECT", "1")
+    binned = mb.quantize_dense(x, 255)
+    a = mb.train_regressor(backend, binned, y, w, **params)
+    monkeypatch.setenv("MPSB_HIST_DIRECT", "0")
+    b = mb.train_regressor(backend, binned, y, w, **params)
+    assert [t.tobytes() for t in a.trees] == [t.tobytes() for t in b.trees]
+    assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
+    ds = port.quantize_dense(x, 255)
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FIXED, **params)
+    assert [t.tobytes() for t in a.trees] == [t.tobytes() for t in want.trees]
+
+
 def test_logistic_against_replica(backend, port):
     x, y, w = _data(41, 6000, 8, 0.1, 2, "binary_logistic")
     params = dict(n_estimators=3, learning_rate=0.2, max_depth=5, min_samples_leaf=4,

@@ -206,6 +206,10 @@ const char* mpsb_cuda_last_error(void);
 int mpsb_cuda_abi_version(void);
 
 /* ---- backend ------------------------------------------------------------------- */
+/* Number of GPUs this library can train on (compute capability 10.3); 0 where there is no
+   CUDA driver or device. Creates no context. The availability probe of the device policy
+   (device_policy.py:64-99 asks diagnostics.is_available for MPS). */
+int mpsb_cuda_device_count(int* out);
 int mpsb_cuda_backend_create(int device, mpsb_cuda_backend** out);
 void mpsb_cuda_backend_destroy(mpsb_cuda_backend* backend);
 int mpsb_cuda_backend_info(const mpsb_cuda_backend* backend, mpsb_cuda_info* out);

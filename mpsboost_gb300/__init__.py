@@ -3,8 +3,8 @@
 gradient/hessian -> histogram build (+ sibling subtraction) -> split-gain scan -> row
 partition, behind the reference's backend contract (include/mpsboost/backend.hpp) and
 exposed through the C ABI in ``include/mpsb_cuda.h``. See ``backend`` for the Python
-mirror of the reference's native interface and ``estimators`` for the sklearn-style
-estimators with ``device="cuda"``.
+mirror of the reference's native interface, ``estimators`` for the sklearn-style
+estimators with ``device="cuda"`` and ``device_policy`` for the device decision.
 """
 
 from ._lib import BackendError, DataError, TrainingError, UnsupportedError
@@ -26,7 +26,25 @@ from .backend import (
     train_softmax,
 )
 
+from .device_policy import DeviceDecision, choose_device, cuda_available, cuda_device_count
+from .estimators import (
+    GradientBoostingClassifier,
+    GradientBoostingRegressor,
+    MPSBoostClassifier,
+    MPSBoostRegressor,
+    RandomForestRegressor,
+)
+
 __all__ = [
+    "DeviceDecision",
+    "GradientBoostingClassifier",
+    "GradientBoostingRegressor",
+    "MPSBoostClassifier",
+    "MPSBoostRegressor",
+    "RandomForestRegressor",
+    "choose_device",
+    "cuda_available",
+    "cuda_device_count",
     "BackendError",
     "BinnedDataset",
     "CudaBackend",

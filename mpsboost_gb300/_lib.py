@@ -138,6 +138,7 @@ _U32, _U64, _I32, _F64 = C.c_uint32, C.c_uint64, C.c_int, C.c_double
 SIGNATURES = {
     "mpsb_cuda_last_error": (C.c_char_p, []),
     "mpsb_cuda_abi_version": (_I32, []),
+    "mpsb_cuda_device_count": (_I32, [C.POINTER(_I32)]),
     "mpsb_cuda_backend_create": (_I32, [_I32, C.POINTER(_VP)]),
     "mpsb_cuda_backend_destroy": (None, [_VP]),
     "mpsb_cuda_backend_info": (_I32, [_VP, C.POINTER(Info)]),

@@ -381,6 +381,28 @@ extern "C" {
 const char* mpsb_cuda_last_error(void) { return g_error.c_str(); }
 int mpsb_cuda_abi_version(void) { return MPSB_CUDA_ABI_VERSION; }
 
+int mpsb_cuda_device_count(int* out) {
+  return guard([&] {
+    if (out == nullptr) throw TrainingError("output pointer must not be null");
+    *out = 0;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {  // no driver or no device
+      cudaGetLastError();
+      return;
+    }
+    int usable = 0;
+    for (int d = 0; d < count; ++d) {
+      int major = 0, minor = 0;
+      if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, d) == cudaSuccess &&
+          cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, d) == cudaSuccess &&
+          major == 10 && minor == 3)
+        ++usable;
+    }
+    cudaGetLastError();
+    *out = usable;
+  });
+}
+
 int mpsb_cuda_backend_create(int device, mpsb_cuda_backend** out) {
   return guard([&] {
     if (out == nullptr) throw TrainingError("output pointer must not be null");

@@ -48,7 +48,7 @@ def test_regressor_equals_direct_fit_and_replica(backend, port):
 def test_poisson_predictions_are_exponentiated(backend):
     x, y, _ = _data(62)
     y = np.floor(np.exp(np.clip(y, -2, 2)))
-    model = mb.GradientBoostingRegressor(n_estimators=3, max_depth=4, loss="poisson").fit(x, y)
+    model = mb.GradientBoostingRegressor(n_estimators=3, max_depth=4, max_bins=255, loss="poisson").fit(x, y)
     raw = model.model_.predict(x).astype(np.float64)
     assert np.allclose(model.predict(x), np.exp(raw), rtol=1e-6)
 

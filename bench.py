@@ -173,6 +173,8 @@ def cpu_baseline(xf, y, w, sample_rows: int, trees: int):
     per_tree_full = dt / trees * (ROWS / sample_rows)
     return {
         "value": 1.0 / per_tree_full, "unit": "trees/s", "cores": 1, "kind": "port",
+        "note": "the reference's own trainer, compiled from its sources on x86 host cores, ran "
+                "2.1x slower than this port on 200,000 x 128 rows, depth 8, with identical trees",
         "sample": f"{trees} tree(s) on the first {sample_rows:,} rows ({dt:.1f} s training, "
                   f"{tq:.1f} s binning), time per tree scaled by rows to {ROWS:,}",
     }
@@ -289,7 +291,9 @@ def run_ours(args, rank, world):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "trees/s", "rows": args.rows,
                               "steps": args.steps, "warmup": args.warmup,
-                              "gpu_launches": int(st["kernel_launches"]), "only_train": True}), flush=True)
+                              "gpu_launches": int(st["kernel_launches"]), "only_train": True,
+                              "hist_cells": int(st["hist_cells"]), "hist_rows": int(st["hist_rows"])}),
+                  flush=True)
         trainer.close()
         return
 
@@ -440,8 +444,9 @@ def run_secondary(mb, backend):
 
     binary logistic 4M x 256 (10 % missing, depth 10, lr 0.1): trees/s over 8 graph-
     replayed rounds, CUDA events on the backend stream, device-binned data resident.
-    one-vs-rest K = 10, 2M x 64, depth 6: per round from two one-shot fits through the
-    public API (12 and 4 rounds; the difference removes setup), 10 trees per round.
+    one-vs-rest K = 10, 2M x 64, depth 6: per round from one-shot fits through the public
+    API (medians of three fits of 20 and of 4 rounds; the difference removes setup), 10
+    trees per round.
     random forest 1M x 100, 256 trees, depth 12, sqrt features, Poisson(1) rows: one
     host-timed fit of the whole forest through the public API (sample expansion, upload,
     training, model readback) after a 16-tree warm-up."""
@@ -469,16 +474,19 @@ def run_secondary(mb, backend):
     del x
     params = dict(max_depth=6, learning_rate=0.1, min_samples_leaf=20, min_child_weight=1.0, reg_lambda=1.0)
     mb.train_ovr(backend, dset, labels, 10, n_estimators=2, **params)  # warm
-    times = {}
-    for rounds in (4, 12):
-        backend.synchronize()
-        t0 = time.perf_counter()
-        mb.train_ovr(backend, dset, labels, 10, n_estimators=rounds, **params)
-        times[rounds] = time.perf_counter() - t0
+    times = {4: [], 20: []}
+    for _ in range(3):
+        for rounds in (4, 20):
+            backend.synchronize()
+            t0 = time.perf_counter()
+            mb.train_ovr(backend, dset, labels, 10, n_estimators=rounds, **params)
+            times[rounds].append(time.perf_counter() - t0)
     dset.close()
-    per_round = (times[12] - times[4]) / 8
+    t4, t20 = statistics.median(times[4]), statistics.median(times[20])
+    per_round = (t20 - t4) / 16
     out["ovr_k10_2Mx64_d6"] = {"value": 10 / per_round, "unit": "trees/s", "ms_per_round": per_round * 1e3,
-                               "fit_seconds_12_rounds": times[12], "timing": "host, (t(12) - t(4)) / 8"}
+                               "fit_seconds_20_rounds": t20,
+                               "timing": "host, (median t(20) - median t(4)) / 16 over three fits each"}
     del labels
 
     x, y, counts, subsets = make_forest_data()

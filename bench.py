@@ -38,11 +38,11 @@ SEED = 20260719 + 2
 PARAMS = dict(max_depth=DEPTH, learning_rate=LR, min_samples_leaf=20, min_child_weight=1.0,
               reg_lambda=1.0, max_bins=BINS)
 METRIC = "trees/s @10Mx128x255bins d8 (fixed-point batched)"
-# DRAM bytes per histogram launch on this workload: one ncu capture of
-# dram__bytes_read.sum + dram__bytes_write.sum over the 24 histogram launches of three
-# steady-state rounds (610.6 MB read + 6.9 MB written per launch on average), recorded
-# with its command in the profile named below.
-HIST_TRAFFIC_BYTES_PER_LAUNCH = 617.5e6
+# DRAM traffic of the histogram launches per algorithmic byte: one ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum over the eight histogram launches of a
+# steady-state round of this workload at 4M rows (2,219.7 MB against 1,958.3 MB), recorded
+# with its command in the profile named below; scaled by the live algorithmic bytes.
+HIST_TRAFFIC_PER_ALG_BYTE = 1.133
 HIST_TRAFFIC_PROFILE = "profiles/hist_build_dram_traffic_10Mx128_d8.md"
 CONFIG = {
     "workload": "regression 10,000,000 rows x 128 features (64 normal, 32 lognormal, 32 int[0,1000)), "
@@ -366,10 +366,11 @@ def run_ours(args, rank, world):
         "gpu_launches": int(st["kernel_launches"]),
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": HIST_TRAFFIC_BYTES_PER_LAUNCH,
-                     "traffic_unit": "bytes per launch (ncu)", "traffic_source": HIST_TRAFFIC_PROFILE,
+                     "frac": achieved / peak, "traffic": HIST_TRAFFIC_PER_ALG_BYTE * per_launch_bytes,
+                     "traffic_unit": "bytes per launch (ncu ratio at 4M rows x live algorithmic bytes)",
+                     "traffic_source": HIST_TRAFFIC_PROFILE,
                      "peak_kind": peak_kind,
-                     "kernel": "hist_build_kernel<fixed>",
+                     "kernel": "hist_build_direct_kernel (fixed point)",
                      "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
                      "cells_per_s": ts["hist_cells"] / (ts["hist_ms"] / 1e3), "levels": levels},
         "tree_roofline": {"bound": "hbm", "bytes_per_tree": tree_bytes, "ms_per_tree": ms_max / args.steps,

@@ -27,6 +27,8 @@
 //    (the plain path): a u32 count and two FP32 reductions per cell.
 //  * The CTA flushes its non-empty cells into the node's global slot with 64-bit
 //    red.global adds (exact integer adds in fixed mode; FP64 adds in float mode).
+#include <type_traits>
+
 #include "device.cuh"
 #include "kernels.h"
 
@@ -595,7 +597,10 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDe
   constexpr int CELLS = kSlots * kBlockFeatures;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* hist_smem = smem;
-  __shared__ ItemDesc s_desc;
+  // The next item's description lives after the flush staging; with no static shared
+  // memory the histogram starts the CTA's dynamic shared memory (128-byte aligned in
+  // practice, which the reduction address arithmetic exploits; checked below).
+  ItemDesc* s_desc = reinterpret_cast<ItemDesc*>(smem + HistSmem<MODE>::kBytes + kFlushBytes);
 
   const int tid = threadIdx.x;
   const uint32_t lane = uint32_t(tid & 31);
@@ -606,10 +611,14 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDe
   const uint32_t lb = lane & 3u;
   const uint32_t byte_sel = (0u ^ lb) | ((1u ^ lb) << 4) | ((2u ^ lb) << 8) | ((3u ^ lb) << 12);
 
-  if (warp == kFlushWarps) fetch_item_warp(a, lane, &s_desc);
+  if (warp == kFlushWarps) fetch_item_warp(a, lane, s_desc);
   __syncthreads();
+  // With hist_base 128-byte aligned, hist_base + 4 (lane ^ i) = (hist_base + 4 lane) ^ 4 i
+  // (4 lane and 4 i stay below 128), one instruction per reduction round.
+  const bool aligned = (hist_base & 127u) == 0u;  // CTA-uniform
+  const uint32_t lane_base = hist_base + lane * 4u;
   for (;;) {
-    const ItemDesc d = s_desc;
+    const ItemDesc d = *s_desc;
     if (d.item >= d.limit) break;
     const uint32_t fb = d.fb;
     const BuildEntry e = d.e;
@@ -688,25 +697,31 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDe
         }
 #pragma unroll
         for (uint32_t k8 = 0; k8 < 8; ++k8) w[k8] = __byte_perm(w[k8], 0u, byte_sel);
+        auto reduce_row = [&](auto aligned_tag) {
+          constexpr bool ALIGNED = decltype(aligned_tag)::value;
 #pragma unroll
-        for (uint32_t i = 0; i < 32; ++i) {
-          const uint32_t bin = (w[i >> 2] >> (8u * (i & 3u))) & 0xFFu;
-          const uint32_t addr = hist_base + (lane ^ i) * 4u + bin * (kBlockFeatures * 4u);
-          if constexpr (MODE == kModeFixed) {
-            red_shared_u32<0>(addr, 1u);
-            red_shared_u32<1u * CELLS * 4u>(addr, glo);
-            red_shared_u32<2u * CELLS * 4u>(addr, ghi);
-            red_shared_u32<3u * CELLS * 4u>(addr, hlo);
-            red_shared_u32<4u * CELLS * 4u>(addr, hhi);
-          } else if constexpr (MODE == kModeFixedG) {
-            red_shared_u32<0>(addr, glo);
-            red_shared_u32<1u * CELLS * 4u>(addr, ghi);
-          } else {
-            red_shared_u32<0>(addr, 1u);
-            red_shared_u32<1u * CELLS * 4u>(addr, glo);
-            red_shared_u32<2u * CELLS * 4u>(addr, ghi);
+          for (uint32_t i = 0; i < 32; ++i) {
+            const uint32_t bin = (w[i >> 2] >> (8u * (i & 3u))) & 0xFFu;
+            const uint32_t cell = ALIGNED ? (lane_base ^ (i << 2)) : hist_base + ((lane ^ i) << 2);
+            const uint32_t addr = cell + (bin << 7);  // bin * kBlockFeatures * 4 bytes
+            if constexpr (MODE == kModeFixed) {
+              red_shared_u32<0>(addr, 1u);
+              red_shared_u32<1u * CELLS * 4u>(addr, glo);
+              red_shared_u32<2u * CELLS * 4u>(addr, ghi);
+              red_shared_u32<3u * CELLS * 4u>(addr, hlo);
+              red_shared_u32<4u * CELLS * 4u>(addr, hhi);
+            } else if constexpr (MODE == kModeFixedG) {
+              red_shared_u32<0>(addr, glo);
+              red_shared_u32<1u * CELLS * 4u>(addr, ghi);
+            } else {
+              red_shared_u32<0>(addr, 1u);
+              red_shared_u32<1u * CELLS * 4u>(addr, glo);
+              red_shared_u32<2u * CELLS * 4u>(addr, ghi);
+            }
           }
-        }
+        };
+        if (aligned) reduce_row(std::true_type{});
+        else reduce_row(std::false_type{});
       }
       b0 = b1;
       g0 = g1;
@@ -716,7 +731,7 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDe
     }
     __syncthreads();
     // The next item's description is fetched while the flush warps work.
-    if (warp == kFlushWarps) fetch_item_warp(a, lane, &s_desc);
+    if (warp == kFlushWarps) fetch_item_warp(a, lane, s_desc);
     flush_cta_histogram_bulk<MODE, THREADS>(
         a, e, fb, hist_smem, reinterpret_cast<unsigned long long*>(hist_smem + HistSmem<MODE>::kBytes),
         q_unit_h, row_count);
@@ -727,7 +742,8 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDe
 
 template <int MODE, int THREADS>
 cudaError_t launch_direct(const TrainerDev& a, int grid, cudaStream_t stream) {
-  const size_t smem = HistSmem<MODE>::kBytes + kFlushBytes;
+  static_assert(kBlockFeatures * 4 == 128, "a bin row of the CTA histogram is 128 bytes");
+  const size_t smem = HistSmem<MODE>::kBytes + kFlushBytes + (sizeof(ItemDesc) + 15) / 16 * 16;
   static std::atomic<unsigned long long> configured{0};  // one bit per device
   const cudaError_t err = opt_in_dynamic_smem(configured, hist_build_direct_kernel<MODE, THREADS>, smem);
   if (err != cudaSuccess) return err;

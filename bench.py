@@ -292,7 +292,8 @@ def run_ours(args, rank, world):
             print(json.dumps({"metric": METRIC, "value": value, "unit": "trees/s", "rows": args.rows,
                               "steps": args.steps, "warmup": args.warmup,
                               "gpu_launches": int(st["kernel_launches"]), "only_train": True,
-                              "hist_cells": int(st["hist_cells"]), "hist_rows": int(st["hist_rows"])}),
+                              "hist_cells": int(st["hist_cells"]), "hist_rows": int(st["hist_rows"]),
+                              "part_rows": int(st["part_rows"])}),
                   flush=True)
         trainer.close()
         return

@@ -33,7 +33,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-ROWS, FEATURES, BINS, DEPTH, LR = 10_000_000, 128, 255, 8, 0.05
+ROWS, FEATURES, BINS, DEPTH, LR, TREES = 10_000_000, 128, 255, 8, 0.05, 200
 SEED = 20260719 + 2
 PARAMS = dict(max_depth=DEPTH, learning_rate=LR, min_samples_leaf=20, min_child_weight=1.0,
               reg_lambda=1.0, max_bins=BINS)
@@ -48,6 +48,7 @@ CONFIG = {
     "workload": "regression 10,000,000 rows x 128 features (64 normal, 32 lognormal, 32 int[0,1000)), "
                 "255 bins, depth 8, lr 0.05, weighted squared error",
     "rows": ROWS, "features": FEATURES, "bins": BINS, "max_depth": DEPTH, "learning_rate": LR,
+    "n_estimators": TREES,
     "hist": "int64 fixed-point, all frontier nodes per launch, one CUDA graph per round",
     "l2": "inputs (1.28 GB binned matrix) exceed the 129 MB L2; no flush between steps",
 }
@@ -344,8 +345,8 @@ def run_ours(args, rank, world):
     # same fit from ordinary (pageable) numpy arrays.
     e2e = e2e_pageable = None
     if rank == 0 or world > 1:
-        e2e = run_e2e(mb, backend, binned, y, w, args.steps, pinned=True)
-        e2e_pageable = run_e2e(mb, backend, binned, y, w, args.steps, pinned=False)
+        e2e = run_e2e(mb, backend, binned, y, w, args.e2e_trees, pinned=True)
+        e2e_pageable = run_e2e(mb, backend, binned, y, w, args.e2e_trees, pinned=False)
     trainer.close()
     secondary = run_secondary(mb, backend) if world == 1 and not args.no_secondary else None
 
@@ -437,8 +438,9 @@ def run_e2e(mb, backend, binned, y, w, trees, pinned=True):
     return {"value": trees / dt, "unit": "trees/s", "h2d_bytes_per_step": h2d // trees,
             "d2h_bytes_per_step": d2h // trees, "seconds": dt,
             "host_memory": "page-locked (registered before timing)" if pinned else "pageable numpy arrays",
-            "note": "one fit of K trees: dataset upload (asynchronous, beside the host's label and "
-                    "weight checks), training, tree readback"}
+            "trees": trees,
+            "note": "one fit of the configured model through mpsb_cuda_train_regressor: dataset upload "
+                    "(asynchronous, beside the host's label and weight checks), training, tree readback"}
 
 
 def run_secondary(mb, backend):
@@ -548,6 +550,8 @@ def main():
                     help="trees of the CPU baseline sample (about 10 s of single-core training)")
     ap.add_argument("--ref-rows", type=int, default=500_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-trees", type=int, default=TREES,
+                    help="trees of the end-to-end fit (default: the configuration's 200)")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the bounded logistic / one-vs-rest / forest measurements")
     ap.add_argument("--rows", type=int, default=ROWS,

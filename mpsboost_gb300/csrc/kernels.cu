@@ -1206,8 +1206,15 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
     __syncthreads();
   }
   __syncthreads();
+  // Work items per SM of the next level: a level of few large nodes loses more to each
+  // item's fixed cost (zero, flush) than to load imbalance, a level of many nodes (each
+  // with a partial last chunk) the other way round: one item fewer below 8 nodes here,
+  // one more from 8 (measured on the 10M x 128 workload: 2 best for depths 1-3, 4 for
+  // depths 4-7).
+  const uint32_t base_per_sm = a.items_per_sm ? a.items_per_sm : 3u;
+  const uint32_t level_per_sm = n >= 8 ? base_per_sm + 1 : (base_per_sm > 2 ? base_per_sm - 1 : base_per_sm);
   const uint32_t item_rows =
-      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(built_units) * 256, a.nfb, a.sm_count, a.items_per_sm);
+      a.item_rows ? a.item_rows : adaptive_item_rows(uint64_t(built_units) * 256, a.nfb, a.sm_count, level_per_sm);
 
   // Phase B1: acceptance under max_leaves, accepted prefix, chunk prefixes.
   // Scanned values: 0 accepted, 1 build chunks, 2 partition chunks, 3 leaf segments,

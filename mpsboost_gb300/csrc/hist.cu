@@ -589,8 +589,9 @@ __device__ __forceinline__ void fetch_item_warp(const TrainerDev& a, uint32_t la
 // the fixed byte i. Row ids are loaded three groups ahead, bins and g/h two ahead; the
 // warps meet only at work-item boundaries (zero, flush), while warp kFlushWarps fetches the
 // next item's description during the flush.
-template <int MODE, int THREADS>
+template <int MODE, int THREADS, int PF>
 __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDev a) {
+  static_assert(PF >= 2 && PF <= 4, "bins and pairs 2-4 groups ahead");
   static_assert(MODE == kModeFixed || MODE == kModeFixedCG || MODE == kModeFixedG, "fixed-point modes");
   static_assert(THREADS / 32 > kFlushWarps, "a warp besides the flush warps fetches the next item");
   constexpr int WARPS = THREADS / 32;
@@ -657,14 +658,23 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDe
       if (k >= my || pos >= row_count) return make_float2(0.f, 0.f);
       return gh_seg ? __ldg(gh_seg + pos) : __ldg(gh_row + r);
     };
-    const uint32_t r0 = row_at(0), r1 = row_at(1);
-    uint32_t r2 = row_at(2);
-    Bins32 b0 = bins_at(0, r0), b1 = bins_at(1, r1);
-    float2 g0 = gh_at(0, r0), g1 = gh_at(1, r1);
+    // Ring of the next PF groups' bins and pairs; the row id of group k + PF is loaded
+    // one iteration before its bins.
+    Bins32 bq[PF];
+    float2 gq[PF];
+#pragma unroll
+    for (int j = 0; j < PF; ++j) {
+      const uint32_t r = row_at(uint32_t(j));
+      bq[j] = bins_at(uint32_t(j), r);
+      gq[j] = gh_at(uint32_t(j), r);
+    }
+    uint32_t r_ahead = row_at(PF);
     for (uint32_t k = 0; k < my; ++k) {
-      const uint32_t r3 = row_at(k + 3);
-      const Bins32 b2 = bins_at(k + 2, r2);
-      const float2 g2 = gh_at(k + 2, r2);
+      const uint32_t r_next = row_at(k + PF + 1);
+      const Bins32 b_new = bins_at(k + PF, r_ahead);
+      const float2 g_new = gh_at(k + PF, r_ahead);
+      const Bins32& b0 = bq[0];
+      const float2& g0 = gq[0];
       if (pos_of(k) < row_count) {
         // Limbs of the row's quantized values (|q| <= 2^30): unsigned low 16 bits and the
         // signed high part.
@@ -723,11 +733,14 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDe
         if (aligned) reduce_row(std::true_type{});
         else reduce_row(std::false_type{});
       }
-      b0 = b1;
-      g0 = g1;
-      b1 = b2;
-      g1 = g2;
-      r2 = r3;
+#pragma unroll
+      for (int j = 0; j + 1 < PF; ++j) {
+        bq[j] = bq[j + 1];
+        gq[j] = gq[j + 1];
+      }
+      bq[PF - 1] = b_new;
+      gq[PF - 1] = g_new;
+      r_ahead = r_next;
     }
     __syncthreads();
     // The next item's description is fetched while the flush warps work.
@@ -740,15 +753,24 @@ __global__ void __launch_bounds__(THREADS, 1) hist_build_direct_kernel(TrainerDe
   bulk_wait_all();  // this thread's bulk reductions have reached the slots
 }
 
-template <int MODE, int THREADS>
+template <int MODE, int THREADS, int PF = 2>
 cudaError_t launch_direct(const TrainerDev& a, int grid, cudaStream_t stream) {
   static_assert(kBlockFeatures * 4 == 128, "a bin row of the CTA histogram is 128 bytes");
   const size_t smem = HistSmem<MODE>::kBytes + kFlushBytes + (sizeof(ItemDesc) + 15) / 16 * 16;
   static std::atomic<unsigned long long> configured{0};  // one bit per device
-  const cudaError_t err = opt_in_dynamic_smem(configured, hist_build_direct_kernel<MODE, THREADS>, smem);
+  const cudaError_t err = opt_in_dynamic_smem(configured, hist_build_direct_kernel<MODE, THREADS, PF>, smem);
   if (err != cudaSuccess) return err;
-  hist_build_direct_kernel<MODE, THREADS><<<grid, THREADS, smem, stream>>>(a);
+  hist_build_direct_kernel<MODE, THREADS, PF><<<grid, THREADS, smem, stream>>>(a);
   return cudaGetLastError();
+}
+
+// Register-direct launch for a mode: 768 threads (bins two groups ahead), 640 (three
+// ahead: the deeper ring needs more registers than 768 threads leave) or 512 (two ahead).
+template <int MODE>
+cudaError_t launch_direct_shape(const TrainerDev& a, int threads, int grid, cudaStream_t stream) {
+  if (threads == 512) return launch_direct<MODE, 512>(a, grid, stream);
+  if (threads == 640) return launch_direct<MODE, 640, 3>(a, grid, stream);
+  return launch_direct<MODE, 768>(a, grid, stream);
 }
 
 template <int MODE, int THREADS, int NSTAGE, bool TMA = false>
@@ -772,14 +794,9 @@ cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int gr
                              a.bins_row_stride == uint64_t(a.nfb) * kBlockFeatures;
   if (cfg.direct && a.mode != kModeFloat && !row_major_tma) {
     const int t = a.mode == kModeFixedG ? cfg.root_threads : cfg.threads;
-    if (a.mode == kModeFixedG)
-      return t == 512 ? launch_direct<kModeFixedG, 512>(a, grid, stream)
-                      : launch_direct<kModeFixedG, 768>(a, grid, stream);
-    if (a.mode == kModeFixedCG)
-      return t == 512 ? launch_direct<kModeFixedCG, 512>(a, grid, stream)
-                      : launch_direct<kModeFixedCG, 768>(a, grid, stream);
-    return t == 512 ? launch_direct<kModeFixed, 512>(a, grid, stream)
-                    : launch_direct<kModeFixed, 768>(a, grid, stream);
+    if (a.mode == kModeFixedG) return launch_direct_shape<kModeFixedG>(a, t, grid, stream);
+    if (a.mode == kModeFixedCG) return launch_direct_shape<kModeFixedCG>(a, t, grid, stream);
+    return launch_direct_shape<kModeFixed>(a, t, grid, stream);
   }
   // Shared memory: 160 KB (fixed) / 64 KB (gradient only) / 96 KB (float) histogram +
   // stages x threads x 40 B.

@@ -354,7 +354,7 @@ def test_tma_staging_equals_cp_async(backend, monkeypatch, threads):
     assert a.train_predictions.tobytes() == b.train_predictions.tobytes()
 
 
-@pytest.mark.parametrize("threads", ["768", "512"])
+@pytest.mark.parametrize("threads", ["768", "640", "512"])
 @pytest.mark.parametrize("weighted", [True, False])
 def test_direct_loads_equal_staged_builds(backend, port, monkeypatch, threads, weighted):
     """Register-direct histogram builds (the trainer's default: each lane loads its row's

@@ -212,7 +212,9 @@ def quantize_dense(matrix, max_bins: int = 256, n_threads: int = 0) -> BinnedDat
 # Backend
 # --------------------------------------------------------------------------------------
 class DeviceDataset:
-    """A binned dataset resident in HBM (column-blocked u8, missing at slot 255)."""
+    """A binned dataset resident in HBM: column-blocked u8 bins with missing rows at slot
+    255, or u16 bins for a wide dataset (a feature with more than 256 bins, or 256 bins and
+    missing values) with missing rows at its last histogram slot."""
 
     @classmethod
     def _adopt(cls, backend: "CudaBackend", handle, rows: int, features: int) -> "DeviceDataset":

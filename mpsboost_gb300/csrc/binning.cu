@@ -364,22 +364,32 @@ mpsb_cuda_dataset* finish_dataset(mpsb_cuda_backend* b, const uint8_t* bins_fm, 
   d->nfb = (features + kBlockFeatures - 1) / kBlockFeatures;
   d->h_bin_count = std::move(bin_count);
   d->h_has_missing.assign(features, 0);
-  for (uint32_t f = 0; f < features; ++f) {
-    d->h_has_missing[f] = missing_count[f] ? 1 : 0;
-    if (d->h_has_missing[f] && d->h_bin_count[f] > 255)
-      throw UnsupportedError("a feature with missing values may have at most 255 bins on the CUDA backend");
-  }
+  for (uint32_t f = 0; f < features; ++f) d->h_has_missing[f] = missing_count[f] ? 1 : 0;
+  // 256 bins and missing values in one feature: the wide layout's missing slot.
+  d->slots = dataset_slots(d->h_bin_count.data(), d->h_has_missing.data(), features);
   d->missing_count = std::move(missing_count);
   d->bin_count.alloc(features * sizeof(uint32_t));
   d->has_missing.alloc(features);
   CK(cudaMemcpyAsync(d->bin_count.p, d->h_bin_count.data(), features * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d->has_missing.p, d->h_has_missing.data(), features, cudaMemcpyHostToDevice, s));
-  d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
-  d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
-  d->bins_fm.alloc(size_t(features) * rows);
-  CK(launch_pack_bins(bins_fm, 1, missing, d->bin_count.as<uint32_t>(), rows, features, d->nfb,
-                      d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(), d->bins_fm.as<uint8_t>(),
-                      b->error.as<uint32_t>(), s));
+  if (d->slots != uint32_t(kSlots)) {
+    d->bins16.alloc(size_t(d->nfb) * rows * kBlockFeatures * sizeof(uint16_t));
+    d->bins16_fm.alloc(size_t(features) * rows * sizeof(uint16_t));
+    for (uint32_t fb = 0; fb < d->nfb; ++fb) {
+      const size_t first = size_t(fb) * kBlockFeatures * rows;
+      CK(launch_pack_bins16_block(bins_fm + first, 1, missing ? missing + first : nullptr,
+                                  d->bin_count.as<uint32_t>(), rows,
+                                  features, fb, d->slots, d->bins16.as<uint16_t>(),
+                                  d->bins16_fm.as<uint16_t>(), b->error.as<uint32_t>(), s));
+    }
+  } else {
+    d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+    d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+    d->bins_fm.alloc(size_t(features) * rows);
+    CK(launch_pack_bins(bins_fm, 1, missing, d->bin_count.as<uint32_t>(), rows, features, d->nfb,
+                        d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(), d->bins_fm.as<uint8_t>(),
+                        b->error.as<uint32_t>(), s));
+  }
   if (b->take_error()) throw DataError("Binned value exceeds the feature histogram range");
   attach_bins_tmap(d.get());
   return d.release();
@@ -536,6 +546,24 @@ int mpsb_cuda_dataset_export(const mpsb_cuda_dataset* d, uint8_t* bins, uint8_t*
     d->backend->activate();
     cudaStream_t s = d->backend->stream;
     const size_t cells = size_t(d->n_rows) * d->features;
+    if (d->slots != uint32_t(kSlots)) {
+      // Wide layout (u16, missing rows at slots - 1): exported as u8 when every bin fits.
+      for (uint32_t f = 0; f < d->features; ++f)
+        if (d->h_bin_count[f] > 256)
+          throw UnsupportedError("the dataset has more than 256 bins per feature: u8 export is not possible");
+      std::vector<uint16_t> wide(cells);
+      CK(cudaMemcpyAsync(wide.data(), d->bins16_fm.p, cells * sizeof(uint16_t), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (uint32_t f = 0; f < d->features; ++f) {
+        for (uint32_t r = 0; r < d->n_rows; ++r) {
+          const size_t i = size_t(f) * d->n_rows + r;
+          const bool miss = d->h_has_missing[f] && wide[i] == d->slots - 1;
+          if (missing) missing[i] = miss ? 1 : 0;
+          bins[i] = miss ? 0 : uint8_t(wide[i]);
+        }
+      }
+      return;
+    }
     CK(cudaMemcpyAsync(bins, d->bins_fm.p, cells, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     // The device keeps missing rows at bin 255; the reference stores bin 0 + a flag.

@@ -27,6 +27,7 @@
 //    (the plain path): a u32 count and two FP32 reductions per cell.
 //  * The CTA flushes its non-empty cells into the node's global slot with 64-bit
 //    red.global adds (exact integer adds in fixed mode; FP64 adds in float mode).
+#include <algorithm>
 #include <type_traits>
 
 #include "device.cuh"
@@ -788,8 +789,173 @@ cudaError_t launch_variant(const TrainerDev& a, int grid, cudaStream_t stream,
 
 }  // namespace
 
+namespace {
+
+// ---- Wide datasets (more than 256 slots per feature) -----------------------------------
+//
+// The work items of the u8 kernels (build node, row chunk, block of 32 features) over the
+// u16 column blocks (a row's block is 64 contiguous bytes, one gather per row). A CTA holds
+// the histograms of `group` features of its block at a time in shared memory as 64-bit
+// cells {count, g, h}, updated by 64-bit shared atomics (integer adds, exact in any order;
+// float mode FP64 adds), then adds its non-empty cells into the node's slot. Features whose
+// slots leave no room for one feature's cells (group 0) add each row straight into the
+// slot with 64-bit global atomics.
+constexpr int kWideThreads = 512;
+constexpr size_t kWideSmemBytes = 200 * 1024;
+constexpr size_t kWideCellBytes = 3 * sizeof(unsigned long long);
+
+// Features of a block whose cells fit in the wide kernel's shared memory at once (0: none).
+uint32_t wide_group(uint32_t slots) {
+  return uint32_t(std::min<size_t>(kBlockFeatures, kWideSmemBytes / (size_t(slots) * kWideCellBytes)));
+}
+
+__device__ __forceinline__ uint32_t u16_of_block(const uint4 (&v)[4], int j) {
+  const uint4 q = v[j >> 3];
+  const int c = (j & 7) >> 1;
+  const uint32_t w = c == 0 ? q.x : c == 1 ? q.y : c == 2 ? q.z : q.w;
+  return (j & 1) ? (w >> 16) : (w & 0xFFFFu);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kWideThreads) hist_build_wide_kernel(TrainerDev a, uint32_t group) {
+  extern __shared__ __align__(16) unsigned long long wcell[];  // [group][slots][3]
+  __shared__ uint32_t s_item, s_entry;
+  const int tid = threadIdx.x;
+  const uint32_t n = a.n_rows, nfb = a.nfb, S = a.slots;
+  for (;;) {
+    const uint32_t limit = a.item_end ? a.item_end : a.ctl->hist_items;
+    if (tid == 0) {
+      const uint32_t item = a.item_begin + atomicAdd(&a.ctl->hist_counter, 1u);
+      s_item = item;
+      if (item < limit) {
+        const uint32_t chunk = item / nfb;
+        uint32_t lo = 0, hi = a.ctl->n_build;  // last entry with prefix <= chunk
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (a.build_prefix[mid] <= chunk) lo = mid; else hi = mid;
+        }
+        s_entry = lo;
+      }
+    }
+    __syncthreads();
+    const uint32_t item = s_item;
+    if (item >= limit) break;
+    const uint32_t fb = item % nfb;
+    const uint32_t chunk = item / nfb;
+    const BuildEntry e = a.build[s_entry];
+    const uint32_t item_rows = a.item_rows ? a.item_rows : a.ctl->item_rows;
+    const uint32_t row_begin = (chunk - a.build_prefix[s_entry]) * item_rows;
+    const uint32_t row_count = row_begin < e.seg_cnt ? min(item_rows, e.seg_cnt - row_begin) : 0u;
+    const size_t seg = (size_t(e.tree) * 2 + e.parity) * a.seg_stride + e.seg_off + row_begin;
+    const uint32_t* rows = a.rows + seg;
+    const float2* gh_seg = a.gh_ordered ? a.gh + seg : nullptr;
+    const float2* gh_row = a.gh_ordered ? nullptr : a.gh + size_t(e.tree) * n;
+    const uint16_t* bins = a.bins16 + size_t(fb) * n * kBlockFeatures;
+    const int kg = a.trees[e.tree].kg;
+    const int kh = a.trees[e.tree].kh;
+    const long long q_unit_h = MODE == kModeFixedCG ? quantize_f32(1.0f, kh) : 0ll;
+    const uint32_t width = min(uint32_t(kBlockFeatures), a.features - fb * kBlockFeatures);
+    unsigned long long* dst_base = a.hist + (size_t(e.slot) * a.features + size_t(fb) * kBlockFeatures) * S * 3;
+    const uint32_t step = group ? group : width;
+    for (uint32_t f0 = 0; f0 < width; f0 += step) {
+      const uint32_t gw = min(step, width - f0);
+      if (group) {
+        for (uint32_t i = tid; i < gw * S * 3; i += kWideThreads) wcell[i] = 0ull;
+        __syncthreads();
+      }
+      // Cell words of feature j of the block (shared, or the node's slot).
+      auto cell_of = [&](uint32_t j, uint32_t b) -> unsigned long long* {
+        return group ? wcell + (size_t(j - f0) * S + b) * 3 : dst_base + (size_t(j) * S + b) * 3;
+      };
+      for (uint32_t i = tid; i < row_count; i += kWideThreads) {
+        uint32_t r = __ldg(rows + i);
+        r = r < n ? r : 0u;  // row ids are < n by construction
+        const float2 p = gh_seg ? __ldg(gh_seg + i) : __ldg(gh_row + r);
+        const uint4* rb = reinterpret_cast<const uint4*>(bins + size_t(r) * kBlockFeatures);
+        uint4 v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = __ldg(rb + q);
+        long long qg = 0, qh = 0;
+        if constexpr (MODE != kModeFloat) qg = quantize_f32(p.x, kg);
+        if constexpr (MODE == kModeFixed) qh = quantize_f32(p.y, kh);
+        if constexpr (MODE == kModeFixedCG) qh = q_unit_h;
+#pragma unroll
+        for (int j = 0; j < kBlockFeatures; ++j) {
+          if (uint32_t(j) < f0 || uint32_t(j) >= f0 + gw) continue;
+          const uint32_t b = u16_of_block(v, j);
+          if (b >= S) continue;  // the pack checked every bin against its feature's count
+          unsigned long long* c = cell_of(uint32_t(j), b);
+          if constexpr (MODE == kModeFloat) {
+            atomicAdd(c, 1ull);
+            atomicAdd(reinterpret_cast<double*>(c + 1), double(p.x));
+            atomicAdd(reinterpret_cast<double*>(c + 2), double(p.y));
+          } else {
+            if constexpr (MODE != kModeFixedG) atomicAdd(c, 1ull);
+            atomicAdd(c + 1, (unsigned long long)qg);
+            // Unit-hessian builds add count x unit at the flush (straight adds: per row).
+            if constexpr (MODE == kModeFixed) atomicAdd(c + 2, (unsigned long long)qh);
+            if constexpr (MODE == kModeFixedCG) {
+              if (!group) atomicAdd(c + 2, (unsigned long long)qh);
+            }
+          }
+        }
+      }
+      if (group) {
+        __syncthreads();
+        for (uint32_t i = tid; i < gw * S; i += kWideThreads) {
+          const unsigned long long* c = wcell + size_t(i) * 3;
+          const uint32_t j = f0 + i / S, b = i % S;
+          unsigned long long* dst = dst_base + (size_t(j) * S + b) * 3;
+          if constexpr (MODE == kModeFixedG) {
+            if (c[1] != 0ull) atomicAdd(dst + 1, c[1]);
+          } else {
+            if (c[0] == 0ull) continue;
+            atomicAdd(dst + 0, c[0]);
+            if constexpr (MODE == kModeFloat) {
+              atomicAdd(reinterpret_cast<double*>(dst + 1), __longlong_as_double((long long)c[1]));
+              atomicAdd(reinterpret_cast<double*>(dst + 2), __longlong_as_double((long long)c[2]));
+            } else {
+              atomicAdd(dst + 1, c[1]);
+              if constexpr (MODE == kModeFixedCG)
+                atomicAdd(dst + 2, (unsigned long long)((long long)c[0] * q_unit_h));
+              else
+                atomicAdd(dst + 2, c[2]);
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (tid == 0) {
+      atomicAdd(&a.ctl->cells, (unsigned long long)row_count * width);
+      if (fb == 0) atomicAdd(&a.ctl->rows_built, (unsigned long long)row_count);
+    }
+    __syncthreads();
+  }
+}
+
+template <int MODE>
+cudaError_t launch_wide(const TrainerDev& a, int grid, cudaStream_t stream) {
+  static std::atomic<unsigned long long> configured{0};  // one bit per device
+  const cudaError_t err = opt_in_dynamic_smem(configured, hist_build_wide_kernel<MODE>, kWideSmemBytes);
+  if (err != cudaSuccess) return err;
+  const uint32_t group = wide_group(a.slots);
+  const size_t smem = size_t(group) * a.slots * kWideCellBytes;
+  hist_build_wide_kernel<MODE><<<grid, kWideThreads, smem, stream>>>(a, group);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int grid,
                               cudaStream_t stream) {
+  if (a.slots != uint32_t(kSlots)) {
+    if (!a.bins16 || a.slots < uint32_t(kSlots) || a.slots > 65536u) return cudaErrorInvalidValue;
+    if (a.mode == kModeFixedG) return launch_wide<kModeFixedG>(a, grid, stream);
+    if (a.mode == kModeFixedCG) return launch_wide<kModeFixedCG>(a, grid, stream);
+    if (a.mode == kModeFixed) return launch_wide<kModeFixed>(a, grid, stream);
+    return launch_wide<kModeFloat>(a, grid, stream);
+  }
   const bool row_major_tma = cfg.bins_tmap && a.mode == kModeFixed && a.bins_block_stride == kBlockFeatures &&
                              a.bins_row_stride == uint64_t(a.nfb) * kBlockFeatures;
   if (cfg.direct && a.mode != kModeFloat && !row_major_tma) {

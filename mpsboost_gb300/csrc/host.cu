@@ -80,9 +80,23 @@ std::string describe_device_error(uint32_t bits) {
 void attach_bins_tmap(mpsb_cuda_dataset* d) {
   d->has_bins_tmap = false;
   const char* v = std::getenv("MPSB_HIST_TMA");
-  if (!v || std::atoi(v) == 0) return;
+  if (!v || std::atoi(v) == 0 || d->slots != uint32_t(kSlots)) return;
   d->has_bins_tmap = encode_bins_tmap(&d->bins_tmap, d->bins.as<uint8_t>(),
                                       uint64_t(d->nfb) * kBlockFeatures, d->n_rows);
+}
+
+uint32_t dataset_slots(const uint32_t* bin_count, const uint8_t* has_missing, uint32_t features) {
+  uint64_t need = 0;
+  for (uint32_t f = 0; f < features; ++f) {
+    if (bin_count[f] == 0) throw DataError("every feature needs at least one bin");
+    if (bin_count[f] > 65536) throw DataError("a feature may have at most 65536 bins");
+    const uint64_t n = uint64_t(bin_count[f]) + (has_missing && has_missing[f] ? 1 : 0);
+    if (n > 65536)
+      throw UnsupportedError("a feature with missing values may have at most 65535 bins on the CUDA backend");
+    need = std::max(need, n);
+  }
+  if (need <= uint64_t(kSlots)) return uint32_t(kSlots);
+  return uint32_t((need + kSlots - 1) / kSlots * kSlots);
 }
 
 // ---- reference semantics evaluated on the host --------------------------------------
@@ -539,28 +553,28 @@ std::unique_ptr<mpsb_cuda_dataset> start_dataset(mpsb_cuda_backend* b, const voi
   d->nfb = (features + kBlockFeatures - 1) / kBlockFeatures;
   d->h_bin_count.assign(bin_count, bin_count + features);
   d->h_has_missing.assign(features, 0);
-  for (uint32_t f = 0; f < features; ++f) {
-    if (bin_count[f] == 0) throw DataError("every feature needs at least one bin");
-    if (bin_count[f] > 256)
-      throw UnsupportedError("the CUDA backend supports at most 256 bins per feature");
-  }
   if (missing) {
     for (uint32_t f = 0; f < features; ++f) {
       const uint8_t* m = missing + uint64_t(f) * rows;
       for (uint64_t r = 0; r < rows; ++r)
         if (m[r]) { d->h_has_missing[f] = 1; break; }
-      if (d->h_has_missing[f] && bin_count[f] > 255)
-        throw UnsupportedError("a feature with missing values may have at most 255 bins on the CUDA backend");
     }
   }
+  d->slots = dataset_slots(bin_count, d->h_has_missing.data(), features);
+  const bool wide = d->slots != uint32_t(kSlots);
   trace.mark("bin counts, missing scan");
   d->bin_count.alloc(features * sizeof(uint32_t));
   d->has_missing.alloc(features);
   CK(cudaMemcpyAsync(d->bin_count.p, bin_count, features * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
   CK(cudaMemcpyAsync(d->has_missing.p, d->h_has_missing.data(), features, cudaMemcpyHostToDevice, b->stream));
-  d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
-  d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
-  d->bins_fm.alloc(size_t(features) * rows);
+  if (wide) {
+    d->bins16.alloc(size_t(d->nfb) * rows * kBlockFeatures * sizeof(uint16_t));
+    d->bins16_fm.alloc(size_t(features) * rows * sizeof(uint16_t));
+  } else {
+    d->bins.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+    d->bins_blocked.alloc(size_t(d->nfb) * rows * kBlockFeatures);
+    d->bins_fm.alloc(size_t(features) * rows);
+  }
   d->pack_error.alloc(sizeof(uint32_t));
   CK(cudaMemsetAsync(d->pack_error.p, 0, sizeof(uint32_t), b->stream));
   CK(cudaEventCreateWithFlags(&d->ready, cudaEventDisableTiming));
@@ -597,10 +611,16 @@ std::unique_ptr<mpsb_cuda_dataset> start_dataset(mpsb_cuda_backend* b, const voi
                          b->copy_stream));
     CK(cudaEventRecord(ev.e[k], b->copy_stream));
     CK(cudaStreamWaitEvent(b->stream, ev.e[k], 0));
-    CK(launch_pack_bins_block(stage[k].p, width, missing ? mstage[k].as<uint8_t>() : nullptr,
-                              d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb, fb,
-                              d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(),
-                              d->bins_fm.as<uint8_t>(), d->pack_error.as<uint32_t>(), b->stream));
+    if (wide)
+      CK(launch_pack_bins16_block(stage[k].p, width, missing ? mstage[k].as<uint8_t>() : nullptr,
+                                  d->bin_count.as<uint32_t>(), d->n_rows, features, fb, d->slots,
+                                  d->bins16.as<uint16_t>(), d->bins16_fm.as<uint16_t>(),
+                                  d->pack_error.as<uint32_t>(), b->stream));
+    else
+      CK(launch_pack_bins_block(stage[k].p, width, missing ? mstage[k].as<uint8_t>() : nullptr,
+                                d->bin_count.as<uint32_t>(), d->n_rows, features, d->nfb, fb,
+                                d->bins.as<uint8_t>(), d->bins_blocked.as<uint8_t>(),
+                                d->bins_fm.as<uint8_t>(), d->pack_error.as<uint32_t>(), b->stream));
     CK(cudaEventRecord(ev.e[2 + k], b->stream));
   }
   CK(cudaEventRecord(d->ready, b->stream));
@@ -1043,6 +1063,9 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.bins_row_stride = uint64_t(ds->nfb) * kBlockFeatures;
   a.bins_block_stride = kBlockFeatures;
   a.bins_fm = ds->bins_fm.as<uint8_t>();
+  a.slots = ds->slots;
+  a.bins16 = ds->bins16.as<uint16_t>();
+  a.bins16_fm = ds->bins16_fm.as<uint16_t>();
   a.bin_count = ds->bin_count.as<uint32_t>();
   a.sm_count = uint32_t(b->sm_count);
   a.has_missing = ds->has_missing.as<uint8_t>();
@@ -1100,7 +1123,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
                   (p->objective == MPSB_SQUARED_ERROR || p->objective == MPSB_QUANTILE);
   if (const char* v = std::getenv("MPSB_ROOT_REUSE")) t->root_reuse = t->root_reuse && std::atoi(v) != 0;
   if (t->root_reuse) {
-    a.root_cache = t->alloc<unsigned long long>(size_t(T) * F * kSlots * 2);
+    a.root_cache = t->alloc<unsigned long long>(size_t(T) * F * ds->slots * 2);
     a.root_cache_kh = t->alloc<int>(T);
   }
   TreeParams& tp = a.params;
@@ -1233,7 +1256,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
     a.lw_scan_map = t->alloc<uint32_t>(2 * size_t(T));
     t->lw_steps = uint32_t(leaves > 0 ? leaves - 1 : 0);
   }
-  const uint64_t slot_words = uint64_t(F) * kSlots * 3;
+  const uint64_t slot_words = uint64_t(F) * ds->slots * 3;
   a.hist = t->alloc<unsigned long long>(uint64_t(a.n_slots) * slot_words);
   a.free_stack = t->alloc<uint32_t>(a.n_slots);
   for (int q = 0; q < 2; ++q) {
@@ -1648,7 +1671,7 @@ int mpsb_cuda_train_forest(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
     const uint64_t leaves = std::min<uint64_t>(
         {uint64_t(1) << std::min<uint32_t>(p->max_depth, 30), std::max<uint64_t>(effective_max_leaves(*p), 2),
          std::max<uint64_t>(1, (cap_all + p->min_samples_leaf - 1) / p->min_samples_leaf)});
-    const uint64_t per_tree = leaves * uint64_t(F) * kSlots * 24 + cap_all * (2 * 12 + 8) + n * 8 +
+    const uint64_t per_tree = leaves * uint64_t(F) * ds->slots * 24 + cap_all * (2 * 12 + 8) + n * 8 +
                               uint64_t(2 * leaves + 1) * 64 * 8;
     size_t free_b = 0, total_b = 0;
     b->activate();
@@ -1778,7 +1801,8 @@ void predict_trees(mpsb_cuda_backend* b, const std::vector<const std::vector<mps
   cudaStream_t s = b->stream;
   CK(cudaMemcpyAsync(d_nodes.p, flat.data(), flat.size() * sizeof(mpsb_tree_node), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d_off.p, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, s));
-  CK(launch_predict(ds->bins_fm.as<uint8_t>(), ds->n_rows, ds->nfb, ds->has_missing.as<uint8_t>(),
+  CK(launch_predict(ds->bins_fm.as<uint8_t>(), ds->bins16_fm.as<uint16_t>(), ds->slots, ds->n_rows,
+                    ds->nfb, ds->has_missing.as<uint8_t>(),
                     d_nodes.as<TreeNodeOut>(), d_off.as<uint32_t>(), uint32_t(trees.size()), base, lr,
                     d_out.as<double>(), b->error.as<uint32_t>(), s));
   CK(cudaMemcpyAsync(out, d_out.p, size_t(ds->n_rows) * sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -95,6 +95,10 @@ std::string describe_device_error(uint32_t bits);
 void attach_bins_tmap(mpsb_cuda_dataset* d);
 void fixed_scales(const float* pairs32, uint64_t n, uint64_t n_rows, int32_t* kg, int32_t* kh);
 void validate_tree_params(const mpsb_train_params& p, uint32_t features);
+// Histogram slots per feature for these bin counts and missing flags: 256 when every
+// feature's bins and missing slot fit in 256, else the next multiple of 256 (at most 65536;
+// a feature with missing values then has at most 65535 bins).
+uint32_t dataset_slots(const uint32_t* bin_count, const uint8_t* has_missing, uint32_t features);
 
 }  // namespace mpsb
 
@@ -127,7 +131,12 @@ struct mpsb_cuda_backend {
 struct mpsb_cuda_dataset {
   mpsb_cuda_backend* backend = nullptr;
   uint32_t n_rows = 0, features = 0, nfb = 0;
+  // Histogram slots per feature: 256 (u8 copies bins, bins_blocked, bins_fm; missing rows
+  // at 255) or, for a wide dataset, the multiple of 256 that holds every feature's bins and
+  // its missing slot (u16 copies bins16, bins16_fm; missing rows at slots - 1).
+  uint32_t slots = 256;
   mpsb::DevBuf bins, bins_blocked, bins_fm, bin_count, has_missing;
+  mpsb::DevBuf bins16, bins16_fm;
   CUtensorMap bins_tmap{};  // row-major bins for TMA gathers (valid when has_bins_tmap)
   bool has_bins_tmap = false;
   std::vector<uint32_t> h_bin_count;

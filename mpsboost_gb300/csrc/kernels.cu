@@ -374,7 +374,7 @@ __global__ void zero_build_slots_kernel(TrainerDev a) {
   if (a.node_screen)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.max_level_nodes; i += gridDim.x * blockDim.x)
       a.node_screen[i] = 0u;
-  const uint64_t words_per_slot = uint64_t(a.features) * kSlots * 3;
+  const uint64_t words_per_slot = uint64_t(a.features) * a.slots * 3;
   const uint64_t total = uint64_t(a.ctl->n_build) * (words_per_slot / 2);
   for (uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; idx < total;
        idx += uint64_t(gridDim.x) * blockDim.x) {
@@ -383,7 +383,7 @@ __global__ void zero_build_slots_kernel(TrainerDev a) {
     if (a.tree_feature_masks) {
       // A forest tree reads only its own features' histograms (and feature 0's, for the
       // root statistics): the others are neither cleared nor subtracted nor scanned.
-      const uint32_t f = uint32_t(w * 2 / (kSlots * 3));
+      const uint32_t f = uint32_t(w * 2 / (a.slots * 3));
       const uint32_t mask = a.tree_feature_masks[size_t(a.build[e].tree) * a.params.path_words + (f >> 5)];
       if (f != 0 && !((mask >> (f & 31)) & 1u)) continue;
     }
@@ -398,7 +398,7 @@ __global__ void zero_build_slots_kernel(TrainerDev a) {
 // first round of a fit builds the roots in full and saves those two words per cell; later
 // rounds build only the gradient limbs and restore them. The hessian scale is checked.
 __global__ void root_cache_kernel(TrainerDev a, int save) {
-  const uint64_t per_tree = uint64_t(a.features) * kSlots;
+  const uint64_t per_tree = uint64_t(a.features) * a.slots;
   const uint64_t total = per_tree * a.n_trees;
   for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < total;
        i += uint64_t(gridDim.x) * blockDim.x) {
@@ -426,10 +426,10 @@ __global__ void root_stats_kernel(TrainerDev a) {
   const int lane = threadIdx.x & 31;
   for (uint32_t t = threadIdx.x >> 5; t < a.n_trees; t += blockDim.x >> 5) {
     NodeRec& r = a.nodes[0][t];
-    const unsigned long long* base = a.hist + size_t(r.slot) * a.features * kSlots * 3;
+    const unsigned long long* base = a.hist + size_t(r.slot) * a.features * a.slots * 3;
     unsigned long long cnt = 0;
     long long qg = 0, qh = 0;
-    for (int s = lane; s < kSlots; s += 32) {
+    for (uint32_t s = lane; s < a.slots; s += 32) {
       cnt += base[s * 3 + 0];
       qg += (long long)base[s * 3 + 1];
       qh += (long long)base[s * 3 + 2];
@@ -449,7 +449,7 @@ __global__ void root_stats_kernel(TrainerDev a) {
         r.h = q_image(qh, st.inv_h);
       } else {  // FP64 total in slot order
         double g = 0.0, h = 0.0;
-        for (int s = 0; s < kSlots; ++s) {
+        for (uint32_t s = 0; s < a.slots; ++s) {
           g = __dadd_rn(g, __longlong_as_double((long long)base[s * 3 + 1]));
           h = __dadd_rn(h, __longlong_as_double((long long)base[s * 3 + 2]));
         }
@@ -477,7 +477,7 @@ __global__ void root_stats_kernel(TrainerDev a) {
 // slot_parent := slot_parent - slot_built for every pair (the parent slot becomes the
 // sibling's histogram).
 __global__ void subtract_kernel(TrainerDev a) {
-  const uint64_t bins_per_slot = uint64_t(a.features) * kSlots;
+  const uint64_t bins_per_slot = uint64_t(a.features) * a.slots;
   const uint64_t total = uint64_t(a.ctl->n_sub) * bins_per_slot;
   uint32_t err = 0;
   for (uint64_t idx = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; idx < total;
@@ -485,7 +485,7 @@ __global__ void subtract_kernel(TrainerDev a) {
     const SubEntry e = a.sub[idx / bins_per_slot];
     const uint64_t b = idx % bins_per_slot;
     if (a.tree_feature_masks) {  // a forest tree's own features only (sub[k] pairs build[k])
-      const uint32_t f = uint32_t(b / kSlots);
+      const uint32_t f = uint32_t(b / a.slots);
       const uint32_t mask =
           a.tree_feature_masks[size_t(a.build[idx / bins_per_slot].tree) * a.params.path_words + (f >> 5)];
       if (!((mask >> (f & 31)) & 1u)) continue;
@@ -729,7 +729,12 @@ constexpr uint32_t kChunkExact = 0x80000000u;
 //    it can win neither its chunk nor the node.
 // EXACT alone (screen off, or no node maxima: the per-feature entry point) screens each
 // feature against its own maximum. Each chunk's best split goes to partial[node][chunk].
-template <bool FIXED, bool SCREEN>
+//
+// WIDE (a dataset with more than kSlots slots per feature): each warp walks its feature's
+// slots in pages of kSlots, first for the total count and the missing slot (the last
+// page's slot kMissingSlot), then per scan pass page by page with the left prefix carried
+// from page to page; thresholds are numbered across pages.
+template <bool FIXED, bool SCREEN, bool WIDE>
 __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev a, int parity) {
   using V = typename Stat<FIXED>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -798,44 +803,68 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
       const uint32_t nb = a.bin_count[f];
       const bool hm = a.has_missing[f] != 0;
       unsigned long long* sh = s_hist + size_t(warp) * (kScanHistBytes / 8);
-      stage_feature_hist(a.hist + (size_t(node.slot) * a.features + f) * kSlots * 3, sh, lane);
-      // Slot lane * 8 + k: word w at sh[(w * 8 + k) * 32 + lane].
+      const uint32_t pages = WIDE ? a.slots / uint32_t(kSlots) : 1u;
+      const unsigned long long* fhist =
+          a.hist + (size_t(node.slot) * a.features + f) * size_t(WIDE ? a.slots : uint32_t(kSlots)) * 3;
+      // Slot lane * 8 + k of the staged page: word w at sh[(w * 8 + k) * 32 + lane].
       auto slot_word = [&](int k, int w) -> unsigned long long { return sh[(w * 8 + k) * 32 + lane]; };
-      // Lane totals of 8 consecutive slots (the missing slot excluded from the scan).
-      Stat<FIXED> sum = stat_zero<FIXED>(), miss = stat_zero<FIXED>();
-      unsigned long long total_count = 0;
+      // The lane's total of its 8 slots of the staged page; the missing slot (slot
+      // kMissingSlot of the last page) goes to `miss` instead. Raw counts add to `count`.
+      auto page_sums = [&](bool last, Stat<FIXED>& sum, Stat<FIXED>& miss,
+                           unsigned long long& count) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int s = lane * 8 + k;
-        Stat<FIXED> b;
-        const unsigned long long raw_count = slot_word(k, 0);
-        b.count = uint32_t(raw_count);  // the total below checks the full word
-        if constexpr (FIXED) {
-          b.g = (long long)slot_word(k, 1);
-          b.h = (long long)slot_word(k, 2);
-        } else {
-          b.g = __longlong_as_double((long long)slot_word(k, 1));
-          b.h = __longlong_as_double((long long)slot_word(k, 2));
-          if (!isfinite(b.g) || !isfinite(b.h) || b.h < 0.0) err |= kErrNonFinite;
+        for (int k = 0; k < 8; ++k) {
+          const int s = lane * 8 + k;
+          Stat<FIXED> b;
+          const unsigned long long raw_count = slot_word(k, 0);
+          b.count = uint32_t(raw_count);  // the total below checks the full word
+          if constexpr (FIXED) {
+            b.g = (long long)slot_word(k, 1);
+            b.h = (long long)slot_word(k, 2);
+          } else {
+            b.g = __longlong_as_double((long long)slot_word(k, 1));
+            b.h = __longlong_as_double((long long)slot_word(k, 2));
+            if (!isfinite(b.g) || !isfinite(b.h) || b.h < 0.0) err |= kErrNonFinite;
+          }
+          count += raw_count;
+          if (hm && last && s == kMissingSlot) {
+            miss = b;
+          } else {
+            sum = stat_add<FIXED>(sum, b);
+          }
         }
-        total_count += raw_count;
-        if (hm && s == kMissingSlot) {
-          miss = b;
-        } else {
-          sum = stat_add<FIXED>(sum, b);
+      };
+      auto inclusive_prefix = [&](Stat<FIXED> incl) -> Stat<FIXED> {
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const Stat<FIXED> y = shfl_up_stat<FIXED>(incl, off);
+          if (lane >= off) incl = stat_add<FIXED>(y, incl);
         }
+        return incl;
+      };
+      auto exclusive_of = [&](const Stat<FIXED>& incl) -> Stat<FIXED> {
+        Stat<FIXED> cin = shfl_up_stat<FIXED>(incl, 1);
+        if (lane == 0) cin = stat_zero<FIXED>();
+        return cin;
+      };
+      Stat<FIXED> miss = stat_zero<FIXED>(), carry_in = stat_zero<FIXED>();
+      unsigned long long total_count = 0;
+      if constexpr (WIDE) {
+        for (uint32_t p = 0; p < pages; ++p) {
+          __syncwarp();
+          stage_feature_hist(fhist + size_t(p) * kSlots * 3, sh, lane);
+          Stat<FIXED> unused = stat_zero<FIXED>();
+          page_sums(p + 1 == pages, unused, miss, total_count);
+        }
+      } else {
+        stage_feature_hist(fhist, sh, lane);
+        Stat<FIXED> sum = stat_zero<FIXED>();
+        page_sums(true, sum, miss, total_count);
+        carry_in = exclusive_of(inclusive_prefix(sum));
       }
       miss = shfl_stat<FIXED>(miss, 31);
       for (int off = 16; off > 0; off >>= 1)
         total_count += __shfl_xor_sync(0xffffffffu, total_count, off);
-      Stat<FIXED> incl = sum;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const Stat<FIXED> y = shfl_up_stat<FIXED>(incl, off);
-        if (lane >= off) incl = stat_add<FIXED>(y, incl);
-      }
-      Stat<FIXED> carry_in = shfl_up_stat<FIXED>(incl, 1);
-      if (lane == 0) carry_in = stat_zero<FIXED>();
       if (total_count != node.count) err |= kErrCountMismatch;
       Stat<FIXED> parent;
       parent.count = node.count;
@@ -918,16 +947,18 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
           *s32 = sc;
           return cls;
         };
-        // Visits every (threshold, missing direction) step of the lane's 8 slots with the
-        // candidate's left/right statistics; `cand` is false where no candidate exists.
-        // Every lane visits every step (the visitor may use warp collectives).
-        auto scan_candidates = [&](auto&& visit) {
-          Stat<FIXED> left = carry_in;
+        // Visits every (threshold, missing direction) step of the lane's 8 slots of the
+        // staged page (the left prefix before them `cin`, the page's first threshold
+        // `base`) with the candidate's left/right statistics; `cand` is false where no
+        // candidate exists. Every lane visits every step (the visitor may use warp
+        // collectives).
+        auto scan_candidates = [&](const Stat<FIXED>& cin, uint32_t base, bool last, auto&& visit) {
+          Stat<FIXED> left = cin;
 #pragma unroll 1
           for (int k = 0; k < 8; ++k) {
             const int s = lane * 8 + k;
             bool empty_bin = false;
-            if (!(hm && s == kMissingSlot)) {  // reload the slot from the staging area
+            if (!(hm && last && s == kMissingSlot)) {  // reload the slot from the staging area
               Stat<FIXED> b;
               b.count = uint32_t(slot_word(k, 0));
               empty_bin = b.count == 0;
@@ -940,7 +971,7 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
               }
               left = stat_add<FIXED>(left, b);
             }
-            const uint32_t t = uint32_t(s);
+            const uint32_t t = base + uint32_t(s);
             const Stat<FIXED> right = stat_sub<FIXED>(nmp, left);
             bool cand = t + 1 < nb;
             if (cand && left.count > nmp.count) {
@@ -961,15 +992,37 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
             }
           }
         };
+        // Runs body(left prefix, first threshold, last page) for each page: the one page
+        // staged above, or (wide) each page staged in turn with the prefix carried over.
+        auto for_pages = [&](auto&& body) {
+          if constexpr (!WIDE) {
+            body(carry_in, 0u, true);
+          } else {
+            Stat<FIXED> carry = stat_zero<FIXED>();
+            for (uint32_t p = 0; p < pages; ++p) {
+              __syncwarp();
+              stage_feature_hist(fhist + size_t(p) * kSlots * 3, sh, lane);
+              const bool last = p + 1 == pages;
+              Stat<FIXED> sum = stat_zero<FIXED>(), unused = stat_zero<FIXED>();
+              unsigned long long unused_count = 0;
+              page_sums(last, sum, unused, unused_count);
+              const Stat<FIXED> incl = inclusive_prefix(sum);
+              body(stat_add<FIXED>(carry, exclusive_of(incl)), p * uint32_t(kSlots), last);
+              carry = stat_add<FIXED>(carry, shfl_stat<FIXED>(incl, 31));
+            }
+          }
+        };
         // The lane's best certainly admissible FP32 score; close calls set `exact`.
         auto screen_scores = [&]() {
-          scan_candidates([&](bool cand, const Stat<FIXED>& cl, const Stat<FIXED>& cr, uint32_t,
-                              uint32_t) {
-            if (!cand) return;
-            float sc = 0.0f;
-            const int cls = classify(cl, cr, &sc);
-            if (cls == 1) best32 = fmaxf(best32, sc);
-            if (cls == 2) exact = true;
+          for_pages([&](const Stat<FIXED>& cin, uint32_t base, bool last) {
+            scan_candidates(cin, base, last, [&](bool cand, const Stat<FIXED>& cl,
+                                                 const Stat<FIXED>& cr, uint32_t, uint32_t) {
+              if (!cand) return;
+              float sc = 0.0f;
+              const int cls = classify(cl, cr, &sc);
+              if (cls == 1) best32 = fmaxf(best32, sc);
+              if (cls == 2) exact = true;
+            });
           });
           for (int off = 16; off > 0; off >>= 1)
             best32 = fmaxf(best32, __shfl_xor_sync(0xffffffffu, best32, off));
@@ -1004,27 +1057,29 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
             __syncwarp();
             queued = 0;
           };
-          scan_candidates([&](bool cand, const Stat<FIXED>& cl, const Stat<FIXED>& cr, uint32_t t,
-                              uint32_t dl) {
-            bool want = cand;
-            if (want && screen && cut > 0.0f) {
-              float sc = 0.0f;
-              const int cls = classify(cl, cr, &sc);
-              want = cls == 2 || (cls == 1 && sc >= cut);
-            }
-            const uint32_t ballot = __ballot_sync(0xffffffffu, want);
-            if (ballot == 0) return;
-            const uint32_t n_new = uint32_t(__popc(ballot));
-            if (queued + n_new > kScanQueue) drain();
-            if (want) {
-              ScanCand<FIXED> e;
-              e.cl = cl;
-              e.cr = cr;
-              e.threshold = t;
-              e.default_left = dl;
-              queue[queued + uint32_t(__popc(ballot & ((1u << lane) - 1u)))] = e;
-            }
-            queued += n_new;
+          for_pages([&](const Stat<FIXED>& cin, uint32_t base, bool last) {
+            scan_candidates(cin, base, last, [&](bool cand, const Stat<FIXED>& cl,
+                                                 const Stat<FIXED>& cr, uint32_t t, uint32_t dl) {
+              bool want = cand;
+              if (want && screen && cut > 0.0f) {
+                float sc = 0.0f;
+                const int cls = classify(cl, cr, &sc);
+                want = cls == 2 || (cls == 1 && sc >= cut);
+              }
+              const uint32_t ballot = __ballot_sync(0xffffffffu, want);
+              if (ballot == 0) return;
+              const uint32_t n_new = uint32_t(__popc(ballot));
+              if (queued + n_new > kScanQueue) drain();
+              if (want) {
+                ScanCand<FIXED> e;
+                e.cl = cl;
+                e.cr = cr;
+                e.threshold = t;
+                e.default_left = dl;
+                queue[queued + uint32_t(__popc(ballot & ((1u << lane) - 1u)))] = e;
+              }
+              queued += n_new;
+            });
           });
           if (queued) drain();
         }
@@ -1478,8 +1533,15 @@ __device__ __forceinline__ uint32_t find_entry(const uint32_t* prefix, uint32_t 
 __device__ __forceinline__ bool row_goes_left(const TrainerDev& a, uint32_t row, uint32_t f,
                                               uint32_t thr, uint32_t dl) {
   // Feature-major copy: a node's rows are sorted, so neighbouring rows share sectors.
-  const uint8_t b = a.bins_fm[size_t(f) * a.n_rows + row];
-  if (a.has_missing[f] && b == kMissingSlot) return dl != 0;
+  uint32_t b, missing_slot;
+  if (a.bins16_fm) {  // wide dataset (launch-uniform)
+    b = a.bins16_fm[size_t(f) * a.n_rows + row];
+    missing_slot = a.slots - 1;
+  } else {
+    b = a.bins_fm[size_t(f) * a.n_rows + row];
+    missing_slot = kMissingSlot;
+  }
+  if (a.has_missing[f] && b == missing_slot) return dl != 0;
   return b <= thr;
 }
 
@@ -2048,10 +2110,12 @@ __global__ void squared_error_kernel(const double* labels, const double* preds, 
 
 // RegressionModel::Predict (trainer.cpp:268-282): per row, trees in order,
 // result += lr * leaf; traversal of RegressionTree::Predict (tree.cpp:179-214).
-__global__ void predict_kernel(const uint8_t* bins_fm, uint32_t n_rows, const uint8_t* has_missing,
-                               const TreeNodeOut* nodes, const uint32_t* tree_offsets,
-                               uint32_t n_trees, double base, double lr, double* out,
-                               uint32_t* error) {
+// BinT: u8 bins (missing rows at 255) or u16 bins of a wide dataset (at missing_slot).
+template <typename BinT>
+__global__ void predict_kernel(const BinT* bins_fm, uint32_t missing_slot, uint32_t n_rows,
+                               const uint8_t* has_missing, const TreeNodeOut* nodes,
+                               const uint32_t* tree_offsets, uint32_t n_trees, double base,
+                               double lr, double* out, uint32_t* error) {
   uint32_t bad = 0;
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
     double acc = base;
@@ -2070,9 +2134,9 @@ __global__ void predict_kernel(const uint8_t* bins_fm, uint32_t n_rows, const ui
           break;
         }
         const uint32_t f = nd.feature_index;
-        const uint8_t b = bins_fm[size_t(f) * n_rows + r];
-        const bool left = (has_missing[f] && b == kMissingSlot) ? nd.default_left != 0
-                                                                 : b <= nd.threshold_bin;
+        const uint32_t b = bins_fm[size_t(f) * n_rows + r];
+        const bool left = (has_missing[f] && b == missing_slot) ? nd.default_left != 0
+                                                                : b <= nd.threshold_bin;
         node = left ? nd.left_child : nd.right_child;
       }
     }
@@ -2207,6 +2271,49 @@ __global__ void pack_bins_kernel(const void* src, uint32_t width, const uint8_t*
   if (bad) atomicOr(error, 1u);
 }
 
+// Wide datasets: one feature block fb (features 32 fb .. 32 fb + 31, staged from src, u8 or
+// u16, with the optional missing mask) -> the u16 column blocks [nfb][n_rows][32] (histogram
+// gathers: a row's block is 64 contiguous bytes) and the feature-major u16 copy (row
+// routing), missing rows at slots - 1. Out-of-range bins set bit 0 of `error`.
+__global__ void pack_bins16_kernel(const void* src, uint32_t width, const uint8_t* missing,
+                                   const uint32_t* bin_count, uint32_t n_rows, uint32_t features,
+                                   uint32_t fb, uint32_t slots, uint16_t* out_blocked,
+                                   uint16_t* out_fm, uint32_t* error) {
+  __shared__ uint16_t tile[32][130];
+  uint32_t bad = 0;
+  for (uint32_t r0 = blockIdx.x * 128; r0 < n_rows; r0 += gridDim.x * 128) {
+    // 32 features x 128 rows, read along rows.
+    for (uint32_t k = threadIdx.x; k < 32 * 128; k += blockDim.x) {
+      const uint32_t c = k / 128, r = k % 128;
+      const uint32_t f = fb * 32 + c, row = r0 + r;
+      uint32_t v = 0;
+      if (f < features && row < n_rows) {
+        const size_t sidx = size_t(c) * n_rows + row;
+        const uint32_t b = width == 1 ? static_cast<const uint8_t*>(src)[sidx]
+                                      : static_cast<const uint16_t*>(src)[sidx];
+        if (missing != nullptr && missing[sidx] != 0) {
+          if (bin_count[f] > slots - 1) bad = 1;
+          v = slots - 1;
+        } else {
+          if (b >= bin_count[f]) bad = 1;
+          v = b;
+        }
+        out_fm[size_t(f) * n_rows + row] = uint16_t(v);
+      }
+      tile[c][r] = uint16_t(v);
+    }
+    __syncthreads();
+    // 128 rows x 32 features: a warp writes one row's 64-byte block.
+    for (uint32_t k = threadIdx.x; k < 32 * 128; k += blockDim.x) {
+      const uint32_t r = k / 32, c = k % 32;
+      const uint32_t row = r0 + r;
+      if (row < n_rows) out_blocked[(size_t(fb) * n_rows + row) * 32 + c] = tile[c][r];
+    }
+    __syncthreads();
+  }
+  if (bad) atomicOr(error, 1u);
+}
+
 }  // namespace
 
 cudaError_t launch_round_begin(const TrainerDev& a, cudaStream_t s) {
@@ -2240,15 +2347,21 @@ cudaError_t launch_subtract(const TrainerDev& a, int grid, cudaStream_t s) {
   subtract_kernel<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
-template <bool FIXED, bool SCREEN>
-cudaError_t launch_scan_variant(const TrainerDev& a, int parity, int grid, int threads, cudaStream_t s) {
+template <bool FIXED, bool SCREEN, bool WIDE>
+cudaError_t launch_scan_shape(const TrainerDev& a, int parity, int grid, int threads, cudaStream_t s) {
   const size_t smem = scan_smem_per_warp<FIXED, SCREEN>() * size_t(threads / 32);
   static std::atomic<unsigned long long> configured{0};  // one bit per device
-  const cudaError_t err = opt_in_dynamic_smem(configured, split_scan_kernel<FIXED, SCREEN>,
+  const cudaError_t err = opt_in_dynamic_smem(configured, split_scan_kernel<FIXED, SCREEN, WIDE>,
                                               scan_smem_per_warp<FIXED, SCREEN>() * (kScanThreadsMax / 32));
   if (err != cudaSuccess) return err;
-  split_scan_kernel<FIXED, SCREEN><<<grid, threads, smem, s>>>(a, parity);
+  split_scan_kernel<FIXED, SCREEN, WIDE><<<grid, threads, smem, s>>>(a, parity);
   return cudaGetLastError();
+}
+template <bool FIXED, bool SCREEN>
+cudaError_t launch_scan_variant(const TrainerDev& a, int parity, int grid, int threads, cudaStream_t s) {
+  if (a.slots == uint32_t(kSlots)) return launch_scan_shape<FIXED, SCREEN, false>(a, parity, grid, threads, s);
+  if (a.slots < uint32_t(kSlots) || a.slots % uint32_t(kSlots)) return cudaErrorInvalidValue;
+  return launch_scan_shape<FIXED, SCREEN, true>(a, parity, grid, threads, s);
 }
 
 uint32_t split_scan_kernels(const TrainerDev& a) {
@@ -2350,14 +2463,33 @@ cudaError_t launch_pack_bins_block(const void* src_block, uint32_t width, const 
                                                             out_fm, error, fb, fb * kBlockFeatures);
   return cudaGetLastError();
 }
-cudaError_t launch_predict(const uint8_t* bins_fm, uint32_t n_rows, uint32_t nfb,
-                           const uint8_t* has_missing, const TreeNodeOut* nodes,
-                           const uint32_t* tree_offsets, uint32_t n_trees, double base,
-                           double lr, double* out, uint32_t* error, cudaStream_t s) {
+cudaError_t launch_pack_bins16_block(const void* src_block, uint32_t width,
+                                     const uint8_t* missing_block, const uint32_t* bin_count,
+                                     uint32_t n_rows, uint32_t features, uint32_t fb,
+                                     uint32_t slots, uint16_t* out_blocked, uint16_t* out_fm,
+                                     uint32_t* error, cudaStream_t s) {
+  if (slots < 2 || slots > 65536) return cudaErrorInvalidValue;
+  const uint32_t gx = std::min<uint32_t>((n_rows + 127) / 128, 4096u);
+  pack_bins16_kernel<<<gx > 0 ? gx : 1, 256, 0, s>>>(src_block, width, missing_block, bin_count, n_rows,
+                                                     features, fb, slots, out_blocked, out_fm, error);
+  return cudaGetLastError();
+}
+cudaError_t launch_predict(const uint8_t* bins_fm, const uint16_t* bins16_fm, uint32_t slots,
+                           uint32_t n_rows, uint32_t nfb, const uint8_t* has_missing,
+                           const TreeNodeOut* nodes, const uint32_t* tree_offsets,
+                           uint32_t n_trees, double base, double lr, double* out,
+                           uint32_t* error, cudaStream_t s) {
   (void)nfb;
   const int grid = int(std::min<uint64_t>((n_rows + 255) / 256, 152ull * 16));
-  predict_kernel<<<grid > 0 ? grid : 1, 256, 0, s>>>(bins_fm, n_rows, has_missing, nodes,
-                                                      tree_offsets, n_trees, base, lr, out, error);
+  if (bins16_fm) {
+    if (slots < 2 || slots > 65536) return cudaErrorInvalidValue;
+    predict_kernel<uint16_t><<<grid > 0 ? grid : 1, 256, 0, s>>>(
+        bins16_fm, slots - 1, n_rows, has_missing, nodes, tree_offsets, n_trees, base, lr, out, error);
+  } else {
+    predict_kernel<uint8_t><<<grid > 0 ? grid : 1, 256, 0, s>>>(
+        bins_fm, uint32_t(kMissingSlot), n_rows, has_missing, nodes, tree_offsets, n_trees, base,
+        lr, out, error);
+  }
   return cudaGetLastError();
 }
 

@@ -19,6 +19,13 @@ struct TrainerDev {
   const uint8_t* bins_fm;       // [features][n_rows] feature-major u8 bins (routing rows)
   const uint32_t* bin_count;    // [features]
   const uint8_t* has_missing;   // [features]
+  // Histogram slots per feature: 256 (u8 bins, missing rows at slot 255), or for wide
+  // datasets (a feature with more than 256 bins, or 256 bins and missing values) a larger
+  // multiple of 256 with missing rows at slot slots - 1; wide datasets keep u16 copies of
+  // the bins in place of the u8 ones.
+  uint32_t slots = kSlots;
+  const uint16_t* bins16;       // wide: [nfb][n_rows][32] column blocks (else null)
+  const uint16_t* bins16_fm;    // wide: [features][n_rows] (else null)
   uint32_t n_rows, features, nfb, n_trees;
   // per-tree arrays
   const double* labels;         // [n_rows]
@@ -47,7 +54,7 @@ struct TrainerDev {
   const int8_t* monotonic;      // [features] or null
   const uint32_t* group_masks;  // [n_groups][path_words]
   const uint32_t* tree_feature_masks;  // [n_trees][path_words] or null
-  // histogram slots: [n_slots][features][256] x {count, g, h} 64-bit words
+  // histogram slots: [n_slots][features][slots] x {count, g, h} 64-bit words
   unsigned long long* hist;
   uint32_t* free_stack;         // [n_slots]
   uint32_t n_slots;
@@ -121,7 +128,7 @@ struct TrainerDev {
   uint32_t* lw_slot_top;        // [n_trees]
   uint32_t* lw_scan_map;        // [2 * n_trees]
   uint32_t lw_cap, lw_slot_cap, lw_max_active, lw_max_leaves;
-  // Root count/hessian histograms of the fit's first round: [n_trees][features][256]
+  // Root count/hessian histograms of the fit's first round: [n_trees][features][slots]
   // {count, qh} and the hessian scale they were built with (null: not reused).
   unsigned long long* root_cache;
   int* root_cache_kh;
@@ -174,11 +181,21 @@ cudaError_t launch_apply_leaves(const TrainerDev& a, int grid, cudaStream_t stre
 cudaError_t launch_round_end(const TrainerDev& a, cudaStream_t stream);
 cudaError_t launch_squared_error(const double* labels, const double* preds, uint64_t n,
                                  double* out_pairs, uint32_t* error, cudaStream_t stream);
-cudaError_t launch_predict(const uint8_t* bins_fm, uint32_t n_rows, uint32_t nfb,
-                           const uint8_t* has_missing, const TreeNodeOut* nodes,
-                           const uint32_t* tree_offsets, uint32_t n_trees, double base,
-                           double learning_rate, double* out, uint32_t* error,
-                           cudaStream_t stream);
+// Bins from the u8 feature-major copy (missing rows at 255), or with bins16_fm set from
+// the u16 one (missing rows at slots - 1).
+cudaError_t launch_predict(const uint8_t* bins_fm, const uint16_t* bins16_fm, uint32_t slots,
+                           uint32_t n_rows, uint32_t nfb, const uint8_t* has_missing,
+                           const TreeNodeOut* nodes, const uint32_t* tree_offsets,
+                           uint32_t n_trees, double base, double learning_rate, double* out,
+                           uint32_t* error, cudaStream_t stream);
+// Wide datasets: one feature block fb of the u16 copies ([nfb][n_rows][32] column blocks
+// and [features][n_rows]) from a staged copy of its source features, missing rows at
+// slots - 1.
+cudaError_t launch_pack_bins16_block(const void* src_block, uint32_t width,
+                                     const uint8_t* missing_block, const uint32_t* bin_count,
+                                     uint32_t n_rows, uint32_t features, uint32_t fb,
+                                     uint32_t slots, uint16_t* out_blocked, uint16_t* out_fm,
+                                     uint32_t* error, cudaStream_t stream);
 // One feature block fb of the dataset from a staged copy of its source features
 // (src_block / missing_block start at feature 32 * fb).
 cudaError_t launch_pack_bins_block(const void* src_block, uint32_t width, const uint8_t* missing_block,

@@ -45,6 +45,9 @@ void base_session(Session& ss, mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds
   a.bins_row_stride = uint64_t(ds->nfb) * kBlockFeatures;
   a.bins_block_stride = kBlockFeatures;
   a.bins_fm = ds->bins_fm.as<uint8_t>();
+  a.slots = ds->slots;
+  a.bins16 = ds->bins16.as<uint16_t>();
+  a.bins16_fm = ds->bins16_fm.as<uint16_t>();
   a.sm_count = uint32_t(b->sm_count);
   a.bin_count = ds->bin_count.as<uint32_t>();
   a.has_missing = ds->has_missing.as<uint8_t>();
@@ -123,7 +126,7 @@ void build_slots(Session& ss, mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
   a.build = ss.upload(build.data(), build.size(), s);
   a.build_prefix = ss.upload(prefix.data(), prefix.size(), s);
   a.n_slots = n_nodes;
-  a.hist = ss.alloc<unsigned long long>(size_t(n_nodes) * ds->features * kSlots * 3);
+  a.hist = ss.alloc<unsigned long long>(size_t(n_nodes) * ds->features * ds->slots * 3);
   Control c{};
   c.n_build = n_nodes;
   c.hist_items = prefix[n_nodes] * ds->nfb;
@@ -144,10 +147,11 @@ void check_ctl(const TrainerDev& a, cudaStream_t s) {
 void decode_slots(const mpsb_cuda_dataset* ds, const std::vector<unsigned long long>& slots,
                   uint32_t n_nodes, int mode, const TreeState& st, mpsb_histogram_bin* out) {
   const uint32_t F = ds->features;
+  const size_t miss = ds->slots - 1;  // missing rows' slot
   size_t k = 0;
   for (uint32_t i = 0; i < n_nodes; ++i) {
     for (uint32_t f = 0; f < F; ++f) {
-      const unsigned long long* base = slots.data() + (size_t(i) * F + f) * kSlots * 3;
+      const unsigned long long* base = slots.data() + (size_t(i) * F + f) * ds->slots * 3;
       const bool hm = ds->h_has_missing[f] != 0;
       for (uint32_t bin = 0; bin < ds->h_bin_count[f]; ++bin) {
         unsigned long long cnt = base[bin * 3];
@@ -155,9 +159,9 @@ void decode_slots(const mpsb_cuda_dataset* ds, const std::vector<unsigned long l
         if (mode == kModeFixed) {
           long long qg = (long long)base[bin * 3 + 1], qh = (long long)base[bin * 3 + 2];
           if (bin == 0 && hm) {
-            cnt += base[kMissingSlot * 3];
-            qg += (long long)base[kMissingSlot * 3 + 1];
-            qh += (long long)base[kMissingSlot * 3 + 2];
+            cnt += base[miss * 3];
+            qg += (long long)base[miss * 3 + 1];
+            qh += (long long)base[miss * 3 + 2];
           }
           o.gradient_sum = double(qg) * st.inv_g;
           o.hessian_sum = double(qh) * st.inv_h;
@@ -167,9 +171,9 @@ void decode_slots(const mpsb_cuda_dataset* ds, const std::vector<unsigned long l
           std::memcpy(&h, &base[bin * 3 + 2], 8);
           if (bin == 0 && hm) {
             double mg, mh;
-            std::memcpy(&mg, &base[kMissingSlot * 3 + 1], 8);
-            std::memcpy(&mh, &base[kMissingSlot * 3 + 2], 8);
-            cnt += base[kMissingSlot * 3];
+            std::memcpy(&mg, &base[miss * 3 + 1], 8);
+            std::memcpy(&mh, &base[miss * 3 + 2], 8);
+            cnt += base[miss * 3];
             g += mg;
             h += mh;
           }
@@ -214,7 +218,7 @@ int mpsb_cuda_build_layer_histograms(mpsb_cuda_backend* b, const mpsb_cuda_datas
     TreeState st;
     build_slots(ss, b, ds, rows, node_offsets, n_nodes, pairs, n_pairs, &st);
     check_ctl(ss.a, b->stream);
-    std::vector<unsigned long long> slots(size_t(n_nodes) * ds->features * kSlots * 3);
+    std::vector<unsigned long long> slots(size_t(n_nodes) * ds->features * ds->slots * 3);
     CK(cudaMemcpy(slots.data(), ss.a.hist, slots.size() * 8, cudaMemcpyDeviceToHost));
     decode_slots(ds, slots, n_nodes, int(ss.a.mode), st, out);
   });

@@ -39,9 +39,10 @@ def _reference_matrix(rows=1025):
 
 
 @pytest.mark.parametrize("mode", ["fixed", "float"])
-@pytest.mark.parametrize("max_bins", [16, 255])
+@pytest.mark.parametrize("max_bins", [16, 255, 257])
 def test_histogram_matches_every_oracle_bin(backend, port, mode, max_bins):
-    """tests/metal/test_mps_histogram.py:31-77 (257 bins exceed this backend's 256)."""
+    """tests/metal/test_mps_histogram.py:31-77: max_bins 16 and 255 (u8) and 257 (u16
+    storage; the linspace column has 257 bins)."""
     x = _reference_matrix()
     labels = np.sin(np.arange(1025) / 17.0)
     selected = np.arange(3, 1025, 2)
@@ -180,9 +181,13 @@ def test_node_entry_errors(backend):
         backend.partition_rows(binned, [1, 2], 0, 99)
     with pytest.raises(mb.TrainingError, match="empty"):
         backend.partition_rows(binned, [], 0, 1)
-    wide = mb.quantize_dense(np.linspace(0, 1, 1000, dtype=np.float32)[:, None], 300)
-    with pytest.raises(mb.UnsupportedError, match="256"):
-        backend.dataset(wide)
+    # 65536 bins and missing values leave no u16 value for the missing slot.
+    col = np.arange(65537, dtype=np.float32)
+    col[7] = np.nan
+    full = mb.quantize_dense(col[:, None], 65536)
+    assert int(full.bin_counts[0]) == 65536
+    with pytest.raises(mb.UnsupportedError, match="65535"):
+        backend.dataset(full)
 
 
 def test_integer_pipe_conversions_match_hardware(tmp_path):

@@ -35,6 +35,11 @@ CASES = [
          params=dict(max_depth=6, max_leaves=9, gamma=0.001, min_gain_to_split=0.0001)),
     dict(rows=300, feats=2, nan=0.3, ints=0, max_bins=300, objective="squared_error",
          params=dict(max_depth=3)),
+    # u16 storage with most features near max_bins and missing values in each.
+    dict(rows=4000, feats=4, nan=0.05, ints=1, max_bins=1500, objective="squared_error",
+         params=dict(max_depth=5, min_samples_leaf=3)),
+    dict(rows=3000, feats=3, nan=0.1, ints=0, max_bins=4096, objective="binary_logistic",
+         params=dict(max_depth=4, min_samples_leaf=2)),
 ]
 
 

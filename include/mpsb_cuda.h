@@ -318,9 +318,11 @@ int mpsb_cuda_build_histogram_noalloc(const uint8_t* bins, uint32_t dataset_rows
 /* QuantizeDense on the GPU: the matrix (scalar_type 1 = float32, 2 = float64; element
    (r, f) at byte offset r * row_stride + f * col_stride) is uploaded, binned with the
    reference's quantile rule and kept resident as a training dataset. NaN is missing, Inf
-   and float64 values outside the float32 range are DataErrors. max_bins <= 256 (255 when a
-   feature has missing values). Bins and boundaries equal mpsb_quantize_dense's, except
-   that a boundary at zero may carry either sign (the two zeros compare equal). */
+   and float64 values outside the float32 range are DataErrors. max_bins in [2, 65536]
+   (a feature with 65536 bins may not have missing values); above 256 the order
+   statistics come from a per-feature sort. Bins and boundaries equal
+   mpsb_quantize_dense's, except that a boundary at zero may carry either sign (the two
+   zeros compare equal). */
 int mpsb_cuda_dataset_quantize(mpsb_cuda_backend* backend, const void* data, int scalar_type,
                                uint64_t rows, uint32_t features, uint64_t row_stride,
                                uint64_t col_stride, uint32_t max_bins, mpsb_cuda_dataset** out);
@@ -337,8 +339,12 @@ int mpsb_cuda_dataset_schema(const mpsb_cuda_dataset* dataset, float* boundaries
                              uint64_t* boundary_offset, uint32_t* boundary_count,
                              uint32_t* bin_count, uint64_t* missing_count);
 /* The binned matrix, feature-major u8 [features][rows] (missing rows as bin 0), and the
-   missing flags (may be NULL), as mpsb_quantize_dense lays them out. */
+   missing flags (may be NULL), as mpsb_quantize_dense lays them out; UnsupportedError for
+   a dataset with more than 256 bins in a feature. */
 int mpsb_cuda_dataset_export(const mpsb_cuda_dataset* dataset, uint8_t* bins, uint8_t* missing);
+/* The same as u16 [features][rows], for any dataset (mpsb_quantize_dense's layout when
+   max_bins > 256). */
+int mpsb_cuda_dataset_export16(const mpsb_cuda_dataset* dataset, uint16_t* bins, uint8_t* missing);
 
 /* Softmax models: class count (0 for a regression model), base scores, margins
    [rows][class_count] of a binned dataset, and creation from host trees ordered

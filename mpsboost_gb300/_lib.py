@@ -167,6 +167,7 @@ SIGNATURES = {
     "mpsb_cuda_dataset_boundary_total": (_U64, [_VP]),
     "mpsb_cuda_dataset_schema": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "mpsb_cuda_dataset_export": (_I32, [_VP, _VP, _VP]),
+    "mpsb_cuda_dataset_export16": (_I32, [_VP, _VP, _VP]),
     "mpsb_cuda_model_set_schema": (_I32, [_VP, _U32, _U32, _VP, _U64, _VP, _VP, _VP, _VP]),
     "mpsb_cuda_model_set_objective": (_I32, [_VP, _U32, _F64, _F64]),
     "mpsb_cuda_model_get_objective": (_I32, [_VP, _VP, _VP, _VP]),

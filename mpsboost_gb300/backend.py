@@ -287,9 +287,11 @@ class DeviceBinnedDataset:
 
     def to_host(self) -> BinnedDataset:
         lib = _lib.load()
-        bins = np.empty((self.features, self.rows), np.uint8)
+        wide = self.max_bins > 256  # quantize_dense's storage: u16 above 256 bins
+        bins = np.empty((self.features, self.rows), np.uint16 if wide else np.uint8)
         missing = np.empty((self.features, self.rows), np.uint8)
-        check(lib.mpsb_cuda_dataset_export(self._dev.handle, ptr(bins), ptr(missing)))
+        export = lib.mpsb_cuda_dataset_export16 if wide else lib.mpsb_cuda_dataset_export
+        check(export(self._dev.handle, ptr(bins), ptr(missing)))
         return BinnedDataset(self.rows, self.features, self.max_bins, bins, missing.astype(bool),
                              self.boundaries_flat.copy(), self.boundary_offsets.copy(),
                              self.boundary_counts.copy(), self.bin_counts.copy(), self.missing_counts.copy())

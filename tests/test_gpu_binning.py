@@ -1,7 +1,9 @@
 """Quantile binning on the device against the host restatement (QuantizeDense /
 TransformDense, binned_dataset.cpp:95-238; the host path is pinned to the reference in
 test_oracle_pin.py). Bins, missing flags, boundary counts and bin counts are identical;
-boundaries are equal as floats (a boundary at zero may carry either sign)."""
+boundaries are equal as floats (a boundary at zero may carry either sign). Up to 256 bins
+the boundaries come from the radix selection, above 256 (u16 bins) from a per-feature
+sort."""
 
 from __future__ import annotations
 
@@ -44,11 +46,12 @@ def _matrix(seed, rows, cols):
 
 
 @pytest.mark.parametrize("rows,cols,max_bins", [(1, 3, 16), (7, 9, 4), (1000, 10, 255), (50_000, 12, 64),
-                                                (123_457, 8, 256), (20_000, 40, 2)])
+                                                (123_457, 8, 256), (20_000, 40, 2), (3, 4, 300),
+                                                (50_000, 9, 1000), (123_457, 8, 4096), (30_000, 5, 65536),
+                                                (70_001, 3, 65535)])
 def test_quantize_matches_host(backend, rows, cols, max_bins):
+    """256 bins with missing values train on the wide layout; above 256 the bins are u16."""
     x = _matrix(rows + cols, rows, cols)
-    if max_bins == 256:  # 256 bins leave no slot for missing values on the device
-        x = np.nan_to_num(x, nan=1.5)
     _same(mb.quantize_device(backend, x, max_bins), mb.quantize_dense(x, max_bins))
 
 
@@ -62,21 +65,23 @@ def test_layouts_and_dtypes(backend):
     _same(mb.quantize_device(backend, wide[:, ::2], 128), host)              # strided view
 
 
-def test_transform_matches_host(backend):
+@pytest.mark.parametrize("max_bins", [200, 3000])
+def test_transform_matches_host(backend, max_bins):
     x = _matrix(11, 20_000, 10)
     y = _matrix(12, 7_000, 10)
-    host = mb.quantize_dense(x, 200)
-    dev = mb.quantize_device(backend, x, 200)
+    host = mb.quantize_dense(x, max_bins)
+    dev = mb.quantize_device(backend, x, max_bins)
     _same(dev.transform(y), host.transform(y))
 
 
-def test_training_on_device_bins_equals_host_bins(backend):
+@pytest.mark.parametrize("max_bins", [255, 1024])
+def test_training_on_device_bins_equals_host_bins(backend, max_bins):
     x = _matrix(13, 30_000, 10)
     rng = np.random.default_rng(14)
     y = np.nan_to_num(x[:, 0]) * 2 + rng.normal(size=x.shape[0])
     params = dict(n_estimators=3, learning_rate=0.2, max_depth=6, min_samples_leaf=3)
-    a = mb.train_regressor(backend, mb.quantize_dense(x, 255), y, **params)
-    dev = mb.quantize_device(backend, x, 255)
+    a = mb.train_regressor(backend, mb.quantize_dense(x, max_bins), y, **params)
+    dev = mb.quantize_device(backend, x, max_bins)
     b = mb.train_regressor(backend, dev, y, **params)
     for t1, t2 in zip(a.trees, b.trees):
         assert t1.tobytes() == t2.tobytes()
@@ -94,8 +99,10 @@ def test_quantize_errors(backend):
     big[2, 2] = 1e39
     with pytest.raises(mb.DataError, match="float32"):
         mb.quantize_device(backend, big, 16)
-    with pytest.raises(mb.UnsupportedError):
-        mb.quantize_device(backend, x, 300)
+    full = np.arange(65537, dtype=np.float32)[:, None]  # 65536 bins and a missing value
+    full[9] = np.nan
+    with pytest.raises(mb.UnsupportedError, match="65535"):
+        mb.quantize_device(backend, full, 65536)
     with pytest.raises(mb.DataError, match="max_bins"):
         mb.quantize_device(backend, x, 1)
 

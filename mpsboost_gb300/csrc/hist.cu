@@ -794,34 +794,59 @@ namespace {
 // ---- Wide datasets (more than 256 slots per feature) -----------------------------------
 //
 // The work items of the u8 kernels (build node, row chunk, block of 32 features) over the
-// u16 column blocks (a row's block is 64 contiguous bytes, one gather per row). A CTA holds
-// the histograms of `group` features of its block at a time in shared memory as 64-bit
-// cells {count, g, h}, updated by 64-bit shared atomics (integer adds, exact in any order;
-// float mode FP64 adds), then adds its non-empty cells into the node's slot. Features whose
-// slots leave no room for one feature's cells (group 0) add each row straight into the
-// slot with 64-bit global atomics.
-constexpr int kWideThreads = 512;
-constexpr size_t kWideSmemBytes = 200 * 1024;
-constexpr size_t kWideCellBytes = 3 * sizeof(unsigned long long);
-
-// Features of a block whose cells fit in the wide kernel's shared memory at once (0: none).
-uint32_t wide_group(uint32_t slots) {
-  return uint32_t(std::min<size_t>(kBlockFeatures, kWideSmemBytes / (size_t(slots) * kWideCellBytes)));
-}
-
-__device__ __forceinline__ uint32_t u16_of_block(const uint4 (&v)[4], int j) {
-  const uint4 q = v[j >> 3];
-  const int c = (j & 7) >> 1;
-  const uint32_t w = c == 0 ? q.x : c == 1 ? q.y : c == 2 ? q.z : q.w;
-  return (j & 1) ? (w >> 16) : (w & 0xFFFFu);
-}
+// u16 column blocks (a row's block is 64 contiguous bytes). A CTA accumulates `group`
+// features of its block at a time (a power of two: as many as the shared-memory budget
+// holds) in the u8 kernels' 32-bit limbs per cell ([limb][bin][feature]; exact over the
+// item's <= 2^16 rows), then adds the non-empty cells into the node's slot. A warp takes
+// 32 gathered rows at a time: lane l quantizes row l's values once, then group / 2 lanes
+// per row each load one 4-byte word (two features' bins) of a row, with the row id and the
+// limbs shuffled from the quantizing lane, and reduce both features, neighbouring rows in
+// opposite order, so that each round's reductions spread over the group's features.
+// Features too wide for one feature's cells in shared memory (group 0) add each row
+// straight into the slot with 64-bit global atomics.
+constexpr uint32_t kWideBatch = 4;  // gathered words in flight per lane
+constexpr size_t kWideSmemBytes = 200 * 1024;  // the CTA histogram's limbs
+// Fixed-point flushes go through TMA bulk reductions of 8 cells of one feature (192
+// bytes), staged by kWideFlushWarps warps in rows after the histogram.
+constexpr int kWideFlushWarps = 4;
+constexpr size_t kWideStagingBytes = size_t(kWideFlushWarps) * 32 * kFlushRowWords * 8;
 
 template <int MODE>
-__global__ void __launch_bounds__(kWideThreads) hist_build_wide_kernel(TrainerDev a, uint32_t group) {
-  extern __shared__ __align__(16) unsigned long long wcell[];  // [group][slots][3]
+__host__ __device__ constexpr int wide_words() {  // 32-bit limbs per cell
+  return MODE == kModeFixed ? 5 : (MODE == kModeFixedG ? 2 : 3);
+}
+
+// Features per shared-memory pass: the largest power of two <= 32 whose cells fit (0: none).
+template <int MODE>
+uint32_t wide_group(uint32_t slots) {
+  const size_t fit = kWideSmemBytes / (size_t(slots) * wide_words<MODE>() * sizeof(uint32_t));
+  uint32_t g = kBlockFeatures;
+  while (g > fit) g >>= 1;
+  return g;
+}
+
+__device__ __forceinline__ uint32_t ld_nc_u32(const void* p) {
+  uint32_t v;
+  asm volatile("ld.global.nc.u32 %0, [%1];\n" : "=r"(v) : "l"(p));
+  return v;
+}
+
+template <int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS) hist_build_wide_kernel(TrainerDev a, uint32_t group) {
+  constexpr int WORDS = wide_words<MODE>();
+  constexpr int WARPS = THREADS / 32;
+  extern __shared__ __align__(16) uint32_t wsm[];  // [WORDS][slots][group], then the staging rows
   __shared__ uint32_t s_item, s_entry;
   const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
   const uint32_t n = a.n_rows, nfb = a.nfb, S = a.slots;
+  const uint32_t cells = S * group;
+  const uint32_t L = group >= 2 ? group / 2 : 1u;  // lanes per row
+  const uint32_t R = 32u / L;                      // rows per step
+  const uint32_t flip = (uint32_t(lane) / L) & 1u;
+  const uint32_t w = uint32_t(lane) % L;           // the lane's word of a row's group
+  const uint32_t hist_base = static_cast<uint32_t>(__cvta_generic_to_shared(wsm));
+  const uint32_t plane = cells * 4u;               // bytes per limb plane
   for (;;) {
     const uint32_t limit = a.item_end ? a.item_end : a.ctl->hist_items;
     if (tid == 0) {
@@ -856,72 +881,174 @@ __global__ void __launch_bounds__(kWideThreads) hist_build_wide_kernel(TrainerDe
     const long long q_unit_h = MODE == kModeFixedCG ? quantize_f32(1.0f, kh) : 0ll;
     const uint32_t width = min(uint32_t(kBlockFeatures), a.features - fb * kBlockFeatures);
     unsigned long long* dst_base = a.hist + (size_t(e.slot) * a.features + size_t(fb) * kBlockFeatures) * S * 3;
+    const uint32_t ntiles = (row_count + 31u) / 32u;
     const uint32_t step = group ? group : width;
     for (uint32_t f0 = 0; f0 < width; f0 += step) {
       const uint32_t gw = min(step, width - f0);
       if (group) {
-        for (uint32_t i = tid; i < gw * S * 3; i += kWideThreads) wcell[i] = 0ull;
+        uint4* z = reinterpret_cast<uint4*>(wsm);
+        for (uint32_t i = tid; i < uint32_t(WORDS) * cells / 4u; i += THREADS) z[i] = make_uint4(0, 0, 0, 0);
         __syncthreads();
       }
-      // Cell words of feature j of the block (shared, or the node's slot).
-      auto cell_of = [&](uint32_t j, uint32_t b) -> unsigned long long* {
-        return group ? wcell + (size_t(j - f0) * S + b) * 3 : dst_base + (size_t(j) * S + b) * 3;
+      // Row id and values of the lane's row of tile t (zeros past the item's end).
+      auto load_row = [&](uint32_t t, uint32_t& r, float2& p) {
+        const uint32_t pos = t * 32u + uint32_t(lane);
+        r = 0u;
+        p = make_float2(0.f, 0.f);
+        if (t < ntiles && pos < row_count) {
+          r = __ldg(rows + pos);
+          r = r < n ? r : 0u;  // row ids are < n by construction
+          p = gh_seg ? __ldg(gh_seg + pos) : __ldg(gh_row + r);
+        }
       };
-      for (uint32_t i = tid; i < row_count; i += kWideThreads) {
-        uint32_t r = __ldg(rows + i);
-        r = r < n ? r : 0u;  // row ids are < n by construction
-        const float2 p = gh_seg ? __ldg(gh_seg + i) : __ldg(gh_row + r);
-        const uint4* rb = reinterpret_cast<const uint4*>(bins + size_t(r) * kBlockFeatures);
-        uint4 v[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] = __ldg(rb + q);
-        long long qg = 0, qh = 0;
-        if constexpr (MODE != kModeFloat) qg = quantize_f32(p.x, kg);
-        if constexpr (MODE == kModeFixed) qh = quantize_f32(p.y, kh);
-        if constexpr (MODE == kModeFixedCG) qh = q_unit_h;
-#pragma unroll
-        for (int j = 0; j < kBlockFeatures; ++j) {
-          if (uint32_t(j) < f0 || uint32_t(j) >= f0 + gw) continue;
-          const uint32_t b = u16_of_block(v, j);
-          if (b >= S) continue;  // the pack checked every bin against its feature's count
-          unsigned long long* c = cell_of(uint32_t(j), b);
-          if constexpr (MODE == kModeFloat) {
-            atomicAdd(c, 1ull);
-            atomicAdd(reinterpret_cast<double*>(c + 1), double(p.x));
-            atomicAdd(reinterpret_cast<double*>(c + 2), double(p.y));
+      uint32_t r_nxt;
+      float2 p_nxt;
+      load_row(uint32_t(warp), r_nxt, p_nxt);
+      for (uint32_t t = warp; t < ntiles; t += WARPS) {
+        const uint32_t pos = t * 32u + uint32_t(lane);
+        const uint32_t r = r_nxt;
+        const float2 p = p_nxt;
+        load_row(t + WARPS, r_nxt, p_nxt);  // the warp's next tile, in flight meanwhile
+        if (!group) {  // straight into the slot, each lane its own row
+          if (pos < row_count) {
+            const long long qg = MODE == kModeFloat ? 0ll : quantize_f32(p.x, kg);
+            const long long qh = MODE == kModeFixed ? quantize_f32(p.y, kh) : q_unit_h;
+            for (uint32_t j = f0; j < f0 + gw; ++j) {
+              const uint32_t b = __ldg(bins + size_t(r) * kBlockFeatures + j);
+              if (b >= S) continue;  // the pack checked every bin against its feature's count
+              unsigned long long* c = dst_base + (size_t(j) * S + b) * 3;
+              if constexpr (MODE == kModeFloat) {
+                atomicAdd(c, 1ull);
+                atomicAdd(reinterpret_cast<double*>(c + 1), double(p.x));
+                atomicAdd(reinterpret_cast<double*>(c + 2), double(p.y));
+              } else {
+                if constexpr (MODE != kModeFixedG) atomicAdd(c, 1ull);
+                atomicAdd(c + 1, (unsigned long long)qg);
+                if constexpr (MODE != kModeFixedG) atomicAdd(c + 2, (unsigned long long)qh);
+              }
+            }
+          }
+          continue;
+        }
+        // The row's limbs, as the u8 kernels stage them.
+        uint2 v = make_uint2(0u, 0u);
+        if (pos < row_count) {
+          if constexpr (MODE == kModeFixed) {
+            const long long qg = quantize_f32(p.x, kg);
+            const long long qh = quantize_f32(p.y, kh);
+            const uint32_t glo = uint32_t(qg) & 0xFFFFu, ghi = uint32_t(qg >> 16) & 0xFFFFu;
+            const uint32_t hlo = uint32_t(qh) & 0xFFFFu, hhi = uint32_t(qh >> 16) & 0xFFFFu;
+            v = make_uint2(glo | (hlo << 16), ghi | (hhi << 16));
+          } else if constexpr (MODE == kModeFloat) {
+            v = make_uint2(__float_as_uint(p.x), __float_as_uint(p.y));
           } else {
-            if constexpr (MODE != kModeFixedG) atomicAdd(c, 1ull);
-            atomicAdd(c + 1, (unsigned long long)qg);
-            // Unit-hessian builds add count x unit at the flush (straight adds: per row).
-            if constexpr (MODE == kModeFixed) atomicAdd(c + 2, (unsigned long long)qh);
-            if constexpr (MODE == kModeFixedCG) {
-              if (!group) atomicAdd(c + 2, (unsigned long long)qh);
+            v = make_uint2(uint32_t(quantize_f32(p.x, kg)), 0u);
+          }
+        }
+        auto accumulate = [&](uint32_t cell, uint32_t vx, uint32_t vy) {
+          const uint32_t addr = hist_base + cell * 4u;
+          if constexpr (MODE == kModeFixed) {
+            red_shared_u32(addr, 1u);
+            red_shared_u32(addr + plane, vx & 0xFFFFu);
+            red_shared_u32(addr + 2u * plane, uint32_t(int32_t(int16_t(vy & 0xFFFFu))));
+            red_shared_u32(addr + 3u * plane, vx >> 16);
+            red_shared_u32(addr + 4u * plane, vy >> 16);
+          } else if constexpr (MODE == kModeFixedG) {
+            red_shared_u32(addr, vx & 0xFFFFu);
+            red_shared_u32(addr + plane, uint32_t(int32_t(vx) >> 16));
+          } else if constexpr (MODE == kModeFixedCG) {
+            red_shared_u32(addr, 1u);
+            red_shared_u32(addr + plane, vx & 0xFFFFu);
+            red_shared_u32(addr + 2u * plane, uint32_t(int32_t(vx) >> 16));
+          } else {
+            red_shared_u32(addr, 1u);
+            red_shared_f32(addr + plane, __uint_as_float(vx));
+            red_shared_f32(addr + 2u * plane, __uint_as_float(vy));
+          }
+        };
+        // Steps in batches of kWideBatch: the batch's gathers are issued together, then
+        // reduced. A step's word is that of row st * R + lane / L of the tile.
+        for (uint32_t st0 = 0; st0 < L; st0 += kWideBatch) {
+          uint32_t word[kWideBatch], bx[kWideBatch], by[kWideBatch];
+          bool ok[kWideBatch];
+#pragma unroll
+          for (uint32_t k = 0; k < kWideBatch; ++k) {
+            const uint32_t src = (st0 + k) * R + uint32_t(lane) / L;  // < 32 while st0 + k < L
+            const uint32_t src_lane = src & 31u;
+            const uint32_t rr = __shfl_sync(0xffffffffu, r, int(src_lane));
+            bx[k] = __shfl_sync(0xffffffffu, v.x, int(src_lane));
+            by[k] = __shfl_sync(0xffffffffu, v.y, int(src_lane));
+            ok[k] = st0 + k < L && t * 32u + src < row_count && 2u * w < gw;
+            word[k] = 0u;
+            if (ok[k])
+              word[k] = group >= 2 ? ld_nc_u32(bins + size_t(rr) * kBlockFeatures + f0 + 2u * w)
+                                   : uint32_t(__ldg(bins + size_t(rr) * kBlockFeatures + f0));
+          }
+#pragma unroll
+          for (uint32_t k = 0; k < kWideBatch; ++k) {
+            if (!ok[k]) continue;
+#pragma unroll
+            for (uint32_t i = 0; i < 2; ++i) {
+              const uint32_t sel = (i + flip) & 1u;
+              const uint32_t fl = 2u * w + sel;
+              const uint32_t b = sel ? word[k] >> 16 : word[k] & 0xFFFFu;
+              if (fl < gw && b < S) accumulate(b * group + fl, bx[k], by[k]);
             }
           }
         }
       }
       if (group) {
         __syncthreads();
-        for (uint32_t i = tid; i < gw * S; i += kWideThreads) {
-          const unsigned long long* c = wcell + size_t(i) * 3;
-          const uint32_t j = f0 + i / S, b = i % S;
-          unsigned long long* dst = dst_base + (size_t(j) * S + b) * 3;
-          if constexpr (MODE == kModeFixedG) {
-            if (c[1] != 0ull) atomicAdd(dst + 1, c[1]);
-          } else {
-            if (c[0] == 0ull) continue;
-            atomicAdd(dst + 0, c[0]);
-            if constexpr (MODE == kModeFloat) {
-              atomicAdd(reinterpret_cast<double*>(dst + 1), __longlong_as_double((long long)c[1]));
-              atomicAdd(reinterpret_cast<double*>(dst + 2), __longlong_as_double((long long)c[2]));
-            } else {
-              atomicAdd(dst + 1, c[1]);
-              if constexpr (MODE == kModeFixedCG)
-                atomicAdd(dst + 2, (unsigned long long)((long long)c[0] * q_unit_h));
-              else
-                atomicAdd(dst + 2, c[2]);
+        if constexpr (MODE == kModeFloat) {
+          for (uint32_t idx = tid; idx < cells; idx += THREADS) {
+            const uint32_t fl = idx % group, b = idx / group;
+            if (fl >= gw || wsm[idx] == 0) continue;
+            unsigned long long* dst = dst_base + (size_t(f0 + fl) * S + b) * 3;
+            atomicAdd(dst + 0, (unsigned long long)wsm[idx]);
+            atomicAdd(reinterpret_cast<double*>(dst + 1), double(__uint_as_float(wsm[cells + idx])));
+            atomicAdd(reinterpret_cast<double*>(dst + 2), double(__uint_as_float(wsm[2 * cells + idx])));
+          }
+        } else if (warp < kWideFlushWarps) {
+          // Lane (bin group bg, feature fl) of a warp's tile converts 8 consecutive bins of
+          // its feature into the slot's 24 words and hands them to one bulk reduction.
+          unsigned long long* row = reinterpret_cast<unsigned long long*>(
+              reinterpret_cast<unsigned char*>(wsm) + size_t(WORDS) * cells * 4) + (size_t(warp) * 32 + lane) * kFlushRowWords;
+          const uint32_t row_addr = static_cast<uint32_t>(__cvta_generic_to_shared(row));
+          const uint32_t per_tile = 32u / group;  // bin groups per tile (group divides 32)
+          const uint32_t fl = uint32_t(lane) % group, bg = uint32_t(lane) / group;
+          for (uint32_t g0 = uint32_t(warp) * per_tile; g0 < S / kFlushBins; g0 += kWideFlushWarps * per_tile) {
+            const uint32_t b0 = (g0 + bg) * kFlushBins;  // S / 8 is a multiple of 32
+            bulk_wait_read();  // the row's previous bulk reduction has read it
+            unsigned long long any = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < kFlushBins; ++j) {
+              const uint32_t idx = (b0 + j) * group + fl;
+              unsigned long long c, g, h;
+              if constexpr (MODE == kModeFixed) {
+                c = wsm[idx];
+                g = (unsigned long long)((long long)int32_t(wsm[2 * cells + idx]) * 65536 + (long long)wsm[cells + idx]);
+                h = (unsigned long long)((long long)wsm[4 * cells + idx] * 65536 + (long long)wsm[3 * cells + idx]);
+              } else if constexpr (MODE == kModeFixedG) {
+                c = 0;  // the gradient-only root's count and hessian words are restored afterwards
+                g = (unsigned long long)((long long)int32_t(wsm[cells + idx]) * 65536 + (long long)wsm[idx]);
+                h = 0;
+              } else {
+                c = wsm[idx];
+                g = (unsigned long long)((long long)int32_t(wsm[2 * cells + idx]) * 65536 + (long long)wsm[cells + idx]);
+                h = (unsigned long long)((long long)c * q_unit_h);
+              }
+              row[3 * j + 0] = c;
+              row[3 * j + 1] = g;
+              row[3 * j + 2] = h;
+              any |= c | g | h;
+            }
+            if (fl < gw && any != 0ull) {
+              asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the row's stores before the bulk read
+              bulk_reduce_add_u64(dst_base + (size_t(f0 + fl) * S + b0) * 3, row_addr, kFlushBins * 3 * 8);
+              bulk_commit();
             }
           }
+          bulk_wait_read();  // the staging rows are free again
         }
         __syncthreads();
       }
@@ -932,17 +1059,26 @@ __global__ void __launch_bounds__(kWideThreads) hist_build_wide_kernel(TrainerDe
     }
     __syncthreads();
   }
+  bulk_wait_all();  // this thread's bulk reductions have reached the slots
 }
 
-template <int MODE>
+template <int MODE, int THREADS>
 cudaError_t launch_wide(const TrainerDev& a, int grid, cudaStream_t stream) {
   static std::atomic<unsigned long long> configured{0};  // one bit per device
-  const cudaError_t err = opt_in_dynamic_smem(configured, hist_build_wide_kernel<MODE>, kWideSmemBytes);
+  const cudaError_t err = opt_in_dynamic_smem(configured, hist_build_wide_kernel<MODE, THREADS>,
+                                              kWideSmemBytes + kWideStagingBytes);
   if (err != cudaSuccess) return err;
-  const uint32_t group = wide_group(a.slots);
-  const size_t smem = size_t(group) * a.slots * kWideCellBytes;
-  hist_build_wide_kernel<MODE><<<grid, kWideThreads, smem, stream>>>(a, group);
+  const uint32_t group = wide_group<MODE>(a.slots);
+  const size_t smem = group ? size_t(group) * a.slots * wide_words<MODE>() * sizeof(uint32_t) + kWideStagingBytes : 0;
+  hist_build_wide_kernel<MODE, THREADS><<<grid, THREADS, smem, stream>>>(a, group);
   return cudaGetLastError();
+}
+
+// Wide launches: 1024 threads, or 512.
+template <int MODE>
+cudaError_t launch_wide_shape(const TrainerDev& a, int threads, int grid, cudaStream_t stream) {
+  if (threads == 512) return launch_wide<MODE, 512>(a, grid, stream);
+  return launch_wide<MODE, 1024>(a, grid, stream);
 }
 
 }  // namespace
@@ -951,10 +1087,11 @@ cudaError_t launch_hist_build(const TrainerDev& a, const HistConfig& cfg, int gr
                               cudaStream_t stream) {
   if (a.slots != uint32_t(kSlots)) {
     if (!a.bins16 || a.slots < uint32_t(kSlots) || a.slots > 65536u) return cudaErrorInvalidValue;
-    if (a.mode == kModeFixedG) return launch_wide<kModeFixedG>(a, grid, stream);
-    if (a.mode == kModeFixedCG) return launch_wide<kModeFixedCG>(a, grid, stream);
-    if (a.mode == kModeFixed) return launch_wide<kModeFixed>(a, grid, stream);
-    return launch_wide<kModeFloat>(a, grid, stream);
+    const int t = cfg.wide_threads;
+    if (a.mode == kModeFixedG) return launch_wide_shape<kModeFixedG>(a, t, grid, stream);
+    if (a.mode == kModeFixedCG) return launch_wide_shape<kModeFixedCG>(a, t, grid, stream);
+    if (a.mode == kModeFixed) return launch_wide_shape<kModeFixed>(a, t, grid, stream);
+    return launch_wide_shape<kModeFloat>(a, t, grid, stream);
   }
   const bool row_major_tma = cfg.bins_tmap && a.mode == kModeFixed && a.bins_block_stride == kBlockFeatures &&
                              a.bins_row_stride == uint64_t(a.nfb) * kBlockFeatures;

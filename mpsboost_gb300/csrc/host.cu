@@ -1112,6 +1112,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   t->hcfg.direct = true;
   if (const char* v = std::getenv("MPSB_HIST_DIRECT")) t->hcfg.direct = std::atoi(v) != 0;
   if (const char* v = std::getenv("MPSB_ROOT_THREADS")) t->hcfg.root_threads = std::atoi(v);
+  if (const char* v = std::getenv("MPSB_WIDE_THREADS")) t->hcfg.wide_threads = std::atoi(v);
   if (const char* v = std::getenv("MPSB_BLOCKED_LEVELS")) t->blocked_levels = uint32_t(std::atoi(v));
   if (const char* v = std::getenv("MPSB_ITEMS_PER_SM")) a.items_per_sm = uint32_t(std::max(1, std::atoi(v)));
   if (const char* v = std::getenv("MPSB_ITEM_ROWS"))

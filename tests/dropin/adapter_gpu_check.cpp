@@ -3,8 +3,8 @@
 // detection by dynamic_cast (as tree_histogram.cpp:83-84 does), squared-error gradients,
 // layer and node histograms against FP64 row-order sums on the host (count exact, G within
 // 2e-5 and H within 1e-6, the reference's GPU tolerances, tests/metal/test_mps_histogram.py),
-// missing rows in bin 0, a second dataset replacing the resident one, and the contract's
-// errors. Prints "adapter ok" on success; exits non-zero with a message otherwise.
+// missing rows in bin 0, a second dataset replacing the resident one, a u16 dataset (up to
+// 4000 bins), and the contract's errors. Prints "adapter ok" on success; exits non-zero with a message otherwise.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -22,12 +22,15 @@ static int fail(const char* what) {
   return 1;
 }
 
-static BinnedDataset make_dataset(std::uint64_t rows, std::uint32_t features, unsigned seed) {
+// u8 storage with 2 .. 255 bins per feature, or (wide) u16 storage with up to 4000 bins.
+static BinnedDataset make_dataset(std::uint64_t rows, std::uint32_t features, unsigned seed,
+                                  bool wide = false) {
   std::mt19937_64 gen(seed);
-  std::vector<std::uint8_t> bins(rows * features), missing(rows * features, 0);
+  std::vector<std::uint16_t> bins(rows * features);
+  std::vector<std::uint8_t> missing(rows * features, 0);
   std::vector<FeatureBinMetadata> meta(features);
   for (std::uint32_t f = 0; f < features; ++f) {
-    meta[f].bin_count = 2 + (f * 37) % 254;  // 2 .. 255 bins
+    meta[f].bin_count = wide ? 2 + (f * 997) % 3999 : 2 + (f * 37) % 254;
     for (std::uint64_t r = 0; r < rows; ++r) {
       const std::size_t c = std::size_t(f) * rows + r;
       if (f % 3 == 0 && gen() % 10 == 0) {  // every third feature has missing values
@@ -35,11 +38,13 @@ static BinnedDataset make_dataset(std::uint64_t rows, std::uint32_t features, un
         bins[c] = 0;
         ++meta[f].missing_count;
       } else {
-        bins[c] = std::uint8_t(gen() % meta[f].bin_count);
+        bins[c] = std::uint16_t(gen() % meta[f].bin_count);
       }
     }
   }
-  return BinnedDataset(rows, features, std::move(bins), std::move(missing), std::move(meta));
+  if (wide) return BinnedDataset(rows, features, std::move(bins), std::move(missing), std::move(meta));
+  return BinnedDataset(rows, features, std::vector<std::uint8_t>(bins.begin(), bins.end()), std::move(missing),
+                       std::move(meta));
 }
 
 static bool check_node(const BinnedDataset& ds, const std::vector<std::uint64_t>& rows,
@@ -84,8 +89,9 @@ int main() {
   std::vector<GradientPair> weighted(gp);
   for (std::uint64_t i = 0; i < n; ++i) weighted[i].hessian = 0.5 + double(i % 7) / 7.0;
 
-  for (unsigned round = 0; round < 2; ++round) {  // the second dataset replaces the resident one
-    const BinnedDataset ds = make_dataset(n, round == 0 ? 70 : 33, 100 + round);
+  // The second dataset replaces the resident one; the third stores u16 bins.
+  for (unsigned round = 0; round < 3; ++round) {
+    const BinnedDataset ds = make_dataset(n, round == 0 ? 70 : (round == 1 ? 33 : 9), 100 + round, round == 2);
     std::vector<std::vector<std::uint64_t>> nodes(3);
     for (std::uint64_t r = 0; r < n; ++r) nodes[(r * 2654435761u >> 7) % 3].push_back(r);
     nodes[2].resize(nodes[2].size() / 4);  // a small node

@@ -53,23 +53,32 @@ class BinnedDataset {
                 std::vector<std::uint8_t> missing, std::vector<FeatureBinMetadata> metadata)
       : rows_(rows), features_(features), bins_(std::move(bins)), missing_(std::move(missing)),
         metadata_(std::move(metadata)) {}
+  // u16 storage (max_bins above 256, binned_dataset.cpp:132).
+  BinnedDataset(std::uint64_t rows, std::uint32_t features, std::vector<std::uint16_t> bins,
+                std::vector<std::uint8_t> missing, std::vector<FeatureBinMetadata> metadata)
+      : rows_(rows), features_(features), bins16_(std::move(bins)), missing_(std::move(missing)),
+        metadata_(std::move(metadata)) {}
   std::uint64_t rows() const noexcept { return rows_; }
   std::uint32_t features() const noexcept { return features_; }
-  BinStorage storage() const noexcept { return BinStorage::kUInt8; }
+  BinStorage storage() const noexcept { return bins16_.empty() ? BinStorage::kUInt8 : BinStorage::kUInt16; }
   const std::vector<FeatureBinMetadata>& feature_metadata() const noexcept { return metadata_; }
-  const void* bin_data() const noexcept { return bins_.data(); }
+  const void* bin_data() const noexcept {
+    return bins16_.empty() ? static_cast<const void*>(bins_.data()) : static_cast<const void*>(bins16_.data());
+  }
   bool IsMissing(std::uint64_t row, std::uint32_t feature) const {
     return missing_[static_cast<std::size_t>(feature) * rows_ + row] != 0;
   }
-  std::uint8_t Bin(std::uint64_t row, std::uint32_t feature) const {
-    return bins_[static_cast<std::size_t>(feature) * rows_ + row];
+  std::uint32_t Bin(std::uint64_t row, std::uint32_t feature) const {
+    const std::size_t i = static_cast<std::size_t>(feature) * rows_ + row;
+    return bins16_.empty() ? bins_[i] : bins16_[i];
   }
 
  private:
   std::uint64_t rows_;
   std::uint32_t features_;
-  std::vector<std::uint8_t> bins_;     // [features][rows], missing rows in bin 0
-  std::vector<std::uint8_t> missing_;  // [features][rows]
+  std::vector<std::uint8_t> bins_;      // [features][rows], missing rows in bin 0
+  std::vector<std::uint16_t> bins16_;   // the same, u16 storage
+  std::vector<std::uint8_t> missing_;   // [features][rows]
   std::vector<FeatureBinMetadata> metadata_;
 };
 

@@ -186,3 +186,17 @@ def test_wide_partition_matches_oracle(backend, port):
             gl, gr = backend.partition_rows(binned, sel, 1, thr, default_left=dl)
             wl, wr = port.partition_rows(ds, sel, 1, thr, default_left=dl)
             assert gl == wl.tolist() and gr == wr.tolist()
+
+
+def test_wide_launch_shapes_build_the_same_trees(backend, monkeypatch):
+    """512 and 1024 threads per CTA (MPSB_WIDE_THREADS) give byte-identical models."""
+    x = seeded_matrix(64, 30000, 40, 0.05, 2)
+    y, w = _labels(x, 65)
+    binned = mb.quantize_dense(x, 1500)
+    params = dict(n_estimators=2, learning_rate=0.2, max_depth=6, min_samples_leaf=3)
+    models = []
+    for threads in ("1024", "512"):
+        monkeypatch.setenv("MPSB_WIDE_THREADS", threads)
+        models.append(mb.train_regressor(backend, binned, y, w, **params))
+    assert [t.tobytes() for t in models[0].trees] == [t.tobytes() for t in models[1].trees]
+    assert models[0].train_predictions.tobytes() == models[1].train_predictions.tobytes()

@@ -245,27 +245,28 @@ def run_ours(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     xf, y, w = make_data(args.rows)
     t0 = time.perf_counter()
-    binned = mb.quantize_dense(xf.T, BINS)
+    binned = mb.quantize_dense(xf.T, args.max_bins)
     t_bin = time.perf_counter() - t0
+    params = dict(PARAMS, max_bins=args.max_bins)
     backend = mb.CudaBackend(local)
     # The same binning on the device (QuantizeDense on the GPU), host matrix to resident
     # bins; checked against the host bins.
-    mb.quantize_device(backend, xf[:, :1024].T, BINS).close()  # warm the kernels
+    mb.quantize_device(backend, xf[:, :1024].T, args.max_bins).close()  # warm the kernels
     backend.synchronize()
     t0 = time.perf_counter()
-    dbin = mb.quantize_device(backend, xf.T, BINS)
+    dbin = mb.quantize_device(backend, xf.T, args.max_bins)
     backend.synchronize()
     t_dbin = time.perf_counter() - t0
     dbin_equal = bool(np.array_equal(dbin.bin_counts, binned.bin_counts))
     dbin.close()
     # Launch shape for this fit shape: the autotuner times rounds under candidate shapes and
     # every later session below (timed, roofline, end to end) uses the fastest.
-    tuning = (backend.autotune(binned, y, w, rounds_per_trial=5, **PARAMS) if not args.no_autotune
+    tuning = (backend.autotune(binned, y, w, rounds_per_trial=5, **params) if not args.no_autotune
               else {"hist_threads": 768, "hist_stages": 2, "root_threads": 1024, "items_per_sm": 3,
                     "blocked_levels": 2, "scan_threads": 128, "trials": 0, "ms_per_round": 0.0,
                     "default_ms_per_round": 0.0})
     n_rounds = args.warmup + args.steps
-    trainer = mb.Trainer(backend, binned, y, w, n_estimators=2 * n_rounds + 4, **PARAMS)
+    trainer = mb.Trainer(backend, binned, y, w, n_estimators=2 * n_rounds + 4, **params)
     trainer.run(args.warmup)
     trainer.synchronize()
     trainer.reset_stats()
@@ -291,6 +292,7 @@ def run_ours(args, rank, world):
     if args.only_train:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "trees/s", "rows": args.rows,
+                              "max_bins": args.max_bins,
                               "steps": args.steps, "warmup": args.warmup,
                               "gpu_launches": int(st["kernel_launches"]), "only_train": True,
                               "hist_cells": int(st["hist_cells"]), "hist_rows": int(st["hist_rows"]),
@@ -456,8 +458,28 @@ def run_secondary(mb, backend):
     trees per round.
     random forest 1M x 100, 256 trees, depth 12, sqrt features, Poisson(1) rows: one
     host-timed fit of the whole forest through the public API (sample expansion, upload,
-    training, model readback) after a 16-tree warm-up."""
+    training, model readback) after a 16-tree warm-up.
+    wide bins: the regression workload's generator at 4M rows with max_bins 1024 (u16
+    bins, 1024 histogram slots per feature), device-binned; trees/s over 8 graph-replayed
+    rounds, CUDA events."""
     out = {}
+    xf, y, w = make_data(4_000_000)
+    dset = mb.quantize_device(backend, xf.T, 1024)
+    del xf
+    params = dict(PARAMS, max_bins=1024)
+    t = mb.Trainer(backend, dset, y, w, n_estimators=12, **params)
+    t.run(3)
+    t.synchronize()
+    backend.timer_begin()
+    t.run(8)
+    ms = backend.timer_end()
+    t.synchronize()
+    t.close()
+    dset.close()
+    out["regression_1024bins_4Mx128_d8"] = {"value": 8 / (ms / 1e3), "unit": "trees/s", "ms_per_tree": ms / 8,
+                                            "rounds": 8, "timing": "CUDA events, graph per round"}
+    del y, w
+
     x, y = make_logistic_data()
     dset = mb.quantize_device(backend, x, 255)
     del x
@@ -566,7 +588,11 @@ def main():
                     help="keep the built-in launch shape (profiling runs)")
     ap.add_argument("--only-train", action="store_true",
                     help="time the training rounds only (for launch lists and ncu captures)")
+    ap.add_argument("--max-bins", type=int, default=BINS,
+                    help="with --only-train: bins per feature (above 256: u16 bins, the wide kernels)")
     args = ap.parse_args()
+    if args.max_bins != BINS and not args.only_train:
+        ap.error("--max-bins applies to --only-train runs")
     if args.warmup < 3:
         args.warmup = 3
     rank, world = dist_setup()

@@ -564,6 +564,36 @@ def run_forest(args, rank, world):
                                   "training, model readback), binned data resident"}), flush=True)
 
 
+def run_logistic(args, rank, world):
+    """Binary logistic configuration: 4M x 256 (10 % missing cells), depth 10, lr 0.1,
+    device-binned to 255 bins; K graph-replayed rounds after W warm-up rounds, CUDA events
+    (rows from --rows when given below the default)."""
+    import mpsboost_gb300 as mb
+
+    rows = min(args.rows, 4_000_000)
+    x, y = make_logistic_data(rows)
+    backend = mb.CudaBackend(int(os.environ.get("LOCAL_RANK", "0")))
+    dset = mb.quantize_device(backend, x, 255)
+    del x
+    params = dict(max_depth=10, learning_rate=0.1, objective="binary_logistic", min_samples_leaf=20,
+                  min_child_weight=1.0, reg_lambda=1.0, max_bins=255)
+    t = mb.Trainer(backend, dset, y, None, n_estimators=args.warmup + args.steps + 1, **params)
+    t.run(args.warmup)
+    t.synchronize()
+    barrier(world)
+    backend.timer_begin()
+    t.run(args.steps)
+    ms = reduce_max(backend.timer_end(), world)
+    t.synchronize()
+    st = t.stats()
+    t.close()
+    if rank == 0:
+        print(json.dumps({"metric": "trees/s @4Mx256 logistic d10", "value": world * args.steps / (ms / 1e3),
+                          "unit": "trees/s", "rows": rows, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_tree": ms / args.steps, "gpu_launches": int(st["kernel_launches"]),
+                          "dtype": "int64", "data": "synthetic"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -581,8 +611,9 @@ def main():
                     help="skip the bounded logistic / one-vs-rest / forest measurements")
     ap.add_argument("--rows", type=int, default=ROWS,
                     help="rows of the synthetic workload (profiling runs use fewer)")
-    ap.add_argument("--workload", choices=["regression", "forest"], default="regression",
-                    help="forest: the 256-tree random-forest configuration instead of the default")
+    ap.add_argument("--workload", choices=["regression", "forest", "logistic"], default="regression",
+                    help="forest: the 256-tree random-forest configuration instead of the default; "
+                         "logistic: the binary-logistic configuration's training rounds")
     ap.add_argument("--forest-trees", type=int, default=256)
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the built-in launch shape (profiling runs)")
@@ -600,6 +631,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "forest":
         run_forest(args, rank, world)
+    elif args.workload == "logistic":
+        run_logistic(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:

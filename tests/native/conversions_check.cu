@@ -1,6 +1,6 @@
 // Checks the software IEEE conversions of device.cuh (s64_to_f32_rn, f64_to_f32_rn,
-// f64_finite on 2^26 seeded inputs per family; u32_to_f32_rn on every 32-bit input) bit
-// for bit against the hardware conversions, plus the edge cases: ties at every rounding
+// f64_finite on 2^26 seeded inputs per family) bit for bit against the hardware
+// conversions, plus the edge cases: ties at every rounding
 // position, the float overflow threshold, the subnormal range and its boundaries, signed
 // zeros, infinities and NaNs.
 // Exit status 0 when every result matches; prints the first mismatch otherwise.
@@ -114,17 +114,6 @@ __global__ void check_kernel(uint32_t family, unsigned long long n, Report* r) {
   }
 }
 
-// u32_to_f32_rn over every 32-bit input.
-__global__ void check_u32_kernel(Report* r) {
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < (1ull << 32);
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    const uint32_t x = uint32_t(i);
-    const uint32_t got = __float_as_uint(u32_to_f32_rn(x));
-    const uint32_t want = __float_as_uint(__uint2float_rn(x));
-    if (got != want) record(r, 7, i, got, want);
-  }
-}
-
 int main() {
   Report* r = nullptr;
   if (cudaMalloc(&r, sizeof(Report)) != cudaSuccess) return 2;
@@ -143,16 +132,6 @@ int main() {
                   h.first_input, h.first_got, h.first_want);
       ++failures;
     }
-  }
-  cudaMemset(r, 0, sizeof(Report));
-  check_u32_kernel<<<sms * 8, 256>>>(r);
-  Report h{};
-  if (cudaMemcpy(&h, r, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
-  std::printf("u32 -> f32: 4294967296 inputs, %llu mismatches\n", h.mismatches);
-  if (h.mismatches) {
-    std::printf("  first: input 0x%08llx got 0x%08x want 0x%08x\n", h.first_input, h.first_got,
-                h.first_want);
-    ++failures;
   }
   cudaFree(r);
   return failures ? 1 : 0;

@@ -62,7 +62,25 @@ struct TreeParams {
   uint32_t objective;
   double objective_alpha;
   double tweedie_variance_power;
+  // The split scan's FP32 screen constants, derived on the host (set_screen_constants):
+  // computed in the kernel, the double-to-float conversions and FP64 compares were
+  // re-evaluated at their uses inside the candidate loop, on the narrow FP64 pipe.
+  float screen_lambda;                 // float(reg_lambda)
+  float screen_mcw_lo, screen_mcw_hi;  // float(min_child_weight) x (1 - 3e-6), x (1 + 3e-6)
+  uint32_t screen_mcw_on;              // min_child_weight > 0
+  uint32_t screen_params;              // split_strategy 0, reg_alpha 0, reg_lambda > 0
 };
+
+// Fills the screen constants of a TreeParams from its FP64 fields (IEEE float conversion
+// and multiplication: the same values the device computes).
+inline void set_screen_constants(TreeParams& p) {
+  const float mcw32 = float(p.min_child_weight);
+  p.screen_lambda = float(p.reg_lambda);
+  p.screen_mcw_lo = mcw32 * (1.0f - 3e-6f);
+  p.screen_mcw_hi = mcw32 * (1.0f + 3e-6f);
+  p.screen_mcw_on = p.min_child_weight > 0.0 ? 1u : 0u;
+  p.screen_params = (p.split_strategy == 0 && p.reg_alpha == 0.0 && p.reg_lambda > 0.0) ? 1u : 0u;
+}
 
 // One node of a depth level. Statistics are exact int64 (fixed mode; g/h hold the FP64
 // images q * 2^-k) or FP64 (float mode).

@@ -1146,6 +1146,7 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   tp.objective = p->objective;
   tp.objective_alpha = p->objective_alpha;
   tp.tweedie_variance_power = p->tweedie_variance_power;
+  set_screen_constants(tp);
   cudaStream_t s = b->stream;
   const uint32_t W = tp.path_words;
 

@@ -754,10 +754,10 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
   const uint32_t items = n_nodes * n_chunks;
   const bool two_phase = !SCREEN && a.node_screen != nullptr && a.scan_two_phase != 0;
   // Launch-wide screen constants (FP64 tests and conversions stay out of the item loop).
-  const bool screen_params = P.split_strategy == 0 && P.reg_alpha == 0.0 && P.reg_lambda > 0.0;
-  const float lam32 = float(P.reg_lambda), mcw32 = float(P.min_child_weight);
-  const bool mcw_on = P.min_child_weight > 0.0;
-  const float mcw_lo = mcw32 * (1.0f - 3e-6f), mcw_hi = mcw32 * (1.0f + 3e-6f);
+  const bool screen_params = P.screen_params != 0;
+  const float lam32 = P.screen_lambda;
+  const bool mcw_on = P.screen_mcw_on != 0;
+  const float mcw_lo = P.screen_mcw_lo, mcw_hi = P.screen_mcw_hi;
   for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
     const uint32_t i = item / n_chunks, c = item % n_chunks;
     const NodeRec node = a.nodes[parity][i];

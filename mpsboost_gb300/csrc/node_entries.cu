@@ -260,6 +260,7 @@ int mpsb_cuda_scan_splits(mpsb_cuda_backend* b, const mpsb_cuda_dataset* ds,
     tp.random_seed = p->random_seed;
     tp.has_monotonic = p->n_monotonic ? 1 : 0;
     tp.path_words = W;
+    set_screen_constants(tp);
     if (p->n_monotonic) a.monotonic = ss.upload(p->monotonic_constraints, F, s);
     NodeRec node{};
     node.seg_off = 0;

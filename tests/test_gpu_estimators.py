@@ -26,18 +26,20 @@ def _data(seed, n=6000, f=8, nan=0.05):
     return x, y, rng.uniform(0.5, 1.5, n)
 
 
-def test_regressor_equals_direct_fit_and_replica(backend, port):
+@pytest.mark.parametrize("max_bins", [255, 256, 1024])
+def test_regressor_equals_direct_fit_and_replica(backend, port, max_bins):
+    """255 bins: u8; 256 (the reference's default) with missing values and 1024: u16 bins."""
     x, y, w = _data(61)
-    model = mb.GradientBoostingRegressor(n_estimators=4, max_depth=5, learning_rate=0.2, max_bins=255)
+    model = mb.GradientBoostingRegressor(n_estimators=4, max_depth=5, learning_rate=0.2, max_bins=max_bins)
     assert model.fit(x, y, sample_weight=w) is model
     assert model.device_ == "cuda" and model.n_estimators_ == 4
     assert model.device_decision_["selected"] == "cuda"
-    binned = mb.quantize_dense(x, 255)
+    binned = mb.quantize_dense(x, max_bins)
     params = dict(n_estimators=4, max_depth=5, learning_rate=0.2, min_samples_leaf=20, min_child_weight=1.0)
     direct = mb.train_regressor(backend, binned, y, w, **params)
     trees = model.model_.model.trees
     assert [t.tobytes() for t in trees] == [t.tobytes() for t in direct.trees]
-    want = port.train_regressor(port.quantize_dense(x, 255), y, w, hist_mode=oracle.HIST_FIXED, **params)
+    want = port.train_regressor(port.quantize_dense(x, max_bins), y, w, hist_mode=oracle.HIST_FIXED, **params)
     assert [t.tobytes() for t in trees] == [t.tobytes() for t in want.trees]
     pred = model.predict(x)
     assert pred.dtype == np.float32

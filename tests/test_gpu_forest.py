@@ -55,6 +55,9 @@ CASES = {
                         params=dict(max_depth=5, min_samples_leaf=2, split_strategy="random_threshold")),
     "logistic": dict(seed=55, rows=3000, feats=8, nan=0.0, ints=2, trees=4, max_features=0.5,
                      objective="binary_logistic", params=dict(max_depth=4, min_samples_leaf=4)),
+    # u16 bins (1000 per feature, missing values): the wide kernels under ragged forests.
+    "wide_bins": dict(seed=56, rows=4000, feats=9, nan=0.05, ints=1, trees=5, max_features=0.6,
+                      max_bins=1000, params=dict(max_depth=5, min_samples_leaf=3)),
 }
 
 
@@ -67,13 +70,14 @@ def test_forest_trees_bit_exact_to_replica(backend, port, name):
         c["rows"], c["feats"], c["trees"], random_state=c["seed"], bootstrap=c.get("bootstrap", True),
         sample_fraction=c.get("sample_fraction", 1.0), max_features=c["max_features"])
     params = dict(c["params"], objective=objective)
-    binned = mb.quantize_dense(x, 64)
+    max_bins = c.get("max_bins", 64)
+    binned = mb.quantize_dense(x, max_bins)
     models = mb.train_forest(backend, binned, y, w, row_counts=counts, feature_subsets=subsets,
-                             seeds=seeds, **params)
-    ds = port.quantize_dense(x, 64)
+                             seeds=seeds, **dict(params, max_bins=max_bins))
+    ds = port.quantize_dense(x, max_bins)
     assert len(models) == c["trees"]
     for t, m in enumerate(models):
-        base, nodes = _oracle_tree(port, ds, y, w, counts[t], subsets[t], params, seeds[t])
+        base, nodes = _oracle_tree(port, ds, y, w, counts[t], subsets[t], dict(params, max_bins=max_bins), seeds[t])
         assert float(m.base_score).hex() == float(base).hex()
         assert m.learning_rate == 1.0 and len(m.trees) == 1
         assert m.trees[0].tobytes() == nodes.tobytes(), f"tree {t}"

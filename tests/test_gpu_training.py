@@ -451,12 +451,13 @@ def test_loss_against_fp64_reference(backend, port, name):
     np.testing.assert_allclose(model.train_predictions, want.predict(ds), rtol=1e-5, atol=1e-9)
 
 
-def test_ovr_equals_independent_binary_fits(backend, port):
+@pytest.mark.parametrize("max_bins", [64, 900])
+def test_ovr_equals_independent_binary_fits(backend, port, max_bins):
     rng = np.random.default_rng(42)
     x = rng.normal(size=(4000, 6)).astype(np.float32)
     scores = x @ rng.normal(size=(6, 4)) + rng.gumbel(size=(4000, 4))
     labels = scores.argmax(axis=1).astype(np.float64)
-    binned = mb.quantize_dense(x, 64)
+    binned = mb.quantize_dense(x, max_bins)
     params = dict(n_estimators=2, learning_rate=0.3, max_depth=4, min_samples_leaf=3)
     models = mb.train_ovr(backend, binned, labels, 4, **params)
     assert len(models) == 4
@@ -577,19 +578,20 @@ def test_full_size_properties(backend):
     assert len(totals) == 1
 
 
-def test_softmax_against_replica(backend, port):
+@pytest.mark.parametrize("max_bins", [64, 700])
+def test_softmax_against_replica(backend, port, max_bins):
     """Native softmax: K trees per round in class order, each on the margins updated by
     the earlier classes. Base scores bit-exact; tree structures equal to the oracle's
     fixed-point replica; leaves and margins within 1e-9 (the device's FP64 exp and the
-    host's may differ in the last bit)."""
+    host's may differ in the last bit). 700 bins: u16 storage, the wide kernels."""
     rng = np.random.default_rng(46)
     x = rng.normal(size=(6000, 7)).astype(np.float32)
     x[rng.random(x.shape) < 0.05] = np.nan
     y = (np.nan_to_num(x) @ rng.normal(size=(7, 4)) + rng.gumbel(size=(6000, 4))).argmax(1).astype(np.float64)
     w = rng.uniform(0.5, 1.5, 6000)
-    params = dict(n_estimators=3, learning_rate=0.3, max_depth=5, min_samples_leaf=3)
-    binned = mb.quantize_dense(x, 64)
-    ds = port.quantize_dense(x, 64)
+    params = dict(n_estimators=3, learning_rate=0.3, max_depth=5, min_samples_leaf=3, max_bins=max_bins)
+    binned = mb.quantize_dense(x, max_bins)
+    ds = port.quantize_dense(x, max_bins)
     model = mb.train_softmax(backend, binned, y, 4, w, **params)
     want = port.train_softmax(ds, y, 4, w, hist_mode=oracle.HIST_FIXED, **params)
     assert model.base_scores.tobytes() == want.base_scores.tobytes()
@@ -623,6 +625,9 @@ LEAFWISE_CASES = {
     "regularized": dict(seed=66, rows=3000, feats=5, nan=0.1, ints=1, max_bins=64,
                         params=dict(n_estimators=2, learning_rate=0.3, max_depth=5, max_leaves=10,
                                     reg_lambda=2.0, reg_alpha=0.2, min_child_weight=0.5, gamma=0.001)),
+    "wide_bins": dict(seed=68, rows=8000, feats=7, nan=0.05, ints=1, max_bins=1200,
+                      params=dict(n_estimators=2, learning_rate=0.3, max_depth=6, max_leaves=14,
+                                  min_samples_leaf=3)),
 }
 
 

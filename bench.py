@@ -348,7 +348,12 @@ def run_ours(args, rank, world):
     e2e = e2e_pageable = None
     if rank == 0 or world > 1:
         e2e = run_e2e(mb, backend, binned, y, w, args.e2e_trees, pinned=True)
-        e2e_pageable = run_e2e(mb, backend, binned, y, w, args.e2e_trees, pinned=False)
+        # Fits from pageable memory vary with the host's state between runs (0.74-0.97 s
+        # per 200-tree fit seen on the same build): the median of three fits.
+        fits = sorted((run_e2e(mb, backend, binned, y, w, args.e2e_trees, pinned=False) for _ in range(3)),
+                      key=lambda r: r["seconds"])
+        e2e_pageable = dict(fits[1], fits_seconds=[round(r["seconds"], 4) for r in fits],
+                            timing="median of three fits")
     trainer.close()
     secondary = run_secondary(mb, backend) if world == 1 and not args.no_secondary else None
 

@@ -27,6 +27,8 @@
 //    (the plain path): a u32 count and two FP32 reductions per cell.
 //  * The CTA flushes its non-empty cells into the node's global slot with 64-bit
 //    red.global adds (exact integer adds in fixed mode; FP64 adds in float mode).
+//  * Datasets with more than 256 histogram slots per feature (u16 bins) build with
+//    hist_build_wide_kernel, at the end of this file.
 #include <algorithm>
 #include <type_traits>
 

@@ -245,7 +245,10 @@ int mpsb_transform_dense(const void* data, int scalar_type, uint64_t rows, uint3
 
 /* ---- device-resident dataset ------------------------------------------------------ */
 /* bins: feature-major [features*rows], bin_width_bytes 1 or 2; missing may be NULL.
-   Each feature needs bin_count <= 256, and <= 255 when it has missing rows. */
+   Each feature needs 1 <= bin_count <= 65536, and <= 65535 when it has missing rows.
+   When every feature's bins and missing slot fit in 256 histogram slots the dataset keeps
+   u8 copies; otherwise (more than 256 bins, or 256 bins and missing rows) u16 copies and
+   the wide kernels (about twice the time per tree at 512 slots). */
 int mpsb_cuda_dataset_create(mpsb_cuda_backend* backend, const void* bins,
                              uint32_t bin_width_bytes, const uint8_t* missing,
                              uint64_t rows, uint32_t features, const uint32_t* bin_count,

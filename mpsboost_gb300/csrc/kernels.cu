@@ -747,7 +747,7 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
   ScanCand<FIXED>* s_queue = reinterpret_cast<ScanCand<FIXED>*>(
       smem_raw + (sizeof(SplitRec) + kScanHistBytes) * nwarps);
   static_assert(sizeof(SplitRec) % 8 == 0, "staged words and queue entries stay 8-byte aligned");
-  __shared__ uint32_t s_skip;
+  __shared__ uint32_t s_list[32], s_listed;  // two-phase exact launch: a batch's items to evaluate
   const TreeParams& P = a.params;
   const uint32_t n_chunks = a.n_fchunks;
   const uint32_t n_nodes = a.ctl->n_nodes;
@@ -758,30 +758,11 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
   const float lam32 = P.screen_lambda;
   const bool mcw_on = P.screen_mcw_on != 0;
   const float mcw_lo = P.screen_mcw_lo, mcw_hi = P.screen_mcw_hi;
-  for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) {
+  // The work on one (node, chunk) item; every thread of the CTA calls it.
+  auto eval_item = [&](uint32_t item) {
     const uint32_t i = item / n_chunks, c = item % n_chunks;
     const NodeRec node = a.nodes[parity][i];
     const uint32_t f = c * uint32_t(nwarps) + uint32_t(warp);
-    if (two_phase) {
-      if (threadIdx.x == 0) {
-        const uint32_t cs = a.chunk_screen[size_t(i) * n_chunks + c];
-        const float m = __uint_as_float(a.node_screen[i]);
-        s_skip = !(cs & kChunkExact) && m >= 1e-30f && __uint_as_float(cs) < m * (1.0f - 0x1p-18f);
-        if (s_skip) {
-          SplitRec none;
-          none.valid = 0;
-          none.gain = 0.0;
-          none.feature = c * uint32_t(nwarps);
-          none.threshold = 0;
-          none.default_left = 1;
-          a.partial[size_t(i) * n_chunks + c] = none;
-        }
-      }
-      __syncthreads();
-      const bool skip = s_skip != 0;
-      __syncthreads();
-      if (skip) continue;
-    }
     const double inv_g = a.trees[node.tree].inv_g, inv_h = a.trees[node.tree].inv_h;
     const int st_kg = a.trees[node.tree].kg, st_kh = a.trees[node.tree].kh;
     SplitRec best;
@@ -1139,6 +1120,44 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
       }
       __syncthreads();
     }
+  };
+  if (two_phase) {
+    // Batches of 32 consecutive items: warp 0 tests them against their nodes' final screen
+    // maxima, one lane each, writes "no split" for the chunks below the cut and lists the
+    // rest, which the CTA then evaluates in turn. At the deep levels most chunks are below
+    // the cut, and a CTA that tested them one at a time waited on a global load and two
+    // barriers per chunk.
+    const uint32_t n_batches = (items + 31u) / 32u;
+    for (uint32_t bt = blockIdx.x; bt < n_batches; bt += gridDim.x) {
+      if (warp == 0) {
+        const uint32_t item = bt * 32u + uint32_t(lane);
+        bool keep = false;
+        if (item < items) {
+          const uint32_t i = item / n_chunks, c = item % n_chunks;
+          const uint32_t cs = a.chunk_screen[size_t(i) * n_chunks + c];
+          const float m = __uint_as_float(a.node_screen[i]);
+          keep = (cs & kChunkExact) || !(m >= 1e-30f) || !(__uint_as_float(cs) < m * (1.0f - 0x1p-18f));
+          if (!keep) {
+            SplitRec none;
+            none.valid = 0;
+            none.gain = 0.0;
+            none.feature = c * uint32_t(nwarps);
+            none.threshold = 0;
+            none.default_left = 1;
+            a.partial[size_t(i) * n_chunks + c] = none;
+          }
+        }
+        const uint32_t ballot = __ballot_sync(0xffffffffu, keep);
+        if (keep) s_list[__popc(ballot & ((1u << lane) - 1u))] = item;
+        if (lane == 0) s_listed = uint32_t(__popc(ballot));
+      }
+      __syncthreads();
+      const uint32_t listed = s_listed;
+      for (uint32_t k = 0; k < listed; ++k) eval_item(s_list[k]);
+      __syncthreads();  // the list is rewritten by the next batch
+    }
+  } else {
+    for (uint32_t item = blockIdx.x; item < items; item += gridDim.x) eval_item(item);
   }
   (void)sizeof(V);
 }

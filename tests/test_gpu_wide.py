@@ -200,3 +200,38 @@ def test_wide_launch_shapes_build_the_same_trees(backend, monkeypatch):
         models.append(mb.train_regressor(backend, binned, y, w, **params))
     assert [t.tobytes() for t in models[0].trees] == [t.tobytes() for t in models[1].trees]
     assert models[0].train_predictions.tobytes() == models[1].train_predictions.tobytes()
+
+
+def test_wide_float_path_against_fp64_oracle(backend, port):
+    """The plain FP32 path on u16 bins (FP32 shared atomics, FP64 slot adds): the first
+    tree's structure matches the FP64 reference and the training RMSE is within 1e-4.
+    Leaves within 1e-3: a cell's FP32 sum over a work item's rows (thousands here) carries
+    relative errors near 1e-4 of the bin's absolute sum, which a leaf's cancelling
+    gradients can enlarge; the fixed-point path has no such error."""
+    x = seeded_matrix(66, 20000, 8, 0.05, 1)
+    y, w = _labels(x, 67)
+    params = dict(n_estimators=3, learning_rate=0.2, max_depth=5, min_samples_leaf=5)
+    binned = mb.quantize_dense(x, 1024)
+    ds = port.quantize_dense(x, 1024)
+    want = port.train_regressor(ds, y, w, hist_mode=oracle.HIST_FP64, **params)
+    model = mb.train_regressor(backend, binned, y, w, hist_mode="float", **params)
+    a = [tuple(int(n[k]) for k in _FIELDS) for n in model.trees[0]]
+    b = [tuple(int(n[k]) for k in _FIELDS) for n in want.trees[0]]
+    assert a == b
+    np.testing.assert_allclose(model.trees[0]["leaf_value"], want.trees[0]["leaf_value"], rtol=1e-3, atol=1e-7)
+    rmse = lambda p: float(np.sqrt(np.mean((p - y) ** 2)))  # noqa: E731
+    assert abs(rmse(model.train_predictions) - rmse(want.predict(ds))) <= 1e-4
+
+
+def test_wide_launch_paths_agree(backend):
+    """Batched graph, batched without graph and per-node launches give identical trees."""
+    x = seeded_matrix(68, 30000, 20, 0.05, 2)
+    y, w = _labels(x, 69)
+    binned = mb.quantize_dense(x, 700)
+    params = dict(n_estimators=3, learning_rate=0.1, max_depth=7, min_samples_leaf=2)
+    a = mb.train_regressor(backend, binned, y, w, **params)
+    b = mb.train_regressor(backend, binned, y, w, graph=False, **params)
+    c = mb.train_regressor(backend, binned, y, w, batched=False, **params)
+    for t1, t2, t3 in zip(a.trees, b.trees, c.trees):
+        assert t1.tobytes() == t2.tobytes() == t3.tobytes()
+    assert a.train_predictions.tobytes() == c.train_predictions.tobytes()

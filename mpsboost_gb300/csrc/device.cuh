@@ -95,6 +95,10 @@ struct NodeRec {
   double lo, hi;        // monotone bounds of the node's leaf value
   uint32_t tree;
   uint32_t depth;
+  // 0: the slot holds the node's histogram. k + 1: the slot still holds the parent's, and
+  // the level's first split-scan launch subtracts the built sibling's (slot k) from it,
+  // feature by feature as it scans them, and writes the difference back.
+  uint32_t sub_from;
 };
 
 // Best split of a node or of a (node, feature chunk); the SplitCandidate of

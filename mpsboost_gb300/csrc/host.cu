@@ -831,7 +831,7 @@ struct mpsb_cuda_trainer {
           CK(launch_root_cache(dev, root_gradient_only ? 0 : 1, grid(4), s)); ++k;
         }
         CK(launch_root_stats(dev, s)); ++k;
-      } else {
+      } else if (!dev.fused_sub) {
         CK(launch_subtract(dev, grid(8), s)); ++k;
       }
       if (depth > 0) {
@@ -1064,6 +1064,10 @@ void setup_trainer(mpsb_cuda_trainer* t, mpsb_cuda_backend* b, const mpsb_cuda_d
   a.bins_block_stride = kBlockFeatures;
   a.bins_fm = ds->bins_fm.as<uint8_t>();
   a.slots = ds->slots;
+  // Level-wise growth on u8 datasets: the split scan forms each sibling's histogram
+  // (MPSB_FUSED_SUB=0: subtract_kernel does).
+  a.fused_sub = ds->slots == uint32_t(kSlots) && p->growth_strategy != 1;
+  if (const char* v = std::getenv("MPSB_FUSED_SUB")) a.fused_sub = a.fused_sub && std::atoi(v) != 0;
   a.bins16 = ds->bins16.as<uint16_t>();
   a.bins16_fm = ds->bins16_fm.as<uint16_t>();
   a.bin_count = ds->bin_count.as<uint32_t>();

@@ -343,6 +343,7 @@ __global__ void round_setup_kernel(TrainerDev a) {
       r.hi = INFINITY;
       r.tree = t;
       r.depth = 0;
+      r.sub_from = 0;
       a.nodes[0][t] = r;
       for (uint32_t w = 0; w < a.params.path_words; ++w) {
         uint32_t allowed = 0xffffffffu;
@@ -708,6 +709,63 @@ __device__ __forceinline__ void stage_feature_hist(const unsigned long long* src
   __syncwarp();
 }
 
+// stage_feature_hist of a sibling's histogram, formed on the way: parent minus the built
+// child word by word, with subtract_kernel's checks (count underflow; float mode: finite
+// sums, non-negative hessians, the hessian difference clamped at 0 within 1e-5), and
+// written back over the parent's words in the same 16-byte chunks.
+template <bool FIXED>
+__device__ __forceinline__ void stage_sibling_hist(unsigned long long* parent,
+                                                   const unsigned long long* built,
+                                                   unsigned long long* dst, int lane, uint32_t& err) {
+  constexpr int kChunks = int(kScanHistBytes / 16);  // 384
+  constexpr int kPerLane = kChunks / 32;              // 12
+  constexpr int kBatch = 4;
+  ulonglong2* p2 = reinterpret_cast<ulonglong2*>(parent);
+  const ulonglong2* c2 = reinterpret_cast<const ulonglong2*>(built);
+#pragma unroll 1
+  for (int part = 0; part < kPerLane / kBatch; ++part) {
+    ulonglong2 pv[kBatch], cv[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      pv[j] = p2[(part * kBatch + j) * 32 + lane];
+      cv[j] = c2[(part * kBatch + j) * 32 + lane];
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const uint32_t w0 = uint32_t((part * kBatch + j) * 32 + lane) * 2u;
+      unsigned long long out[2];
+#pragma unroll
+      for (uint32_t q = 0; q < 2; ++q) {
+        const unsigned long long pw = q ? pv[j].y : pv[j].x, cw = q ? cv[j].y : cv[j].x;
+        const uint32_t w = w0 + q, word = w % 3u;
+        unsigned long long r;
+        if (word == 0 || FIXED) {
+          if (word == 0 && cw > pw) err |= kErrSubtraction;
+          r = pw - cw;
+        } else {
+          const double pd = __longlong_as_double((long long)pw), cd = __longlong_as_double((long long)cw);
+          if (word == 1) {
+            const double g = __dadd_rn(pd, -cd);
+            if (!isfinite(pd) || !isfinite(cd) || !isfinite(g)) err |= kErrNonFinite;
+            r = (unsigned long long)__double_as_longlong(g);
+          } else {
+            if (!isfinite(pd) || !isfinite(cd) || pd < 0.0 || cd < 0.0) err |= kErrHessian;
+            const double diff = __dadd_rn(pd, -cd);
+            const double tol = __dmul_rn(1e-5, fmax(1.0, fmax(fabs(pd), fabs(cd))));
+            if (diff < -tol) err |= kErrSubtraction;
+            r = (unsigned long long)__double_as_longlong(diff < 0.0 ? 0.0 : diff);
+          }
+        }
+        out[q] = r;
+        const uint32_t slot = w / 3u;
+        dst[(word * 8u + (slot & 7u)) * 32u + (slot >> 3)] = r;
+      }
+      p2[(part * kBatch + j) * 32 + lane] = make_ulonglong2(out[0], out[1]);
+    }
+  }
+  __syncwarp();
+}
+
 // Bit 31 of a chunk's screen word: some feature of the chunk is evaluated exactly whatever
 // the node's maximum (its screen is off, or a candidate is too close to call in FP32).
 // The low bits hold the chunk's best certainly admissible FP32 score (a non-negative
@@ -753,6 +811,8 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
   const uint32_t n_nodes = a.ctl->n_nodes;
   const uint32_t items = n_nodes * n_chunks;
   const bool two_phase = !SCREEN && a.node_screen != nullptr && a.scan_two_phase != 0;
+  // The level's first launch forms the siblings' histograms (u8 datasets).
+  const bool fuse_sub = !WIDE && a.fused_sub != 0 && (SCREEN || !two_phase);
   // Launch-wide screen constants (FP64 tests and conversions stay out of the item loop).
   const bool screen_params = P.screen_params != 0;
   const float lam32 = P.screen_lambda;
@@ -838,7 +898,13 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
           page_sums(p + 1 == pages, unused, miss, total_count);
         }
       } else {
-        stage_feature_hist(fhist, sh, lane);
+        if (fuse_sub && node.sub_from != 0) {
+          stage_sibling_hist<FIXED>(a.hist + (size_t(node.slot) * a.features + f) * kSlots * 3,
+                                    a.hist + (size_t(node.sub_from - 1) * a.features + f) * kSlots * 3, sh,
+                                    lane, err);
+        } else {
+          stage_feature_hist(fhist, sh, lane);
+        }
         Stat<FIXED> sum = stat_zero<FIXED>();
         page_sums(true, sum, miss, total_count);
         carry_in = exclusive_of(inclusive_prefix(sum));
@@ -1407,6 +1473,10 @@ __global__ void __launch_bounds__(1024) finalize_kernel(TrainerDev a, int parity
         R.hi = b.ru;
         L.tree = R.tree = t;
         L.depth = R.depth = node.depth + 1;
+        // The sibling of the built child keeps the parent's slot; u8 datasets subtract in
+        // the next level's split scan (fused_sub), wide ones with subtract_kernel.
+        L.sub_from = (a.fused_sub && !build_left) ? new_slot + 1 : 0;
+        R.sub_from = (a.fused_sub && build_left) ? new_slot + 1 : 0;
         next[2 * k] = L;
         next[2 * k + 1] = R;
         for (uint32_t w = 0; w < W; ++w) {
@@ -1841,6 +1911,7 @@ __global__ void __launch_bounds__(1024) leafwise_select_kernel(TrainerDev a) {
           n.hi = left ? b.lu : b.ru;
           n.tree = t;
           n.depth = depth;
+          n.sub_from = 0;  // leaf-wise steps subtract with subtract_kernel
           kid[k].best = no_split();
           kid[k].parity = np;
           kid[k].scanned = grow ? 0u : 1u;

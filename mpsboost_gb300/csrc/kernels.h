@@ -102,6 +102,8 @@ struct TrainerDev {
                                 // preds holds the margins [K][n_rows] and the round
                                 // counter modulo K is the class of the current tree
   uint32_t scan_threads;        // block size of the split scan (multiple of 32)
+  uint32_t fused_sub;           // level-wise siblings are subtracted by the split scan
+                                // (NodeRec::sub_from), not by subtract_kernel
   // finalize scratch
   uint32_t* scratch_flags;      // [max_level_nodes]
   uint32_t* scratch_prefix;     // [max_level_nodes] valid-prefix, then accepted-prefix

@@ -674,3 +674,32 @@ def test_leafwise_active_queue_limit(backend, port):
         port.train_regressor(port.quantize_dense(x, 32), y, w, hist_mode=oracle.HIST_FIXED, **params)
     with pytest.raises(mb.TrainingError, match="max_active_leaves"):
         mb.train_regressor(backend, mb.quantize_dense(x, 32), y, w, **params)
+
+
+@pytest.mark.parametrize("variant", ["weighted", "forest", "interaction"])
+def test_fused_sibling_subtraction_equals_subtract_kernel(backend, monkeypatch, variant):
+    """Siblings' histograms formed inside the split scan (the default for level-wise growth
+    on u8 bins) and by subtract_kernel (MPSB_FUSED_SUB=0) give byte-identical fixed-point
+    models, with forest feature masks and interaction constraints (features a node may not
+    split on are skipped). The plain float path's fused subtraction is covered against the
+    FP64 oracle by test_float_path_against_reference (its FP32 atomics do not repeat bit for
+    bit between fits)."""
+    x, y, w = _data(81, 20000, 24, 0.05, 3)
+    binned = mb.quantize_dense(x, 255)
+    params = dict(n_estimators=3, learning_rate=0.2, max_depth=7, min_samples_leaf=3)
+    if variant == "interaction":
+        params["interaction_constraints"] = [[0, 1, 2, 3], [3, 4, 5, 6, 7], list(range(8, 24))]
+
+    def fit():
+        if variant == "forest":
+            counts, subsets, seeds = mb.forest_samples(20000, 24, 6, random_state=3, max_features=0.5)
+            return mb.train_forest(backend, binned, y, w, row_counts=counts, feature_subsets=subsets,
+                                   seeds=seeds, max_depth=7, min_samples_leaf=3)
+        return [mb.train_regressor(backend, binned, y, w, **params)]
+
+    monkeypatch.setenv("MPSB_FUSED_SUB", "1")
+    fused = fit()
+    monkeypatch.setenv("MPSB_FUSED_SUB", "0")
+    separate = fit()
+    for a, b in zip(fused, separate):
+        assert [t.tobytes() for t in a.trees] == [t.tobytes() for t in b.trees]

@@ -713,6 +713,28 @@ __device__ __forceinline__ void stage_feature_hist(const unsigned long long* src
 // child word by word, with subtract_kernel's checks (count underflow; float mode: finite
 // sums, non-negative hessians, the hessian difference clamped at 0 within 1e-5), and
 // written back over the parent's words in the same 16-byte chunks.
+// One word of a sibling's slot: parent minus built child, with subtract_kernel's checks
+// (word 0 count, 1 g, 2 h).
+template <bool FIXED>
+__device__ __forceinline__ unsigned long long sibling_word(unsigned long long pw, unsigned long long cw,
+                                                           uint32_t word, uint32_t& err) {
+  if (word == 0 || FIXED) {
+    if (word == 0 && cw > pw) err |= kErrSubtraction;
+    return pw - cw;
+  }
+  const double pd = __longlong_as_double((long long)pw), cd = __longlong_as_double((long long)cw);
+  if (word == 1) {
+    const double g = __dadd_rn(pd, -cd);
+    if (!isfinite(pd) || !isfinite(cd) || !isfinite(g)) err |= kErrNonFinite;
+    return (unsigned long long)__double_as_longlong(g);
+  }
+  if (!isfinite(pd) || !isfinite(cd) || pd < 0.0 || cd < 0.0) err |= kErrHessian;
+  const double diff = __dadd_rn(pd, -cd);
+  const double tol = __dmul_rn(1e-5, fmax(1.0, fmax(fabs(pd), fabs(cd))));
+  if (diff < -tol) err |= kErrSubtraction;
+  return (unsigned long long)__double_as_longlong(diff < 0.0 ? 0.0 : diff);
+}
+
 template <bool FIXED>
 __device__ __forceinline__ void stage_sibling_hist(unsigned long long* parent,
                                                    const unsigned long long* built,
@@ -738,30 +760,49 @@ __device__ __forceinline__ void stage_sibling_hist(unsigned long long* parent,
       for (uint32_t q = 0; q < 2; ++q) {
         const unsigned long long pw = q ? pv[j].y : pv[j].x, cw = q ? cv[j].y : cv[j].x;
         const uint32_t w = w0 + q, word = w % 3u;
-        unsigned long long r;
-        if (word == 0 || FIXED) {
-          if (word == 0 && cw > pw) err |= kErrSubtraction;
-          r = pw - cw;
-        } else {
-          const double pd = __longlong_as_double((long long)pw), cd = __longlong_as_double((long long)cw);
-          if (word == 1) {
-            const double g = __dadd_rn(pd, -cd);
-            if (!isfinite(pd) || !isfinite(cd) || !isfinite(g)) err |= kErrNonFinite;
-            r = (unsigned long long)__double_as_longlong(g);
-          } else {
-            if (!isfinite(pd) || !isfinite(cd) || pd < 0.0 || cd < 0.0) err |= kErrHessian;
-            const double diff = __dadd_rn(pd, -cd);
-            const double tol = __dmul_rn(1e-5, fmax(1.0, fmax(fabs(pd), fabs(cd))));
-            if (diff < -tol) err |= kErrSubtraction;
-            r = (unsigned long long)__double_as_longlong(diff < 0.0 ? 0.0 : diff);
-          }
-        }
+        const unsigned long long r = sibling_word<FIXED>(pw, cw, word, err);
         out[q] = r;
         const uint32_t slot = w / 3u;
         dst[(word * 8u + (slot & 7u)) * 32u + (slot >> 3)] = r;
       }
       p2[(part * kBatch + j) * 32 + lane] = make_ulonglong2(out[0], out[1]);
     }
+  }
+  __syncwarp();
+}
+
+// A feature with at most 32 bins: its slots 0-31 staged one per lane (slot l's words at
+// dst[(w * 8) * 32 + l]) and its missing slot returned in *miss_words (every lane). All
+// other slots are empty: every bin is below the feature's bin count. sub: parent minus the
+// built child (`built`), written back as stage_sibling_hist does.
+template <bool FIXED>
+__device__ __forceinline__ void stage_few_slots(unsigned long long* slot_hist,
+                                                const unsigned long long* built, bool hm,
+                                                unsigned long long* dst, int lane,
+                                                unsigned long long* miss_words, uint32_t& err) {
+#pragma unroll
+  for (uint32_t w = 0; w < 3; ++w) {
+    const size_t at = size_t(lane) * 3 + w;
+    unsigned long long v = slot_hist[at];
+    if (built) {
+      v = sibling_word<FIXED>(v, built[at], w, err);
+      slot_hist[at] = v;
+    }
+    dst[(w * 8u) * 32u + uint32_t(lane)] = v;
+  }
+#pragma unroll
+  for (uint32_t w = 0; w < 3; ++w) {
+    const size_t at = size_t(kMissingSlot) * 3 + w;
+    unsigned long long v = 0;
+    if (hm) {
+      v = slot_hist[at];
+      if (built) {
+        v = sibling_word<FIXED>(v, built[at], w, err);
+        __syncwarp();
+        if (lane == 0) slot_hist[at] = v;
+      }
+    }
+    miss_words[w] = v;
   }
   __syncwarp();
 }
@@ -843,19 +884,25 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
     if (active) {  // warp-uniform
       const uint32_t nb = a.bin_count[f];
       const bool hm = a.has_missing[f] != 0;
+      // At most 32 bins: one slot per lane (slot = lane), the missing slot apart.
+      const bool few = !WIDE && nb <= 32u;
+      const int kper = few ? 1 : 8;
       unsigned long long* sh = s_hist + size_t(warp) * (kScanHistBytes / 8);
       const uint32_t pages = WIDE ? a.slots / uint32_t(kSlots) : 1u;
       const unsigned long long* fhist =
           a.hist + (size_t(node.slot) * a.features + f) * size_t(WIDE ? a.slots : uint32_t(kSlots)) * 3;
-      // Slot lane * 8 + k of the staged page: word w at sh[(w * 8 + k) * 32 + lane].
+      // Slot lane * 8 + k of the staged page (few bins: slot lane, k = 0): word w at
+      // sh[(w * 8 + k) * 32 + lane].
       auto slot_word = [&](int k, int w) -> unsigned long long { return sh[(w * 8 + k) * 32 + lane]; };
+      auto slot_of = [&](int k) -> int { return few ? lane : lane * 8 + k; };
       // The lane's total of its 8 slots of the staged page; the missing slot (slot
       // kMissingSlot of the last page) goes to `miss` instead. Raw counts add to `count`.
       auto page_sums = [&](bool last, Stat<FIXED>& sum, Stat<FIXED>& miss,
                            unsigned long long& count) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-          const int s = lane * 8 + k;
+          if (k >= kper) break;
+          const int s = slot_of(k);
           Stat<FIXED> b;
           const unsigned long long raw_count = slot_word(k, 0);
           b.count = uint32_t(raw_count);  // the total below checks the full word
@@ -898,18 +945,35 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
           page_sums(p + 1 == pages, unused, miss, total_count);
         }
       } else {
-        if (fuse_sub && node.sub_from != 0) {
-          stage_sibling_hist<FIXED>(a.hist + (size_t(node.slot) * a.features + f) * kSlots * 3,
-                                    a.hist + (size_t(node.sub_from - 1) * a.features + f) * kSlots * 3, sh,
-                                    lane, err);
+        const bool sub = fuse_sub && node.sub_from != 0;
+        unsigned long long* own = a.hist + (size_t(node.slot) * a.features + f) * kSlots * 3;
+        const unsigned long long* built =
+            sub ? a.hist + (size_t(node.sub_from - 1) * a.features + f) * kSlots * 3 : nullptr;
+        unsigned long long mw[3] = {0ull, 0ull, 0ull};
+        if (few) {
+          stage_few_slots<FIXED>(own, built, hm, sh, lane, mw, err);
+        } else if (sub) {
+          stage_sibling_hist<FIXED>(own, built, sh, lane, err);
         } else {
           stage_feature_hist(fhist, sh, lane);
         }
         Stat<FIXED> sum = stat_zero<FIXED>();
         page_sums(true, sum, miss, total_count);
         carry_in = exclusive_of(inclusive_prefix(sum));
+        if (few) {  // the missing slot, in every lane; its rows counted once
+          miss.count = uint32_t(mw[0]);
+          if constexpr (FIXED) {
+            miss.g = (long long)mw[1];
+            miss.h = (long long)mw[2];
+          } else {
+            miss.g = __longlong_as_double((long long)mw[1]);
+            miss.h = __longlong_as_double((long long)mw[2]);
+            if (!isfinite(miss.g) || !isfinite(miss.h) || miss.h < 0.0) err |= kErrNonFinite;
+          }
+          if (lane == 0) total_count += mw[0];
+        }
       }
-      miss = shfl_stat<FIXED>(miss, 31);
+      if (!few) miss = shfl_stat<FIXED>(miss, 31);
       for (int off = 16; off > 0; off >>= 1)
         total_count += __shfl_xor_sync(0xffffffffu, total_count, off);
       if (total_count != node.count) err |= kErrCountMismatch;
@@ -1002,8 +1066,8 @@ __global__ void __launch_bounds__(kScanThreadsMax) split_scan_kernel(TrainerDev 
         auto scan_candidates = [&](const Stat<FIXED>& cin, uint32_t base, bool last, auto&& visit) {
           Stat<FIXED> left = cin;
 #pragma unroll 1
-          for (int k = 0; k < 8; ++k) {
-            const int s = lane * 8 + k;
+          for (int k = 0; k < kper; ++k) {
+            const int s = slot_of(k);
             bool empty_bin = false;
             if (!(hm && last && s == kMissingSlot)) {  // reload the slot from the staging area
               Stat<FIXED> b;

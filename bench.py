@@ -8,6 +8,8 @@ min_samples_leaf 20, min_child_weight 1, reg_lambda 1. A step is one boosting ro
 (one tree). Data are seeded synthetic inputs of that shape and distribution.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --only-train [--rows R] [--max-bins B] [--no-autotune]   (rounds only)
+  python bench.py --workload logistic | forest                            (other configurations)
 
 Our arm prints one JSON line with the whole-job trees/s measured with CUDA events on the
 backend stream (inputs resident in HBM), an end-to-end figure through the C ABI from

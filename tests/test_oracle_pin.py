@@ -140,25 +140,27 @@ def test_gradients_match_reference(port, reference):
         assert port.gradients(obj, y, p, 0.3, 1.4).tobytes() == reference.gradients(obj, y, p, 0.3, 1.4).tobytes()
 
 
-@pytest.mark.parametrize("nan,weighted,max_leaves", [(0.0, False, 0), (0.08, True, 0), (0.03, True, 5)])
-def test_softmax_port_matches_reference(port, reference, nan, weighted, max_leaves):
+@pytest.mark.parametrize("nan,weighted,max_leaves,max_bins", [(0.0, False, 0, 32), (0.08, True, 0, 32),
+                                                             (0.03, True, 5, 32), (0.05, True, 0, 400)])
+def test_softmax_port_matches_reference(port, reference, nan, weighted, max_leaves, max_bins):
     """TrainMulticlassSoftmaxModel: base scores, every (round, class) tree and the margins
-    bit for bit (both sides take exp and log from the same libm)."""
+    bit for bit (both sides take exp and log from the same libm); 400 bins: u16 storage."""
     rng = np.random.default_rng(int(nan * 100) + max_leaves)
     x = rng.normal(size=(500, 5)).astype(np.float32)
     x[rng.random(x.shape) < nan] = np.nan
     scores = np.nan_to_num(x) @ rng.normal(size=(5, 3)) + rng.gumbel(size=(500, 3))
     y = scores.argmax(axis=1).astype(np.float64)
     w = rng.uniform(0.5, 1.5, 500) if weighted else None
-    params = dict(n_estimators=3, learning_rate=0.3, max_depth=4, min_samples_leaf=2, max_leaves=max_leaves)
-    a = port.train_softmax(port.quantize_dense(x, 32), y, 3, w, **params)
-    ds = reference.quantize_dense(x, 32)
+    params = dict(n_estimators=3, learning_rate=0.3, max_depth=4, min_samples_leaf=2, max_leaves=max_leaves,
+                  max_bins=max_bins)
+    a = port.train_softmax(port.quantize_dense(x, max_bins), y, 3, w, **params)
+    ds = reference.quantize_dense(x, max_bins)
     b = reference.train_softmax(ds, y, 3, w, **params)
     assert a.base_scores.tobytes() == b.base_scores.tobytes()
     assert len(a.trees) == len(b.trees) == 9
     for t1, t2 in zip(a.trees, b.trees):
         assert t1.tobytes() == t2.tobytes()
-    assert a.predict_margins(port.quantize_dense(x, 32)).tobytes() == b.predict_margins(ds).tobytes()
+    assert a.predict_margins(port.quantize_dense(x, max_bins)).tobytes() == b.predict_margins(ds).tobytes()
 
 
 LEAFWISE = [dict(max_depth=6, max_leaves=12), dict(max_depth=4), dict(max_depth=8, max_leaves=20, min_samples_leaf=5),
@@ -166,22 +168,23 @@ LEAFWISE = [dict(max_depth=6, max_leaves=12), dict(max_depth=4), dict(max_depth=
             dict(max_depth=6, max_leaves=16, max_active_leaves=16, interaction_constraints=[[0, 1], [1, 2, 3], [4, 5]])]
 
 
+@pytest.mark.parametrize("max_bins", [32, 600])
 @pytest.mark.parametrize("case", range(len(LEAFWISE)))
-def test_leafwise_port_matches_reference(port, reference, case):
+def test_leafwise_port_matches_reference(port, reference, case, max_bins):
     """TrainLeafWiseRegressionTree in FP64, bit for bit (including the reference's rebuild
-    of a histogram whose step-best candidate was superseded)."""
+    of a histogram whose step-best candidate was superseded); 600 bins: u16 storage."""
     rng = np.random.default_rng(5)
     x = rng.normal(size=(800, 6)).astype(np.float32)
     x[rng.random(x.shape) < 0.05] = np.nan
     y = np.nan_to_num(x[:, 0]) * 2 + np.nan_to_num(x[:, 1]) * np.nan_to_num(x[:, 2]) + rng.normal(size=800) * 0.1
     w = rng.uniform(0.5, 1.5, 800)
-    params = dict(LEAFWISE[case], n_estimators=3, learning_rate=0.3, growth_strategy="leaf_wise")
-    a = port.train_regressor(port.quantize_dense(x, 32), y, w, **params)
-    ds = reference.quantize_dense(x, 32)
+    params = dict(LEAFWISE[case], n_estimators=3, learning_rate=0.3, growth_strategy="leaf_wise", max_bins=max_bins)
+    a = port.train_regressor(port.quantize_dense(x, max_bins), y, w, **params)
+    ds = reference.quantize_dense(x, max_bins)
     b = reference.train_regressor(ds, y, w, **params)
     for t1, t2 in zip(a.trees, b.trees):
         assert t1.tobytes() == t2.tobytes()
-    assert a.predict(port.quantize_dense(x, 32)).tobytes() == b.predict(ds).tobytes()
+    assert a.predict(port.quantize_dense(x, max_bins)).tobytes() == b.predict(ds).tobytes()
 
 
 def test_dataset_from_bins_equals_quantized(port):

@@ -69,6 +69,9 @@ def main():
                          objective="binary_logistic", min_samples_leaf=2)),
         dict(seed=8, rows=90, feats=2, nan=0.0, ints=0, max_bins=16,
              params=dict(n_estimators=2, learning_rate=0.3, max_depth=6, max_leaves=5)),
+        # u16 storage (max_bins above 256) with missing values.
+        dict(seed=9, rows=420, feats=3, nan=0.05, ints=0, max_bins=300,
+             params=dict(n_estimators=2, learning_rate=0.3, max_depth=4, min_samples_leaf=2)),
     ]
     for cfg in configs:
         x = matrix(cfg["seed"], cfg["rows"], cfg["feats"], cfg["nan"], cfg["ints"])

@@ -151,7 +151,7 @@ def _cases():
         return json.load(fh)["cases"]
 
 
-@pytest.mark.parametrize("index", range(8))
+@pytest.mark.parametrize("index", range(9))
 def test_reference_cases(port, index):
     case = _cases()[index]
     x = np.array([[np.nan if v is None else _hex(v) for v in row] for row in case["x"]], np.float32)

@@ -218,3 +218,21 @@ def test_dataset_from_bins_equals_quantized(port):
     Given.bins[f, row] = Given.bin_counts[f]
     with pytest.raises(oracle.OracleError, match="exceeds"):
         port.dataset_from_bins(Given)
+
+
+def test_fp64_missing_check_trips_on_logistic_configuration(port, reference):
+    """On the binary-logistic configuration's data (256 features, 10 % missing cells, depth
+    10), the reference's FP64 trainer stops with its own consistency check
+    (tree_split.cpp:186-189: a node's missing-row hessian sum, added in another order than
+    the node's total, exceeds it by rounding), and the port stops the same way. The
+    fixed-point path sums exactly and trains this configuration (the GPU tests compare it
+    with the fixed-point replica)."""
+    import bench
+
+    x, y = bench.make_logistic_data(200_000)
+    params = dict(n_estimators=2, max_depth=10, learning_rate=0.1, objective="binary_logistic")
+    for o, kw in ((reference, {}), (port, dict(hist_mode=oracle.HIST_FP64))):
+        with pytest.raises(oracle.OracleError, match="missing statistics exceed parent"):
+            o.train_regressor(o.quantize_dense(x, 255), y, None, **kw, **params)
+    model = port.train_regressor(port.quantize_dense(x, 255), y, None, hist_mode=oracle.HIST_FIXED, **params)
+    assert len(model.trees) == 2

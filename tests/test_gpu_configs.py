@@ -221,4 +221,3 @@ def test_config4_forest(backend, port):
     for t, (m, (base, nodes)) in enumerate(zip(models, wants)):
         assert float(m.base_score).hex() == float(base).hex(), t
         assert m.trees[0].tobytes() == nodes.tobytes(), t
-

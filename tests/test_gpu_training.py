@@ -360,7 +360,7 @@ def test_direct_loads_equal_staged_builds(backend, port, monkeypatch, threads, w
     """Register-direct histogram builds (the trainer's default: each lane loads its row's
     32 bin bytes with one 256-bit load, no shared-memory staging, flush by TMA bulk
     reductions) give the staged kernel's trees bit for bit (MPSB_HIST_DIRECT=0), and the
-    replica's. Weighted squared error builds five limbs and, from round 2, gradient-only
+    replica's. Weighted squared error builds five limbs and, from the second boosting round, gradient-only
     roots; unweighted builds count and gradient limbs (unit hessian). Depth 9 with 70
     features (a partial feature block), 40,000 rows (dense and sparse nodes, partial row
     groups) and missing values."""
